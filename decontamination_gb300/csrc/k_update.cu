@@ -1,0 +1,328 @@
+// Training-side kernels: per-BMU segmented sums, the neighbourhood contraction with the divide, iteration
+// mode, and the plain divide.
+//
+// The reference scatters every sample into every unit with float32 atomics
+// (algo/som_batch.py:552-566): num_j += rho*exp(-|t_j - t_b|^2/(2 sigma^2))*x, N*M*(D+1) atomics per epoch.
+// Because the factor depends on the sample only through its BMU b, the same sums factor exactly as
+//   num = H.S, den = H.c,  S_b = sum_{i: bmu_i = b} rho_i x_i,  c_b = sum_{i: bmu_i = b} rho_i,
+// so an epoch needs N*(D+1) additions into M*(D+1) float64 bins plus an M x M x (D+1) contraction.
+#include "common.cuh"
+
+namespace somgb {
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------------------------------
+// Segmented sums. CTA (chunk, range) owns the bins of units [lo, lo+cnt) in shared memory (float64) and adds every
+// sample of its chunk whose BMU falls in its range; at the end it flushes the non-zero bins with one float64 atomic
+// each. Ranges exist only when M*(D+1) float64 bins exceed one CTA's shared memory.
+// ---------------------------------------------------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(256) accumulate_kernel(const T* __restrict__ x, const double* __restrict__ rho,
+                                                         const int32_t* __restrict__ bmu, int64_t n, int d,
+                                                         int64_t units_per_range, int64_t m, int64_t chunk,
+                                                         double* __restrict__ S, double* __restrict__ c) {
+    extern __shared__ double bins[];   // cnt x (d + 1)
+    const int64_t lo = (int64_t)blockIdx.y * units_per_range;
+    const int64_t cnt = min64(units_per_range, m - lo);
+    const int stride = d + 1;
+    for (int64_t q = threadIdx.x; q < cnt * stride; q += blockDim.x) bins[q] = 0.0;
+    __syncthreads();
+    const int64_t s0 = (int64_t)blockIdx.x * chunk;
+    const int64_t s1 = min64(n, s0 + chunk);
+    for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+        const int32_t b = bmu[i];
+        if (b < lo || b >= lo + cnt) continue;   // also skips b == -1
+        double r = rho ? rho[i] : 1.0;
+        if (sizeof(T) == 4) r = (double)(float)r;  // the training density is cast to the map dtype (som_batch.py:312)
+        double* bin = bins + (b - lo) * stride;
+        const T* xr = x + i * d;
+        for (int k = 0; k < d; ++k) atomicAdd(bin + k, r * (double)xr[k]);
+        atomicAdd(bin + d, r);
+    }
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < cnt * stride; q += blockDim.x) {
+        const double v = bins[q];
+        if (v == 0.0) continue;
+        const int64_t u = lo + q / stride;
+        const int k = (int)(q % stride);
+        if (k < d) atomicAdd(S + u * d + k, v);
+        else atomicAdd(c + u, v);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------------
+// Neighbourhood contraction: one CTA per unit j, threads stride over the source units b with a non-empty BMU bin.
+// h_jb = exp(-|t_j - t_b|^2 * inv2s2) with |t_j - t_b|^2 typed as the reference types it (float32 differences and
+// squares, float64 sum), exp in float64 (algo/som_batch.py:548-556).
+// ---------------------------------------------------------------------------------------------------------------------
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(256) neighbourhood_kernel(const double* __restrict__ S, const double* __restrict__ c,
+                                                            const T* __restrict__ topo, int64_t m, int d,
+                                                            double inv2s2, T* __restrict__ w_out,
+                                                            double* __restrict__ num_out,
+                                                            double* __restrict__ den_out) {
+    const int64_t j = blockIdx.x;
+    double acc[DMAX + 1];
+#pragma unroll
+    for (int k = 0; k <= DMAX; ++k) acc[k] = 0.0;
+    for (int64_t b = threadIdx.x; b < m; b += blockDim.x) {
+        const double cb = c[b];
+        if (cb == 0.0) continue;
+        const double h = exp(-topo_sqdist(topo, j, b) * inv2s2);
+        const double* Sb = S + b * d;
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k)
+            if (k < d) acc[k] = fma(h, Sb[k], acc[k]);
+        acc[DMAX] = fma(h, cb, acc[DMAX]);
+    }
+    __shared__ double red[DMAX + 1][8];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k <= DMAX; ++k) {
+        if (k < d || k == DMAX) {
+            double v = acc[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[k][wid] = v;
+        }
+    }
+    __syncthreads();
+    __shared__ double den_s;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[DMAX][q];
+        den_s = s;
+        if (den_out) den_out[j] = s;
+    }
+    __syncthreads();
+    const double den = den_s;
+    for (int k = threadIdx.x; k < d; k += blockDim.x) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[k][q];
+        if (num_out) num_out[j * d + k] = s;
+        w_out[j * d + k] = den > FLOAT_EPS ? (T)(s / den) : (T)0;
+    }
+}
+
+// Large D: the per-thread accumulators live in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(128) neighbourhood_wide_kernel(const double* __restrict__ S,
+                                                                 const double* __restrict__ c,
+                                                                 const T* __restrict__ topo, int64_t m, int d,
+                                                                 double inv2s2, T* __restrict__ w_out,
+                                                                 double* __restrict__ num_out,
+                                                                 double* __restrict__ den_out) {
+    extern __shared__ double hs[];   // blockDim.x factors
+    __shared__ double den_s;
+    const int64_t j = blockIdx.x;
+    double den_part = 0.0;
+    // pass 1: den
+    for (int64_t b = threadIdx.x; b < m; b += blockDim.x) {
+        const double cb = c[b];
+        if (cb != 0.0) den_part = fma(exp(-topo_sqdist(topo, j, b) * inv2s2), cb, den_part);
+    }
+    for (int o = 16; o > 0; o >>= 1) den_part += __shfl_xor_sync(0xffffffffu, den_part, o);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = den_part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+        den_s = s;
+        if (den_out) den_out[j] = s;
+    }
+    __syncthreads();
+    const double den = den_s;
+    // pass 2: every thread owns features k = tid, tid + blockDim, ...; factors are staged per block of units
+    for (int k0 = 0; k0 < d; k0 += blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        double acc = 0.0;
+        for (int64_t b0 = 0; b0 < m; b0 += blockDim.x) {
+            __syncthreads();
+            const int64_t b = b0 + threadIdx.x;
+            hs[threadIdx.x] = (b < m && c[b] != 0.0) ? exp(-topo_sqdist(topo, j, b) * inv2s2) : 0.0;
+            __syncthreads();
+            const int64_t nb = min64(blockDim.x, m - b0);
+            if (k < d)
+                for (int64_t q = 0; q < nb; ++q) acc = fma(hs[q], S[(b0 + q) * d + k], acc);
+        }
+        if (k < d) {
+            if (num_out) num_out[j * d + k] = acc;
+            w_out[j * d + k] = den > FLOAT_EPS ? (T)(acc / den) : (T)0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------------
+// Iteration mode (algo/som_batch.py:154-210): every sample has its own radius, so the update does not factor through
+// per-BMU sums. CTA (unit tile, sample chunk): each thread owns one unit and accumulates over the chunk; samples are
+// staged in shared memory.
+// ---------------------------------------------------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(128) iter_kernel(const T* __restrict__ x, const double* __restrict__ rho,
+                                                   const int32_t* __restrict__ bmu, int64_t n, int d,
+                                                   const T* __restrict__ topo, int64_t m, double sigma0,
+                                                   int64_t cur_vector, int64_t n_vectors, int64_t chunk,
+                                                   double* __restrict__ num, double* __restrict__ den) {
+    constexpr int SB = 32;                       // samples staged per round
+    extern __shared__ double sm[];               // SB x d samples, then SB factors info
+    double* xs = sm;
+    double* inv_s = sm + SB * d;
+    double* r_s = inv_s + SB;
+    int* b_s = (int*)(r_s + SB);
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t s0 = (int64_t)blockIdx.y * chunk;
+    const int64_t s1 = min64(n, s0 + chunk);
+    double dacc = 0.0;
+    // per-thread numerator partials are kept in global memory order: one pass per feature block of 8
+    for (int k0 = 0; k0 < d; k0 += 8) {
+        double acc[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+        for (int64_t i0 = s0; i0 < s1; i0 += SB) {
+            __syncthreads();
+            const int nb = (int)min64(SB, s1 - i0);
+            for (int q = threadIdx.x; q < nb * d; q += blockDim.x) xs[q] = (double)x[i0 * d + q];
+            for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+                const int64_t i = i0 + q;
+                double r = rho ? rho[i] : 1.0;
+                if (sizeof(T) == 4) r = (double)(float)r;
+                // sigma_i = sigma0 * 1/(1 + 2 (cur + i)/n_vectors), clamped (som_batch.py:167-170)
+                double sg = sigma0 * (1.0 / (1.0 + 2.0 * (double)(cur_vector + i) / (double)n_vectors));
+                if (sg < FLOAT_EPS) sg = FLOAT_EPS;
+                inv_s[q] = 1.0 / (2.0 * sg * sg);
+                r_s[q] = r;
+                b_s[q] = bmu[i];
+            }
+            __syncthreads();
+            if (j < m) {
+                for (int q = 0; q < nb; ++q) {
+                    const int b = b_s[q];
+                    if (b < 0) continue;
+                    const double h = r_s[q] * exp(-topo_sqdist(topo, j, (int64_t)b) * inv_s[q]);
+#pragma unroll
+                    for (int kk = 0; kk < 8; ++kk)
+                        if (k0 + kk < d) acc[kk] = fma(h, xs[q * d + k0 + kk], acc[kk]);
+                    if (k0 == 0) dacc += h;
+                }
+            }
+        }
+        if (j < m) {
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                if (k0 + kk < d && acc[kk] != 0.0) atomicAdd(num + j * d + k0 + kk, acc[kk]);
+        }
+    }
+    if (j < m && dacc != 0.0) atomicAdd(den + j, dacc);
+}
+
+template <typename T>
+__global__ void divide_kernel(const double* __restrict__ num, const double* __restrict__ den, int64_t m, int d,
+                              T* __restrict__ w_out) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m * d) return;
+    const double dn = den[q / d];
+    w_out[q] = dn > FLOAT_EPS ? (T)(num[q] / dn) : (T)0;
+}
+
+size_t max_dyn_smem() {
+    static size_t cached = 0;
+    if (!cached) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cached = v > 0 ? (size_t)v : 48 * 1024;
+    }
+    return cached;
+}
+
+}  // namespace
+
+template <typename T>
+int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
+                      double* c, cudaStream_t stream) {
+    if (n == 0 || m == 0) return SOMGB_OK;
+    const size_t budget = std::min<size_t>(max_dyn_smem(), 200 * 1024);
+    const int64_t per_unit = (int64_t)(d + 1) * 8;
+    int64_t upr = std::max<int64_t>(1, (int64_t)(budget / per_unit));
+    upr = std::min(upr, m);
+    const int64_t ranges = ceil_div(m, upr);
+    upr = ceil_div(m, ranges);
+    const size_t smem = (size_t)(upr * per_unit);
+    const int64_t ctas_wanted = 2 * (int64_t)num_sms();
+    int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
+    int64_t chunk = std::max<int64_t>(1024, ceil_div(n, chunks));
+    chunks = ceil_div(n, chunk);
+    auto kern = accumulate_kernel<T>;
+    SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<dim3((unsigned)chunks, (unsigned)ranges), 256, smem, stream>>>(x, rho, bmu, n, d, upr, m, chunk, S, c);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
+template <typename T>
+int launch_neighbourhood(const double* S, const double* c, const T* topo, int64_t m, int d, double sigma, T* w_out,
+                         double* num, double* den, cudaStream_t stream) {
+    if (m == 0) return SOMGB_OK;
+    const double inv2s2 = 1.0 / (2.0 * sigma * sigma);
+    if (d <= 8) {
+        neighbourhood_kernel<T, 8><<<(unsigned)m, 256, 0, stream>>>(S, c, topo, m, d, inv2s2, w_out, num, den);
+    } else if (d <= 16) {
+        neighbourhood_kernel<T, 16><<<(unsigned)m, 256, 0, stream>>>(S, c, topo, m, d, inv2s2, w_out, num, den);
+    } else if (d <= 32) {
+        neighbourhood_kernel<T, 32><<<(unsigned)m, 256, 0, stream>>>(S, c, topo, m, d, inv2s2, w_out, num, den);
+    } else {
+        neighbourhood_wide_kernel<T><<<(unsigned)m, 128, 128 * sizeof(double), stream>>>(S, c, topo, m, d, inv2s2,
+                                                                                        w_out, num, den);
+    }
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
+template <typename T>
+int launch_iter(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, const T* topo, int64_t m,
+                double sigma0, int64_t cur_vector, int64_t n_vectors, double* num, double* den,
+                cudaStream_t stream) {
+    if (n == 0 || m == 0) return SOMGB_OK;
+    const int64_t tiles = ceil_div(m, 128);
+    int64_t chunks = std::max<int64_t>(1, (2 * num_sms()) / tiles);
+    int64_t chunk = std::max<int64_t>(256, ceil_div(n, chunks));
+    chunks = ceil_div(n, chunk);
+    const size_t smem = 32 * (size_t)d * sizeof(double) + 32 * (2 * sizeof(double) + sizeof(int));
+    auto kern = iter_kernel<T>;
+    if (smem > 48 * 1024) SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                              (int)smem));
+    kern<<<dim3((unsigned)tiles, (unsigned)chunks), 128, smem, stream>>>(x, rho, bmu, n, d, topo, m, sigma0,
+                                                                        cur_vector, n_vectors, chunk, num, den);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
+template <typename T>
+int launch_divide(const double* num, const double* den, int64_t m, int d, T* w_out, cudaStream_t stream) {
+    const int64_t total = m * d;
+    if (total == 0) return SOMGB_OK;
+    divide_kernel<T><<<(unsigned)ceil_div(total, 256), 256, 0, stream>>>(num, den, m, d, w_out);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
+template int launch_accumulate<float>(const float*, const double*, const int32_t*, int64_t, int, int64_t, double*,
+                                      double*, cudaStream_t);
+template int launch_accumulate<double>(const double*, const double*, const int32_t*, int64_t, int, int64_t, double*,
+                                       double*, cudaStream_t);
+template int launch_neighbourhood<float>(const double*, const double*, const float*, int64_t, int, double, float*,
+                                         double*, double*, cudaStream_t);
+template int launch_neighbourhood<double>(const double*, const double*, const double*, int64_t, int, double, double*,
+                                          double*, double*, cudaStream_t);
+template int launch_iter<float>(const float*, const double*, const int32_t*, int64_t, int, const float*, int64_t,
+                                double, int64_t, int64_t, double*, double*, cudaStream_t);
+template int launch_iter<double>(const double*, const double*, const int32_t*, int64_t, int, const double*, int64_t,
+                                 double, int64_t, int64_t, double*, double*, cudaStream_t);
+template int launch_divide<float>(const double*, const double*, int64_t, int, float*, cudaStream_t);
+template int launch_divide<double>(const double*, const double*, int64_t, int, double*, cudaStream_t);
+
+}  // namespace somgb

@@ -1,0 +1,222 @@
+"""SOM_Batch: batch self-organising map training on GB300.
+
+Drop-in for the reference's ``decontamination.algo.som_batch.SOM_Batch``
+(algo/som_batch.py:29-505): same constructor, ``train`` signature, attributes
+(``_weights``, ``_history``, ``_quantization_errors``,
+``_topographic_errors``, ``_sigma``, ``_n_epochs``, ``_n_vectors``) and HDF5
+header. ``enable_gpu`` / ``threads_per_blocks`` are accepted and ignored.
+
+Epoch mode, per epoch e (reference: :285-374):
+  1. one fused device pass over the data with the weights w(e): BMUs (training
+     semantics), per-BMU sums S and c in float64, and the compute_errors sums
+     of w(e) — which are the errors the reference computes at the end of epoch
+     e-1 (the weights of both passes are identical), so E epochs take E+1
+     passes over the data instead of 2E;
+  2. the neighbourhood contraction w(e+1) = (H.S)/(H.c) on the device.
+The data stay resident on the device for all epochs when they are an array.
+The host synchronises once per epoch only when a stop threshold is set.
+"""
+
+import math
+import typing
+
+import numpy as np
+import torch
+
+from . import _device, _native
+from ._dataset import is_array, iterate_chunks
+from .som_abstract import SOM_Abstract
+
+FLOAT_EPS = 1.0e-12   # algo/som_batch.py:24
+
+
+def asymptotic_decay(epoch: int, epochs: int) -> float:
+    """algo/__init__.py:64-74."""
+    return 1.0 / (1.0 + 2.0 * epoch / epochs)
+
+
+class SOM_Batch(SOM_Abstract):
+    """Self Organizing Maps (standard batch implementation) with constant memory usage.
+
+    Parameters
+    ----------
+    m, n : int
+        Number of neuron rows / columns.
+    dim : int
+        Dimensionality of the input data.
+    dtype : np.float32 (default) or np.float64
+        Neural network data type.
+    topology : str, default None == 'hexagonal'
+        Neural network topology, either 'square' or 'hexagonal'.
+    sigma : float, default None == max(m, n) / 2
+        Starting value of the neighborhood radius.
+    """
+
+    __MODE__ = 'batch'
+
+    def __init__(self, m: int, n: int, dim: int, dtype=np.float32, topology: typing.Optional[str] = None,
+                 sigma: float = None):
+        super().__init__(m, n, dim, dtype, topology)
+        self._sigma = max(m, n) / 2.0 if sigma is None else float(sigma)
+        self._n_epochs = 0
+        self._n_vectors = 0
+        self._header_extra = {'mode': '__MODE__', 'sigma': '_sigma', 'n_epochs': '_n_epochs',
+                              'n_vectors': '_n_vectors'}
+
+    @property
+    def sigma(self) -> float:
+        """Starting value of the neighborhood radius."""
+        return self._sigma
+
+    # ------------------------------------------------------------------------------------------------------------------
+
+    def _epoch_sigma(self, epoch, total):
+        # sigma0 is passed to the reference kernel in the map dtype and multiplied in float64 (som_batch.py:107-110)
+        s = float(self._dtype(self._sigma)) * asymptotic_decay(epoch, total)
+        return FLOAT_EPS if s < FLOAT_EPS else s
+
+    def _chunk_source(self, dataset, dataset_weights, device):
+        """Chunks for the epoch loop: arrays are uploaded once and reused by every epoch."""
+        if (dataset is None or is_array(dataset)) and (dataset_weights is None or is_array(dataset_weights)):
+            chunks = list(iterate_chunks(dataset, dataset_weights, self._dtype, device))
+            return lambda: iter(chunks)
+        return lambda: iterate_chunks(dataset, dataset_weights, self._dtype, device)
+
+    def _epoch_pass(self, xc, rc, w, topo, S, c, err, device):
+        n = _device.rows(xc)
+        M, D = self._m * self._n, self._dim
+        if self._is_f64:
+            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, n, M, D, _native.ALGO_FP32, device)
+            _native.call('somgb_train_epoch_pass_f64', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
+                         topo.data_ptr(), M, self._penalty, S.data_ptr(), c.data_ptr(), _device.ptr(err), wsp, wsb,
+                         _device.stream())
+        else:
+            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, n, M, D, self._algo, device)
+            _native.call('somgb_train_epoch_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
+                         topo.data_ptr(), M, self._penalty, self._algo, S.data_ptr(), c.data_ptr(), _device.ptr(err),
+                         None, wsp, wsb, _device.stream())
+
+    def _update(self, S, c, topo, sigma, w_out):
+        M, D = self._m * self._n, self._dim
+        name = 'somgb_neighbourhood_update_f64' if self._is_f64 else 'somgb_neighbourhood_update'
+        _native.call(name, S.data_ptr(), c.data_ptr(), topo.data_ptr(), M, D, sigma, w_out.data_ptr(), None, None,
+                     _device.stream())
+
+    @staticmethod
+    def _errors_of(err_host):
+        return (err_host[0] / err_host[2], err_host[1] / err_host[2]) if err_host[2] > 0.0 else (np.nan, np.nan)
+
+    # ------------------------------------------------------------------------------------------------------------------
+
+    def train(self, dataset, dataset_weights=None, n_epochs: typing.Optional[int] = None,
+              n_vectors: typing.Optional[int] = None, use_best_epoch: bool = True,
+              stop_quantization_error: typing.Optional[float] = None,
+              stop_topographic_error: typing.Optional[float] = None, show_progress_bar: bool = False,
+              enable_gpu: bool = True, threads_per_blocks: typing.Optional[int] = None) -> None:
+        """Trains the neural network with `n_epochs` epochs or on `n_vectors` vectors (algo/som_batch.py:214-505).
+
+        w_j(e+1) = sum_i h_ji x_i / sum_i h_ji, h_ji = rho_i exp(-|t_j - t_bmu(x_i)|^2 / (2 sigma(e)^2)),
+        sigma(e) = sigma / (1 + 2 e / e_tot).
+        """
+        self._n_epochs = n_epochs
+        self._n_vectors = n_vectors
+        if n_epochs is not None and n_vectors is None:
+            self._train_epochs(dataset, dataset_weights, n_epochs, stop_quantization_error, stop_topographic_error)
+        elif n_epochs is None and n_vectors is not None:
+            self._train_vectors(dataset, dataset_weights, n_vectors)
+        else:
+            raise ValueError('Invalid training method, specify either `n_epochs` or `n_vectors`')
+        if use_best_epoch:
+            self._weights[:] = self._history[np.nanargmin(self._quantization_errors)]
+
+    def _train_epochs(self, dataset, dataset_weights, n_epochs, stop_qe, stop_te):
+        device = _device.require_cuda()
+        sq = -1.0e6 if stop_qe is None else stop_qe
+        st = -1.0e6 if stop_te is None else stop_te
+        check_stop = stop_qe is not None or stop_te is not None
+        M, D = self._m * self._n, self._dim
+        td = _device.torch_dtype(self._dtype)
+        with_errors = M >= 2   # compute_errors returns (nan, nan) below two units (som_abstract.py:547-549)
+
+        chunks = self._chunk_source(dataset, dataset_weights, device)
+        topo = self._device_topography()
+        w = self._device_weights()
+        history = torch.empty((n_epochs, M, D), dtype=td, device=device)
+        S = torch.empty((M, D), dtype=torch.float64, device=device)
+        c = torch.empty(M, dtype=torch.float64, device=device)
+        errs = torch.zeros((n_epochs + 1, 3), dtype=torch.float64, device=device)
+
+        done = n_epochs            # epochs whose update was kept
+        for e in range(n_epochs + 1):
+            S.zero_()
+            c.zero_()
+            err = errs[e] if with_errors else None
+            last = e == n_epochs
+            for xc, rc in chunks():
+                if last:
+                    if with_errors:
+                        n = _device.rows(xc)
+                        name = 'somgb_compute_errors_f64' if self._is_f64 else 'somgb_compute_errors'
+                        if self._is_f64:
+                            _native.call(name, xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(),
+                                         M, self._penalty, err.data_ptr(), _device.stream())
+                        else:
+                            wsp, wsb = self._ws.for_op(_native.OP_ERRORS, n, M, D, self._algo, device)
+                            _native.call(name, xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(),
+                                         M, self._penalty, self._algo, err.data_ptr(), wsp, wsb, _device.stream())
+                else:
+                    self._epoch_pass(xc, rc, w, topo, S, c, err if e > 0 else None, device)
+            if check_stop and e > 0 and with_errors:
+                qe, te = self._errors_of(errs[e].cpu().numpy())
+                if qe <= sq and te <= st:
+                    done = e          # the reference stops after epoch e-1 (som_batch.py:368-374)
+                    break
+            if last:
+                break
+            w_next = torch.empty_like(w)
+            self._update(S, c, topo, self._epoch_sigma(e, n_epochs), w_next)
+            history[e].copy_(w_next)
+            w = w_next
+
+        self._history = np.empty((n_epochs, M, D), dtype=self._dtype)
+        self._history[:done] = history[:done].cpu().numpy()
+        self._quantization_errors = np.full(n_epochs, np.nan, dtype=np.float64)
+        self._topographic_errors = np.full(n_epochs, np.nan, dtype=np.float64)
+        if with_errors:
+            eh = errs.cpu().numpy()
+            for e in range(done):
+                self._quantization_errors[e], self._topographic_errors[e] = self._errors_of(eh[e + 1])
+        self._weights[:] = history[done - 1].cpu().numpy() if done > 0 else self._weights
+
+    def _train_vectors(self, dataset, dataset_weights, n_vectors):
+        device = _device.require_cuda()
+        M, D = self._m * self._n, self._dim
+        td = _device.torch_dtype(self._dtype)
+        topo = self._device_topography()
+        w = self._device_weights()
+        num = torch.zeros((M, D), dtype=torch.float64, device=device)
+        den = torch.zeros(M, dtype=torch.float64, device=device)
+        sigma0 = float(self._dtype(self._sigma))
+        cur = 0
+        name = 'somgb_train_iter_pass_f64' if self._is_f64 else 'somgb_train_iter_pass'
+        for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device):
+            count = min(_device.rows(xc), n_vectors - cur)
+            xk = xc[:count]
+            rk = None if rc is None else rc[:count]
+            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, count, M, D, _native.ALGO_FP32, device)
+            _native.call(name, xk.data_ptr(), _device.ptr(rk), count, D, w.data_ptr(), topo.data_ptr(), M, sigma0,
+                         cur, n_vectors, num.data_ptr(), den.data_ptr(), wsp, wsb, _device.stream())
+            cur += count
+            if cur >= n_vectors:
+                break
+        w_new = torch.empty((M, D), dtype=td, device=device)
+        _native.call('somgb_divide_f64' if self._is_f64 else 'somgb_divide', num.data_ptr(), den.data_ptr(), M, D,
+                     w_new.data_ptr(), _device.stream())
+        self._history = np.empty((1, M, D), dtype=self._dtype)
+        self._history[0] = w_new.cpu().numpy()
+        self._weights[:] = self._history[0]
+        self._quantization_errors = np.zeros(1, dtype=np.float64)
+        self._topographic_errors = np.zeros(1, dtype=np.float64)
+        errors = self.compute_errors(dataset, dataset_weights)
+        self._quantization_errors[0] = errors[0]
+        self._topographic_errors[0] = errors[1]

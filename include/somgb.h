@@ -1,0 +1,147 @@
+/*
+ * somgb — C ABI of the GB300-native batch self-organising-map hot path.
+ *
+ * Every entry point takes caller-owned DEVICE pointers (row-major, contiguous),
+ * sizes, a CUDA stream, and returns an int status (SOMGB_OK == 0). Work is
+ * enqueued on `stream` and is asynchronous with respect to the host; outputs
+ * marked "+=" are accumulated into, so callers zero them first (that is how the
+ * reference's chunked loops use their device accumulators). No entry point
+ * allocates device memory: scratch space is a caller buffer whose size
+ * somgb_workspace_bytes() returns. Calls on distinct streams with distinct
+ * workspaces may run concurrently.
+ *
+ * Each entry point names the reference interface it replaces
+ * (lpsc-euclid/decontamination 0.0.1, paths inside that project). In the
+ * reference these are Numba kernels launched as
+ * `kernel[enable_gpu, threads_per_block, n](*arrays, *scalars)`
+ * (jit/__init__.py:334-412); results go to caller-allocated device arrays.
+ *
+ * Arithmetic contract: BMUs are those of the compiled reference for float32
+ * maps — distance = float64 sum, in feature order, of float32 squares of
+ * float32 differences; argmin by strict '>' (lowest index wins ties); NaN
+ * distances skipped. Float64 maps use float64 throughout.
+ */
+#ifndef SOMGB_H
+#define SOMGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* somgb_stream_t; /* == cudaStream_t; NULL = legacy default stream */
+
+/* status codes */
+#define SOMGB_OK 0
+#define SOMGB_ERR_INVALID 1     /* bad size, null pointer, misaligned pointer */
+#define SOMGB_ERR_CUDA 2        /* a CUDA runtime call or launch failed */
+#define SOMGB_ERR_WORKSPACE 3   /* workspace smaller than somgb_workspace_bytes() */
+#define SOMGB_ERR_UNSUPPORTED 4 /* no device / not an sm_103 device / shape outside a kernel's limits */
+#define SOMGB_ERR_TIMEOUT 5     /* a bounded device-side wait gave up (kernel returned early) */
+
+/* distance-search algorithms */
+#define SOMGB_ALGO_FP32 0       /* CUDA cores: float32 direct differences, margin-gated float64 recheck */
+#define SOMGB_ALGO_TC 1         /* tcgen05 split-BF16 distance GEMM, margin-gated recheck */
+#define SOMGB_ALGO_AUTO 2       /* TC where its shape limits allow, FP32 otherwise */
+
+/* workspace query operations */
+#define SOMGB_OP_FIND_BMUS 0
+#define SOMGB_OP_COUNT_BMUS 1
+#define SOMGB_OP_ERRORS 2
+#define SOMGB_OP_EPOCH 3
+
+int somgb_version(void);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated); returns its full length. */
+size_t somgb_last_error(char* buf, size_t len);
+
+/* Scratch bytes an entry point needs for these sizes (0 if none). */
+size_t somgb_workspace_bytes(int op, int64_t n, int64_t m, int d, int algo);
+
+/* Number of samples the last pass on this thread sent to the exact recheck (diagnostic; synchronises `stream`). */
+int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream);
+
+/*
+ * BMU of every sample: bmu_out[i] = argmin_j |x_i - w_j|^2, 0 when every distance is NaN.
+ * Replaces _find_bmus_kernel / _find_bmu_xpu (algo/som_abstract.py:736-783), called by get_winners (:670-695).
+ */
+int somgb_find_bmus(const float* x, int64_t n, int d, const float* w, int64_t m, int algo, int32_t* bmu_out,
+                    void* ws, size_t ws_bytes, somgb_stream_t stream);
+int somgb_find_bmus_f64(const double* x, int64_t n, int d, const double* w, int64_t m, int32_t* bmu_out,
+                        somgb_stream_t stream);
+
+/*
+ * Activation histogram: hist[bmu(x_i)] += rho_i for rho_i > 0 (rho NULL = all ones); hist is float64 (m,) "+=".
+ * Replaces _count_bmus_kernel (algo/som_abstract.py:700-732), called by get_activation_map (:605-666).
+ */
+int somgb_count_bmus(const float* x, const double* rho, int64_t n, int d, const float* w, int64_t m, int algo,
+                     double* hist, void* ws, size_t ws_bytes, somgb_stream_t stream);
+int somgb_count_bmus_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,
+                         double* hist, somgb_stream_t stream);
+
+/*
+ * Quantisation / topographic error sums, err3 "+=": [sum rho*sqrt(d1), sum rho*[|t_b1-t_b2|^2 > penalty], sum rho]
+ * over samples with rho > 0 and two valid units (b1, b2 = the two smallest (distance, index) pairs).
+ * Replaces _compute_errors_kernel / _compute_errors_xpu (algo/som_abstract.py:787-878), called by
+ * compute_errors (:528-601); penalty is 2.0 for square and 1.0 for hexagonal maps (:575).
+ */
+int somgb_compute_errors(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                         int64_t m, double penalty, int algo, double* err3, void* ws, size_t ws_bytes,
+                         somgb_stream_t stream);
+int somgb_compute_errors_f64(const double* x, const double* rho, int64_t n, int d, const double* w,
+                             const double* topo, int64_t m, double penalty, double* err3, somgb_stream_t stream);
+
+/*
+ * One training pass of epoch mode over a chunk, fused with the error sums of the same weights.
+ * For each sample with (float)rho_i > 0 and a valid BMU b_i (training semantics: all-NaN rows are skipped):
+ *   S[b_i, :] += (double)(float)rho_i * x_i,  c[b_i] += (double)(float)rho_i      (S: m x d, c: m; float64 "+=")
+ * and, when err3 != NULL, the compute_errors sums of `w` as in somgb_compute_errors ("+=").
+ * bmu_out (optional, n) receives b_i (-1 when skipped).
+ * Replaces the BMU half of _train_step1_epoch_kernel/_train_step2_xpu (algo/som_batch.py:94-150, 509-540) and,
+ * fused, the compute_errors pass the reference runs after every epoch (som_batch.py:363). The neighbourhood half
+ * (som_batch.py:542-566) is somgb_neighbourhood_update on the per-BMU sums.
+ */
+int somgb_train_epoch_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                           int64_t m, double penalty, int algo, double* S, double* c, double* err3,
+                           int32_t* bmu_out, void* ws, size_t ws_bytes, somgb_stream_t stream);
+int somgb_train_epoch_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w,
+                               const double* topo, int64_t m, double penalty, double* S, double* c, double* err3,
+                               void* ws, size_t ws_bytes, somgb_stream_t stream);
+
+/*
+ * Neighbourhood contraction and weight update of one epoch:
+ *   num_j = sum_b h_jb S_b, den_j = sum_b h_jb c_b, h_jb = exp(-|t_j - t_b|^2 / (2 sigma^2)),
+ *   w_out_j = num_j / den_j if den_j > 1e-12 else 0.
+ * `sigma` is the decayed, clamped radius of this epoch (sigma0 * 1/(1+2e/E), >= 1e-12, in float64).
+ * Replaces the neighbourhood scatter of _train_step2_xpu (algo/som_batch.py:542-566) and the host divide
+ * (som_batch.py:346-359). num/den (optional, m x d and m) receive the float64 numerator and denominator.
+ */
+int somgb_neighbourhood_update(const double* S, const double* c, const float* topo, int64_t m, int d, double sigma,
+                               float* w_out, double* num, double* den, somgb_stream_t stream);
+int somgb_neighbourhood_update_f64(const double* S, const double* c, const double* topo, int64_t m, int d,
+                                   double sigma, double* w_out, double* num, double* den, somgb_stream_t stream);
+
+/*
+ * Iteration ("n_vectors") mode over a chunk: sample i of the chunk has sigma_i = sigma0 * 1/(1+2(cur+i)/n_vectors)
+ * (clamped >= 1e-12) and adds rho_i * h_j(i) * x_i to num[j] and rho_i * h_j(i) to den[j] for every unit j
+ * (float64 "+="). Replaces _train_step1_iter_kernel (algo/som_batch.py:154-210). sigma0 is the map dtype's value.
+ * Workspace: somgb_workspace_bytes(SOMGB_OP_EPOCH, n, m, d, SOMGB_ALGO_FP32).
+ */
+int somgb_train_iter_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                          int64_t m, double sigma0, int64_t cur_vector, int64_t n_vectors, double* num, double* den,
+                          void* ws, size_t ws_bytes, somgb_stream_t stream);
+int somgb_train_iter_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w,
+                              const double* topo, int64_t m, double sigma0, int64_t cur_vector, int64_t n_vectors,
+                              double* num, double* den, void* ws, size_t ws_bytes, somgb_stream_t stream);
+
+/* w_out_j = num_j / den_j where den_j > 1e-12, else 0 (algo/som_batch.py:481-486). */
+int somgb_divide(const double* num, const double* den, int64_t m, int d, float* w_out, somgb_stream_t stream);
+int somgb_divide_f64(const double* num, const double* den, int64_t m, int d, double* w_out, somgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SOMGB_H */

@@ -1,0 +1,249 @@
+"""GPU parity: the libsomgb kernels (through the C ABI) against the CPU oracle.
+
+BMUs must be bit-identical to the oracle's `numba` mode (the compiled
+reference's arithmetic); activation counts exact; error sums within float64
+summation-order rounding; trained weights within 1e-5 relative of the float64
+oracle (the bar the path is held to) and within the reference's own 1e-4
+known-answer tolerance of its fixtures.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import decontamination_gb300 as dg
+from decontamination_gb300 import _native
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+ALGOS = ['fp32', 'auto']
+W_RTOL = 1e-5          # trained weights vs the float64 oracle
+ERR_RTOL = 1e-9        # error sums: float64, summation order differs
+
+
+def _rand(rng, n, d, kind='uniform'):
+    if kind == 'uniform':
+        return rng.random((n, d), dtype=np.float32)
+    if kind == 'mixture':
+        means = rng.uniform(-3, 3, size=(5, d))
+        return (means[rng.integers(0, 5, n)] + 0.5 * rng.standard_normal((n, d))).astype(np.float32)
+    z = rng.standard_normal((n, d))
+    return np.exp(0.3 * z).astype(np.float32)
+
+
+def _som(m, n, d, w, topology='square', algo='auto', sigma=None, dtype=np.float32):
+    som = dg.SOM_Batch(m, n, d, dtype=dtype, topology=topology, sigma=sigma)
+    som._weights[...] = w
+    som.bmu_algo = algo
+    return som
+
+
+# ----------------------------------------------------------------------------------------------------------------------
+# projection calls
+# ----------------------------------------------------------------------------------------------------------------------
+
+SHAPES = [(1, 1, 3, 50), (1, 2, 4, 300), (4, 4, 4, 25_000), (10, 10, 4, 20_000), (8, 9, 7, 5000),
+          (32, 32, 16, 40_000), (16, 16, 17, 8000), (8, 16, 32, 10_000), (5, 7, 64, 3000), (4, 5, 100, 2000),
+          (64, 64, 16, 6000), (3, 3, 1, 500)]
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+@pytest.mark.parametrize('m,n,d,N', SHAPES)
+def test_winners_bit_exact(cuda, native, oracle, algo, m, n, d, N):
+    rng = np.random.default_rng(m * 1000 + n * 10 + d)
+    x = _rand(rng, N, d, 'lognormal' if d >= 16 else 'uniform')
+    w = x[rng.integers(0, N, m * n)] + 0.01 * rng.standard_normal((m * n, d)).astype(np.float32)
+    som = _som(m, n, d, w, algo=algo)
+    got = som.get_winners(x)
+    want = oracle.find_bmus(w.astype(np.float32), x, 'numba')
+    assert got.dtype == np.int32
+    assert np.array_equal(got, want), f'{np.sum(got != want)} BMU mismatches'
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+def test_kat_activation_map_exact(cuda, native, algo):
+    g = golden('kat_activation')
+    x = np.random.default_rng(int(g['x_seed'])).random(tuple(g['x_shape']), np.float32)
+    som = _som(4, 4, 4, g['w0'], algo=algo)
+    assert np.array_equal(som.get_activation_map(x), g['activation'])
+    gw = golden('kat_winners')
+    assert np.array_equal(_som(4, 4, 4, gw['w0'], algo=algo).get_winners(gw['x']), gw['winners'])
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+@pytest.mark.parametrize('topology', ['square', 'hexagonal'])
+def test_errors_and_activation_vs_oracle(cuda, native, oracle, algo, topology):
+    rng = np.random.default_rng(3)
+    m, n, d, N = 12, 10, 6, 30_000
+    x = _rand(rng, N, d, 'mixture')
+    w = x[rng.integers(0, N, m * n)].copy()
+    rho = rng.standard_normal(N)
+    som = _som(m, n, d, w, topology=topology, algo=algo)
+    topo = oracle.topography(m, n, topology)
+    pen = 2.0 if topology == 'square' else 1.0
+    for r in (None, rho):
+        o = oracle.compute_errors_raw(w, topo, x, r, pen, 'numba')
+        np.testing.assert_allclose(som.compute_errors(x, r), o[:2] / o[2], rtol=ERR_RTOL)
+        h = oracle.count_bmus(w, x, r, 'numba')
+        np.testing.assert_allclose(som.get_activation_map(x, r).ravel(), h.astype(np.float32), rtol=1e-6)
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+def test_edge_cases_golden(cuda, native, algo):
+    """NaN features and rows, a NaN unit, exact ties between duplicated units, zero and negative densities."""
+    g = golden('edge_projection')
+    som = _som(4, 5, 6, g['w0'], algo=algo)
+    assert np.array_equal(som.get_winners(g['x']), g['winners'])
+    assert np.array_equal(som.get_activation_map(g['x']), g['activation'])
+    assert np.array_equal(som.get_activation_map(g['x'], g['rho']), g['activation_weighted'])
+    np.testing.assert_allclose(som.compute_errors(g['x']), g['errors'], rtol=1e-6)
+    np.testing.assert_allclose(som.compute_errors(g['x'], g['rho']), g['errors_weighted'], rtol=1e-6)
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+def test_infinities_and_empty(cuda, native, oracle, algo):
+    rng = np.random.default_rng(4)
+    w = rng.random((9, 3), dtype=np.float32)
+    x = rng.random((64, 3), dtype=np.float32)
+    x[3, 1] = np.inf
+    x[4] = [1e20, -1e20, 3e19]          # float32 squares overflow
+    w[2, 0] = np.inf
+    som = _som(3, 3, 3, w, algo=algo)
+    assert np.array_equal(som.get_winners(x), oracle.find_bmus(w, x, 'numba'))
+    assert som.get_winners(np.zeros((0, 3), np.float32)).shape == (0,)
+    assert np.all(som.get_activation_map(np.zeros((0, 3), np.float32)) == 0)
+
+
+# ----------------------------------------------------------------------------------------------------------------------
+# training
+# ----------------------------------------------------------------------------------------------------------------------
+
+def _oracle_train(oracle, m, n, d, w0, topology, sigma, x, rho=None, **kw):
+    osom = oracle.OracleSOM(m, n, d, topology=topology, sigma=sigma, mode='numba', threads=0, accumulate='fp64')
+    osom.weights = w0.copy()
+    osom.train(x, rho, **kw)
+    return osom
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+def test_kat_training(cuda, native, oracle, algo):
+    for name, kw in (('kat_epoch', dict(n_epochs=1)), ('kat_iter', dict(n_vectors=1000))):
+        g = golden(name)
+        som = _som(4, 4, 4, g['w0'], algo=algo)
+        som.train(g['x'], **kw)
+        # the reference's own known-answer tolerance (test/test_som_batch.py:56)
+        np.testing.assert_allclose(som.weights, g['weights'], rtol=1e-4)
+        np.testing.assert_allclose(som.quantization_errors, g['qe'], rtol=1e-5)
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+@pytest.mark.parametrize('topology', ['square', 'hexagonal'])
+def test_epoch_training_vs_fp64_oracle(cuda, native, oracle, algo, topology):
+    rng = np.random.default_rng(21)
+    m, n, d, N, E = 10, 12, 8, 40_000, 4
+    x = _rand(rng, N, d, 'mixture')
+    rho = rng.random(N).astype(np.float32)
+    rho[rng.random(N) < 0.05] = 0.0
+    w0 = rng.uniform(-1, 1, (m * n, d)).astype(np.float32)
+    som = _som(m, n, d, w0, topology=topology, algo=algo, sigma=4.0)
+    som.train(x, rho, n_epochs=E, use_best_epoch=False)
+    ref = _oracle_train(oracle, m, n, d, w0, topology, 4.0, x, rho, n_epochs=E, use_best_epoch=False)
+    np.testing.assert_allclose(som.weights, ref.weights, rtol=W_RTOL, atol=1e-6)
+    np.testing.assert_allclose(som._history, ref.history, rtol=W_RTOL, atol=1e-6)
+    np.testing.assert_allclose(som.quantization_errors, ref.quantization_errors, rtol=1e-6)
+    np.testing.assert_allclose(som.topographic_errors, ref.topographic_errors, rtol=1e-6)
+
+
+def test_chunked_generator_and_best_epoch(cuda, native, oracle):
+    g = golden('square_chunked_epochs')
+    x, b = g['x'], g['chunk_bounds']
+    chunks = [x[b[i]:b[i + 1]] for i in range(len(b) - 1)]
+    som = _som(5, 7, 3, g['w0'])
+    som.train(lambda: lambda: iter(chunks), n_epochs=2, use_best_epoch=False)
+    np.testing.assert_allclose(som.weights, g['weights'], rtol=1e-4, atol=1e-6)
+    ref = _oracle_train(oracle, 5, 7, 3, g['w0'], 'square', float(g['sigma']), x, n_epochs=2, use_best_epoch=False)
+    np.testing.assert_allclose(som.weights, ref.weights, rtol=W_RTOL, atol=1e-6)
+
+    gh = golden('hex_weighted_epochs')
+    som = _som(6, 5, 7, gh['w0'], topology='hexagonal', sigma=2.5)
+    som.train(gh['x'], gh['rho'], n_epochs=3, use_best_epoch=True)
+    ref = _oracle_train(oracle, 6, 5, 7, gh['w0'], 'hexagonal', 2.5, gh['x'], gh['rho'], n_epochs=3,
+                        use_best_epoch=True)
+    np.testing.assert_allclose(som.weights, ref.weights, rtol=W_RTOL, atol=1e-6)
+    np.testing.assert_allclose(som.quantization_errors, ref.quantization_errors, rtol=1e-6)
+    np.testing.assert_allclose(som.topographic_errors, ref.topographic_errors, rtol=1e-6)
+
+
+def test_early_stop(cuda, native, oracle):
+    rng = np.random.default_rng(8)
+    x = _rand(rng, 5000, 4, 'mixture')
+    w0 = rng.uniform(-1, 1, (36, 4)).astype(np.float32)
+    free = _som(6, 6, 4, w0)
+    free.train(x, n_epochs=6, use_best_epoch=False)
+    stop_at = free.quantization_errors[2] * (1 + 1e-9)
+    som = _som(6, 6, 4, w0)
+    som.train(x, n_epochs=6, use_best_epoch=False, stop_quantization_error=stop_at, stop_topographic_error=1.0)
+    first = int(np.argmax(free.quantization_errors <= stop_at))
+    assert np.all(np.isnan(som.quantization_errors[first + 1:]))
+    # float64 atomics make runs differ at the last bit at most
+    np.testing.assert_allclose(som.quantization_errors[:first + 1], free.quantization_errors[:first + 1], rtol=1e-6)
+    np.testing.assert_allclose(som.weights, free._history[first], rtol=1e-6, atol=1e-7)
+
+
+def test_iter_mode_vs_oracle(cuda, native, oracle):
+    g = golden('hex_weighted_iter')
+    som = _som(4, 6, 5, g['w0'], topology='hexagonal', sigma=3.0)
+    som.train(g['x'], g['rho'], n_vectors=300)
+    np.testing.assert_allclose(som.weights, g['weights'], rtol=1e-4, atol=1e-6)
+    ref = oracle.OracleSOM(4, 6, 5, topology='hexagonal', sigma=3.0, mode='numba', threads=1)
+    ref.weights = g['w0'].copy()
+    ref.train(g['x'], g['rho'], n_vectors=300)
+    np.testing.assert_allclose(som.weights, ref.weights, rtol=1e-5, atol=1e-6)
+
+
+def test_float64_map(cuda, native, oracle):
+    g = golden('float64_epoch')
+    som = _som(3, 4, 4, g['w0'], topology='hexagonal', dtype=np.float64)
+    som.train(g['x'], n_epochs=2, use_best_epoch=False)
+    np.testing.assert_allclose(som.weights, g['weights'], rtol=1e-10)
+    np.testing.assert_allclose(som.quantization_errors, g['qe'], rtol=1e-10)
+    np.testing.assert_allclose(som.topographic_errors, g['te'], rtol=1e-12)
+    assert np.array_equal(som.get_winners(g['x']), oracle.find_bmus(g['weights'], g['x'], 'numba'))
+
+
+# ----------------------------------------------------------------------------------------------------------------------
+# direct C ABI use with caller-owned device buffers
+# ----------------------------------------------------------------------------------------------------------------------
+
+def test_c_abi_epoch_pass_accumulators(cuda, native, oracle):
+    rng = np.random.default_rng(30)
+    M, D, N = 64, 16, 50_000
+    x = _rand(rng, N, D, 'lognormal')
+    w = x[rng.integers(0, N, M)].copy()
+    topo = oracle.topography(8, 8, 'square')
+    xd, wd, td = (torch.from_numpy(a).to(cuda) for a in (x, w, topo))
+    S = torch.zeros((M, D), dtype=torch.float64, device=cuda)
+    c = torch.zeros(M, dtype=torch.float64, device=cuda)
+    err = torch.zeros(3, dtype=torch.float64, device=cuda)
+    bmu = torch.empty(N, dtype=torch.int32, device=cuda)
+    nbytes = native.workspace_bytes(native.OP_EPOCH, N, M, D, native.ALGO_AUTO)
+    ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=cuda)
+    wsp = ws.data_ptr() + (-ws.data_ptr()) % 256
+    s = torch.cuda.current_stream().cuda_stream
+    native.call('somgb_train_epoch_pass', xd.data_ptr(), None, N, D, wd.data_ptr(), td.data_ptr(), M, 2.0,
+                native.ALGO_AUTO, S.data_ptr(), c.data_ptr(), err.data_ptr(), bmu.data_ptr(), wsp, nbytes, s)
+    torch.cuda.synchronize()
+    b = oracle.find_bmus(w, x, 'numba')
+    assert np.array_equal(bmu.cpu().numpy(), b)
+    S_ref = np.zeros((M, D)); np.add.at(S_ref, b, x.astype(np.float64))
+    c_ref = np.bincount(b, minlength=M).astype(np.float64)
+    np.testing.assert_allclose(S.cpu().numpy(), S_ref, rtol=1e-12)
+    assert np.array_equal(c.cpu().numpy(), c_ref)
+    o = oracle.compute_errors_raw(w, topo, x, None, 2.0, 'numba')
+    np.testing.assert_allclose(err.cpu().numpy(), o, rtol=ERR_RTOL)
+    # a workspace one byte short is refused before any launch
+    with pytest.raises(native.SomgbError) as ei:
+        native.call('somgb_train_epoch_pass', xd.data_ptr(), None, N, D, wd.data_ptr(), td.data_ptr(), M, 2.0,
+                    native.ALGO_AUTO, S.data_ptr(), c.data_ptr(), None, None, wsp, nbytes - 1, s)
+    assert ei.value.status == native.SOMGB_ERR_WORKSPACE
