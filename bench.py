@@ -1,0 +1,391 @@
+#!/usr/bin/env python3
+"""Benchmark of the batch-SOM hot path on GB300: one step = one SOM_Batch training epoch.
+
+Workload (default): hexagonal 32x32 map, D=16 float32 features, N=12,582,912 samples (the HEALPix nside=1024
+pixel count) from the seeded correlated log-normal generator (decontamination_gb300.synthetic, seed 2), weights
+U[-1, 1], sigma0 = 16 with the reference's 1/(1+2e/E) decay over a 20-epoch schedule.
+
+  value   epochs with the catalogue resident in HBM (805 MB > L2, so no flush is needed): each epoch is one fused
+          BMU + error pass, the per-BMU segmented sums and the neighbourhood update, timed with CUDA events;
+          metric N*M / epoch time in Gsample.unit/s.
+  e2e     the same metric through the public API call a user makes, SOM_Batch.train(X, n_epochs=1) on a pinned
+          host tensor: host->device copy of the catalogue, training pass, error pass and device->host copy of the
+          weights, history and errors every step.
+  fp32_form  the plain FP32 CUDA-core form of the same epoch (the tensor-core path's baseline).
+  cpu_baseline  the reference's CPU formulation (oracle port: per-sample scatter into every unit with float32
+          atomics, then the error pass) on all host cores, on a bounded prefix of the catalogue.
+
+`--impl reference` times only that CPU formulation (rank 0), each step a bounded sample, and prints its line.
+Under torchrun every rank runs an independent replica (the path is data-parallel; this build keeps one GPU per
+replica and no collective) and value = units processed by all ranks / max time.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name='hex 32x32 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=16, 20-epoch schedule',
+                m=32, n=32, d=16, N=12_582_912, topology='hexagonal', sigma0=16.0, schedule=20, seed=2)
+METRIC = 'SOM epoch Gsample·unit/s'
+UNIT = 'Gsample·unit/s'
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--algo', default='auto', choices=['auto', 'tc', 'fp32'])
+    ap.add_argument('--n', type=int, default=WORKLOAD['N'], help='catalogue rows (default: the full workload)')
+    ap.add_argument('--skip-cpu', action='store_true')
+    ap.add_argument('--skip-e2e', action='store_true')
+    ap.add_argument('--skip-fp32', action='store_true')
+    ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------------------------------------------------
+# helpers
+# ----------------------------------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while active."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        cmd = ['nvidia-smi', f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits', '-lms', '200']
+        if self.gpu_id is not None:
+            cmd.insert(1, f'--id={self.gpu_id}')
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(',')]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable'], 'samples': 0}
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {'sm_mhz': statistics.median(loaded) if loaded else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def gpu_bus_id(torch, dev):
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        return f'{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0'
+    except Exception:
+        return None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return json.load(f), 'measured'
+    except OSError:
+        return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0, 'bf16_tflops_sustained': 1700.0}, 'fallback'
+
+
+def dist_env():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+def make_data(N, w):
+    from decontamination_gb300 import synthetic
+    x = synthetic.correlated_lognormal(N, w['d'], w['seed'])
+    w0 = synthetic.uniform_weights(w['m'] * w['n'], w['d'], w['seed'])
+    return x, w0
+
+
+# ----------------------------------------------------------------------------------------------------------------------
+# CPU formulation of the reference (oracle port) — the reference arm and the cpu_baseline leg
+# ----------------------------------------------------------------------------------------------------------------------
+
+def cpu_epoch_rate(x, w0, w, seconds, threads=0):
+    """Times reference-formulation epochs (scatter with float32 atomics + error pass) on a prefix of x.
+
+    Returns (Gsample.unit/s, samples used, threads)."""
+    from oracle import somref
+    M, D = w['m'] * w['n'], w['d']
+    topo = somref.topography(w['m'], w['n'], w['topology'])
+    nthreads = threads or os.cpu_count()
+
+    def run(ns):
+        num = np.zeros((M, D), np.float32)
+        den = np.zeros(M, np.float32)
+        xs = np.ascontiguousarray(x[:ns])
+        rho = np.ones(ns, np.float32)
+        t0 = time.perf_counter()
+        somref.train_epoch_scatter(num, den, w0, topo, xs, rho, w['sigma0'], 0, w['schedule'], 'numba',
+                                   threads=nthreads)
+        wn = somref.OracleSOM(w['m'], w['n'], D, topology=w['topology'])._divide(num, den)
+        somref.compute_errors_raw(wn, topo, xs, None, 2.0 if w['topology'] == 'square' else 1.0, 'numba',
+                                  threads=nthreads)
+        return time.perf_counter() - t0
+
+    ns = 2048
+    dt = run(ns)
+    ns = int(min(x.shape[0], max(ns, ns * seconds / max(dt, 1e-3))))
+    dt = run(ns)
+    return ns * M / dt / 1e9, ns, nthreads, dt
+
+
+def reference_arm(args, ws, rank):
+    w = WORKLOAD
+    if rank != 0:
+        return
+    x, w0 = make_data(min(args.n, 400_000), w)
+    rates = []
+    info = None
+    for step in range(args.warmup + args.steps):
+        r, ns, nt, dt = cpu_epoch_rate(x, w0, w, seconds=4.0)
+        if step >= args.warmup:
+            rates.append(r)
+            info = (ns, nt)
+    value = statistics.median(rates)
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': args.gpus, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': w['N'] * w['m'] * w['n'] / (value * 1e9) * 1e3,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+        'config': {'workload': w['name'], 'formulation': 'reference CPU epoch (per-sample scatter, float32 atomics, '
+                                                        'error pass), oracle port in C++/OpenMP'},
+        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': info[1], 'kind': 'port',
+                         'sample': f'first {info[0]} samples of the workload, 1 epoch + error pass per step'},
+        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------------------------------------------------
+
+class EpochRunner:
+    """The epoch of SOM_Batch.train with the catalogue resident on the device (same libsomgb calls)."""
+
+    def __init__(self, torch, native, xd, w0, topo, w, algo, device):
+        self.t, self.nat, self.xd, self.topo, self.w, self.dev = torch, native, xd, topo, w, device
+        self.M, self.D, self.N = w['m'] * w['n'], w['d'], int(xd.shape[0])
+        self.algo = native.ALGOS[algo]
+        self.wcur = torch.from_numpy(w0).to(device)
+        self.wnext = torch.empty_like(self.wcur)
+        self.S = torch.empty((self.M, self.D), dtype=torch.float64, device=device)
+        self.c = torch.empty(self.M, dtype=torch.float64, device=device)
+        self.bmu = torch.empty(self.N, dtype=torch.int32, device=device)
+        nbytes = native.workspace_bytes(native.OP_FIND_BMUS, self.N, self.M, self.D, self.algo)
+        self.ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+        self.wsp = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
+        self.wsb = nbytes
+        self.penalty = 2.0 if w['topology'] == 'square' else 1.0
+        self.epoch = 0
+
+    def step(self, err_slot, timer=None):
+        t, nat = self.t, self.nat
+        s = t.cuda.current_stream().cuda_stream
+        self.S.zero_()
+        self.c.zero_()
+        if timer is not None:
+            nat.call('somgb_set_kernel_timer', timer[0].cuda_event, timer[1].cuda_event)
+        nat.call('somgb_train_bmu_pass', self.xd.data_ptr(), None, self.N, self.D, self.wcur.data_ptr(),
+                 self.topo.data_ptr(), self.M, self.penalty, self.algo, self.bmu.data_ptr(), err_slot.data_ptr(),
+                 self.wsp, self.wsb, s)
+        if timer is not None:
+            nat.call('somgb_set_kernel_timer', None, None)
+        nat.call('somgb_accumulate', self.xd.data_ptr(), None, self.bmu.data_ptr(), self.N, self.D, self.M,
+                 self.S.data_ptr(), self.c.data_ptr(), s)
+        e = self.epoch % self.w['schedule']
+        sigma = float(np.float32(self.w['sigma0'])) / (1.0 + 2.0 * e / self.w['schedule'])
+        nat.call('somgb_neighbourhood_update', self.S.data_ptr(), self.c.data_ptr(), self.topo.data_ptr(), self.M,
+                 self.D, max(sigma, 1e-12), self.wnext.data_ptr(), None, None, s)
+        self.wcur, self.wnext = self.wnext, self.wcur
+        self.epoch += 1
+
+
+def time_epochs(torch, runner, warmup, steps):
+    errs = torch.zeros((warmup + steps, 3), dtype=torch.float64, device=runner.dev)
+    for i in range(warmup):
+        runner.step(errs[i])
+    torch.cuda.synchronize()
+    kt = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in kt:          # torch creates the CUDA event at its first record; the library re-records these
+        a.record()
+        b.record()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    launches0 = runner.nat.lib().somgb_kernel_launches()
+    start.record()
+    for i in range(steps):
+        runner.step(errs[warmup + i], timer=kt[i])
+    stop.record()
+    torch.cuda.synchronize()
+    launches = runner.nat.lib().somgb_kernel_launches() - launches0
+    total_ms = start.elapsed_time(stop)
+    kernel_ms = [a.elapsed_time(b) for a, b in kt]
+    return total_ms, kernel_ms, launches, errs.cpu().numpy()
+
+
+def gpu_arm(args, ws, rank, local):
+    import torch
+    import torch.distributed as dist
+    from decontamination_gb300 import build as gbuild, _native
+    import decontamination_gb300 as dg
+
+    gbuild.build()
+    torch.cuda.set_device(local)
+    device = torch.device('cuda', local)
+    if ws > 1:
+        dist.init_process_group('nccl', device_id=device)
+    w = WORKLOAD
+    M, D = w['m'] * w['n'], w['d']
+    x, w0 = make_data(args.n, w)
+    N = x.shape[0]
+    topo_np = dg.SOM_Batch(w['m'], w['n'], D, topology=w['topology'])._topography
+    xh = torch.from_numpy(x).pin_memory()
+    xd = xh.to(device)
+    topo = torch.from_numpy(topo_np).to(device)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # --- main: epochs with the catalogue resident ---------------------------------------------------------------------
+    runner = EpochRunner(torch, _native, xd, w0, topo, w, args.algo, device)
+    used_algo = 'tc' if _native.workspace_bytes(_native.OP_FIND_BMUS, N, M, D, _native.ALGO_TC) > 256 and \
+        args.algo != 'fp32' else 'fp32'
+    barrier()
+    with ClockSampler(gpu_bus_id(torch, device)) as clk:
+        total_ms, kernel_ms, launches, errs = time_epochs(torch, runner, args.warmup, args.steps)
+    barrier()
+    clocks = clk.summary()
+    t_max = total_ms
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    ms_per_step = t_max / args.steps
+    value = ws * N * M / (ms_per_step * 1e-3) / 1e9
+    rechecks = np.zeros(1, dtype=np.int64)
+    _native.call('somgb_last_recheck_count', rechecks.ctypes.data, torch.cuda.current_stream().cuda_stream)
+
+    # roofline of the dominant kernel (the BMU pass): algorithmic 2*N*M*D flops per launch
+    peaks, peak_kind = measured_peaks()
+    k_ms = statistics.mean(kernel_ms)
+    flops = 2.0 * N * M * D
+    achieved_tflops = flops / (k_ms * 1e-3) / 1e12
+    peak = peaks.get('bf16_tflops_sustained', peaks.get('bf16_tflops'))
+    roofline = {'bound': 'tensor', 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
+                'frac': achieved_tflops / peak, 'traffic': None,
+                'kernel': 'BMU pass (%s)' % ('tcgen05 split-BF16' if used_algo == 'tc' else 'FP32 CUDA cores'),
+                'kernel_ms': k_ms, 'kernel_share': k_ms * args.steps / total_ms,
+                'peak_source': f'{peak_kind} bf16_tflops_sustained',
+                'hbm_bytes_algorithmic': N * D * 4 + N * 4,
+                'hbm_frac': (N * D * 4 + N * 4) / (k_ms * 1e-3) / 1e9 / peaks.get('hbm_gbs', 6800.0)}
+    out = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'bf16x3-split/f32acc' if used_algo == 'tc' else 'f32',
+        'data': 'synthetic (seeded correlated log-normal, cond 100, 2% rows x10; weights U[-1,1])',
+        'config': {'workload': w['name'], 'algo': used_algo, 'N_per_gpu': N, 'M': M, 'D': D,
+                   'l2': 'catalogue 805 MB > 129 MB L2 per epoch; no flush', 'parallelism': f'replicas x{ws}'},
+        'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clocks,
+        'recheck_last_epoch': int(rechecks[0]),
+        'qe_last': float(errs[-1][0] / errs[-1][2]) if errs[-1][2] > 0 else None,
+    }
+
+    # --- plain FP32 form of the same epoch ------------------------------------------------------------------------------
+    if not args.skip_fp32 and used_algo == 'tc':
+        r32 = EpochRunner(torch, _native, xd, w0, topo, w, 'fp32', device)
+        t32, k32, _, _ = time_epochs(torch, r32, min(args.warmup, 3), max(3, args.steps // 4))
+        n32 = max(3, args.steps // 4)
+        out['fp32_form'] = {'value': N * M / (t32 / n32 * 1e-3) / 1e9, 'ms_per_step': t32 / n32,
+                            'bmu_kernel_ms': statistics.mean(k32)}
+        out['speedup_vs_fp32_form'] = out['fp32_form']['ms_per_step'] / ms_per_step
+
+    # --- end to end through the public API ------------------------------------------------------------------------------
+    if not args.skip_e2e:
+        som = dg.SOM_Batch(w['m'], w['n'], D, topology=w['topology'], sigma=w['sigma0'])
+        som.bmu_algo = args.algo
+        e2e_steps = max(1, min(args.steps, 5))
+        som._weights[...] = w0
+        som.train(xh, n_epochs=1, use_best_epoch=False)      # warm-up (allocations, library state)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            som._weights[...] = w0
+            som.train(xh, n_epochs=1, use_best_epoch=False)
+        barrier()
+        dt = (time.perf_counter() - t0) / e2e_steps
+        h2d = x.nbytes + w0.nbytes + topo_np.nbytes
+        d2h = 2 * w0.nbytes + 3 * 8 * 2
+        out['e2e'] = {'value': ws * N * M / dt / 1e9, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+                      'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3,
+                      'call': 'SOM_Batch.train(pinned host tensor, n_epochs=1): upload, training pass, error pass, '
+                              'weights/history/errors back to the host'}
+
+    # --- CPU baseline (rank 0, N=1) -------------------------------------------------------------------------------------
+    if not args.skip_cpu and rank == 0 and ws == 1:
+        r, ns, nt, dt = cpu_epoch_rate(x, w0, w, seconds=args.cpu_seconds)
+        out['cpu_baseline'] = {'value': r, 'unit': UNIT, 'cores': nt, 'kind': 'port',
+                               'sample': f'first {ns} samples of the workload, one reference-formulation epoch '
+                                         f'(scatter + float32 atomics) and its error pass, {dt:.1f} s'}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == 'reference':
+        reference_arm(args, ws, rank)
+    else:
+        gpu_arm(args, ws, rank, local)
+
+
+if __name__ == '__main__':
+    main()

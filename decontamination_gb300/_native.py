@@ -40,6 +40,13 @@ SIGNATURES = {
     'somgb_last_error': [ctypes.c_char_p, SZ],
     'somgb_workspace_bytes': [I32, I64, I64, I32, I32],
     'somgb_last_recheck_count': [P, P],
+    'somgb_kernel_launches': [],
+    'somgb_algo_supported': [I32, I64, I64, I32],
+    'somgb_device_status': [P, I32, P],
+    'somgb_set_kernel_timer': [P, P],
+    'somgb_train_bmu_pass': [P, P, I64, I32, P, P, I64, D, I32, P, P, P, SZ, P],
+    'somgb_accumulate': [P, P, P, I64, I32, I64, P, P, P],
+    'somgb_accumulate_f64': [P, P, P, I64, I32, I64, P, P, P],
     'somgb_find_bmus': [P, I64, I32, P, I64, I32, P, P, SZ, P],
     'somgb_find_bmus_f64': [P, I64, I32, P, I64, P, P],
     'somgb_count_bmus': [P, P, I64, I32, P, I64, I32, P, P, SZ, P],
@@ -55,7 +62,7 @@ SIGNATURES = {
     'somgb_divide': [P, P, I64, I32, P, P],
     'somgb_divide_f64': [P, P, I64, I32, P, P],
 }
-_RESTYPES = {'somgb_last_error': SZ, 'somgb_workspace_bytes': SZ}
+_RESTYPES = {'somgb_last_error': SZ, 'somgb_workspace_bytes': SZ, 'somgb_kernel_launches': I64}
 
 
 class SomgbError(RuntimeError):

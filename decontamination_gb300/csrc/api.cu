@@ -1,5 +1,6 @@
 // C ABI of libsomgb (declared in include/somgb.h): argument checks, workspace layout and kernel dispatch.
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <string>
 
@@ -24,6 +25,19 @@ namespace {
 thread_local std::string g_last_error;
 thread_local unsigned long long* g_last_counter = nullptr;
 }  // namespace
+
+std::atomic<int64_t> g_launches{0};
+thread_local cudaEvent_t g_timer_start = nullptr;
+thread_local cudaEvent_t g_timer_stop = nullptr;
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void timer_begin(cudaStream_t s) {
+    if (g_timer_start) cudaEventRecord(g_timer_start, s);
+}
+void timer_end(cudaStream_t s) {
+    if (g_timer_stop) cudaEventRecord(g_timer_stop, s);
+}
 
 int set_error(int status, const char* fmt, ...) {
     char buf[1024];
@@ -105,7 +119,9 @@ int check_common(const void* x, int64_t n, int d, const void* w, int64_t m, int 
 int run_pass(PassArgs a, int algo, const Workspace& ws, bool tc, cudaStream_t stream) {
     SOMGB_CUDA_TRY(cudaMemsetAsync(ws.counter, 0, sizeof(unsigned long long), stream));
     a.recheck_count = ws.counter;
-    if (tc) return launch_tc_pass(a, ws.tc, ws.tc_bytes, stream);
+    if (tc && ((uintptr_t)a.x) % 16 == 0) return launch_tc_pass(a, ws.tc, ws.tc_bytes, stream);
+    if (tc && algo == SOMGB_ALGO_TC)
+        return set_error(SOMGB_ERR_INVALID, "the tensor-core pass needs x 16-byte aligned");
     if (algo == SOMGB_ALGO_TC)
         return set_error(SOMGB_ERR_UNSUPPORTED, "tensor-core path unsupported for n=%lld m=%lld d=%d on this device",
                          (long long)a.n, (long long)a.m, a.d);
@@ -135,6 +151,14 @@ size_t somgb_workspace_bytes(int op, int64_t n, int64_t m, int d, int algo) {
     return ws_bytes_for(op, n, m, d, algo, nullptr);
 }
 
+int64_t somgb_kernel_launches(void) { return g_launches.load(); }
+
+int somgb_set_kernel_timer(void* start_event, void* stop_event) {
+    g_timer_start = (cudaEvent_t)start_event;
+    g_timer_stop = (cudaEvent_t)stop_event;
+    return SOMGB_OK;
+}
+
 int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream) {
     if (!count) return set_error(SOMGB_ERR_INVALID, "count is NULL");
     *count = 0;
@@ -144,6 +168,18 @@ int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream) {
     SOMGB_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
     *count = (int64_t)v;
     return SOMGB_OK;
+}
+
+int somgb_device_status(unsigned int* status, int clear, somgb_stream_t stream) {
+    if (!status) return set_error(SOMGB_ERR_INVALID, "status is NULL");
+    if (int s = read_device_status(status, clear != 0, (cudaStream_t)stream)) return s;
+    return SOMGB_OK;
+}
+
+int somgb_algo_supported(int algo, int64_t n, int64_t m, int d) {
+    if (algo == SOMGB_ALGO_FP32 || algo == SOMGB_ALGO_AUTO) return 1;
+    if (algo == SOMGB_ALGO_TC) return tc_supported(n, m, d, SOMGB_ALGO_TC) ? 1 : 0;
+    return 0;
 }
 
 int somgb_find_bmus(const float* x, int64_t n, int d, const float* w, int64_t m, int algo, int32_t* bmu_out,
@@ -204,6 +240,39 @@ int somgb_train_epoch_pass(const float* x, const double* rho, int64_t n, int d, 
     cudaStream_t st = (cudaStream_t)stream;
     if (int s = run_pass(a, algo, W, tc, st)) return s;
     return launch_accumulate<float>(x, rho, a.train_bmu, n, d, m, S, c, st);
+}
+
+int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                         int64_t m, double penalty, int algo, int32_t* bmu_out, double* err3, void* ws,
+                         size_t ws_bytes, somgb_stream_t stream) {
+    if (int s = check_common(x, n, d, w, m, algo)) return s;
+    if (n > 0 && !bmu_out) return set_error(SOMGB_ERR_INVALID, "bmu_out is NULL");
+    if (err3 && !topo) return set_error(SOMGB_ERR_INVALID, "topo is NULL");
+    Workspace W;
+    bool tc = false;
+    if (int s = carve(ws, ws_bytes, SOMGB_OP_FIND_BMUS, n, m, d, algo, &W, &tc)) return s;
+    if (n == 0) return SOMGB_OK;
+    PassArgs a{};
+    a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.topo = topo; a.penalty = penalty;
+    a.err3 = err3; a.train_bmu = bmu_out;
+    a.outs = OUT_TRAIN | (err3 ? OUT_ERR : 0);
+    return run_pass(a, algo, W, tc, (cudaStream_t)stream);
+}
+
+int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
+                     double* c, somgb_stream_t stream) {
+    if (n < 0 || m <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if (n > 0 && (!x || !bmu)) return set_error(SOMGB_ERR_INVALID, "x/bmu is NULL");
+    if (!S || !c) return set_error(SOMGB_ERR_INVALID, "S/c is NULL");
+    return launch_accumulate<float>(x, rho, bmu, n, d, m, S, c, (cudaStream_t)stream);
+}
+
+int somgb_accumulate_f64(const double* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
+                         double* S, double* c, somgb_stream_t stream) {
+    if (n < 0 || m <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if (n > 0 && (!x || !bmu)) return set_error(SOMGB_ERR_INVALID, "x/bmu is NULL");
+    if (!S || !c) return set_error(SOMGB_ERR_INVALID, "S/c is NULL");
+    return launch_accumulate<double>(x, rho, bmu, n, d, m, S, c, (cudaStream_t)stream);
 }
 
 int somgb_neighbourhood_update(const double* S, const double* c, const float* topo, int64_t m, int d, double sigma,

@@ -21,7 +21,11 @@ int set_error(int status, const char* fmt, ...);
                                       __FILE__, __LINE__);                                                  \
     } while (0)
 
-#define SOMGB_LAUNCH_CHECK() SOMGB_CUDA_TRY(cudaGetLastError())
+#define SOMGB_LAUNCH_CHECK() \
+    do {                     \
+        ::somgb::count_launch(); \
+        SOMGB_CUDA_TRY(cudaGetLastError()); \
+    } while (0)
 
 constexpr double FLOAT_EPS = 1.0e-12;   // algo/som_batch.py:24
 
@@ -31,6 +35,11 @@ __host__ __device__ __forceinline__ int64_t max64(int64_t a, int64_t b) { return
 inline size_t align_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
 
 int num_sms();
+
+// Launch bookkeeping (api.cu): the process-wide launch counter and the optional per-thread kernel timer.
+void count_launch();
+void timer_begin(cudaStream_t s);
+void timer_end(cudaStream_t s);
 
 // ---------------------------------------------------------------------------------------------------------------------
 // Device helpers shared by the kernels.

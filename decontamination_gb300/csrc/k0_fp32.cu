@@ -134,10 +134,12 @@ __global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a) {
 template <int DMAX>
 int launch_dmax(const PassArgs& a, cudaStream_t stream) {
     dim3 grid((unsigned)ceil_div(a.n, K0_THREADS));
+    timer_begin(stream);
     if (a.outs & OUT_ERR)
         k0_pass_kernel<DMAX, true><<<grid, K0_THREADS, 0, stream>>>(a);
     else
         k0_pass_kernel<DMAX, false><<<grid, K0_THREADS, 0, stream>>>(a);
+    timer_end(stream);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }

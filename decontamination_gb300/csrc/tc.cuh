@@ -7,8 +7,12 @@ namespace somgb {
 
 // True when the tensor-core pass handles this shape on the current device for `algo`.
 bool tc_supported(int64_t n, int64_t m, int d, int algo);
+// Shape limits of the tensor-core pass (host-only check, no device query).
+bool tc_shape_ok(int64_t m, int d);
 // Scratch bytes of the tensor-core pass (prepared unit operand, recheck list).
 size_t tc_workspace_bytes(int64_t n, int64_t m, int d);
 int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t stream);
+// Reads (and optionally clears) the device status word that bounded waits set when they give up.
+int read_device_status(unsigned int* status, bool clear, cudaStream_t stream);
 
 }  // namespace somgb

@@ -7,6 +7,7 @@ on the current CUDA device; ``enable_gpu`` and ``threads_per_blocks`` are
 accepted for compatibility and ignored (there is no CPU path).
 """
 
+import ctypes
 import math
 import typing
 
@@ -224,6 +225,15 @@ class SOM_Abstract(object):
         _native.call('somgb_last_recheck_count', cnt.ctypes.data, _device.stream())
         self._last_recheck_count = int(cnt[0])
 
+    @staticmethod
+    def _check_device():
+        """Raises if a bounded device-side wait gave up during the calls since the last check."""
+        st = ctypes.c_uint(0)
+        _native.call('somgb_device_status', ctypes.addressof(st), 1, _device.stream())
+        if st.value:
+            raise _native.SomgbError(_native.SOMGB_ERR_TIMEOUT,
+                                     f'a device-side wait gave up (status {st.value:#x}); results are incomplete')
+
     # -- projection calls -------------------------------------------------------------------------------------------------
 
     def compute_errors(self, dataset, dataset_weights=None, show_progress_bar: bool = False, enable_gpu: bool = True,
@@ -247,6 +257,7 @@ class SOM_Abstract(object):
                              topo.data_ptr(), M, self._penalty, self._algo, out.data_ptr(), wsp, wsb,
                              _device.stream())
         o = out.cpu().numpy()
+        self._check_device()
         return (o[0] / o[2], o[1] / o[2]) if o[2] > 0.0 else (np.nan, np.nan)
 
     def get_activation_map(self, dataset, dataset_weights=None, show_progress_bar: bool = False,
@@ -265,7 +276,9 @@ class SOM_Abstract(object):
                 wsp, wsb = self._ws.for_op(_native.OP_COUNT_BMUS, n, M, D, self._algo, device)
                 _native.call('somgb_count_bmus', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), M, self._algo,
                              hist.data_ptr(), wsp, wsb, _device.stream())
-        return hist.cpu().numpy().astype(self._dtype).reshape((self._m, self._n))
+        h = hist.cpu().numpy()
+        self._check_device()
+        return h.astype(self._dtype).reshape((self._m, self._n))
 
     def get_winners(self, dataset, enable_gpu: bool = True,
                     threads_per_blocks: typing.Optional[int] = None) -> np.ndarray:
@@ -284,4 +297,6 @@ class SOM_Abstract(object):
             _native.call('somgb_find_bmus', x.data_ptr(), n, D, w.data_ptr(), M, self._algo, out.data_ptr(), wsp, wsb,
                          _device.stream())
             self._record_recheck()
-        return out.cpu().numpy()
+        res = out.cpu().numpy()
+        self._check_device()
+        return res

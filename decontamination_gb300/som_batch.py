@@ -187,6 +187,7 @@ class SOM_Batch(SOM_Abstract):
             for e in range(done):
                 self._quantization_errors[e], self._topographic_errors[e] = self._errors_of(eh[e + 1])
         self._weights[:] = history[done - 1].cpu().numpy() if done > 0 else self._weights
+        self._check_device()
 
     def _train_vectors(self, dataset, dataset_weights, n_vectors):
         device = _device.require_cuda()

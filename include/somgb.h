@@ -64,6 +64,25 @@ size_t somgb_workspace_bytes(int op, int64_t n, int64_t m, int d, int algo);
 int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream);
 
 /*
+ * Device status word of the current device (synchronises `stream`): 0 while healthy; non-zero once a bounded
+ * device-side wait of a tensor-core pass gave up, in which case that pass returned early and its outputs are
+ * incomplete. Sticky until read with clear != 0.
+ */
+int somgb_device_status(unsigned int* status, int clear, somgb_stream_t stream);
+
+/* 1 if `algo` can run a pass of these sizes on the current device, else 0. */
+int somgb_algo_supported(int algo, int64_t n, int64_t m, int d);
+
+/* Kernels this library has launched in this process (diagnostic). */
+int64_t somgb_kernel_launches(void);
+
+/*
+ * Diagnostic timer: while set (non-NULL cudaEvent_t handles), every BMU pass on the calling thread records
+ * `start` on its stream just before its dominant kernel and `stop` just after it. Pass NULLs to clear.
+ */
+int somgb_set_kernel_timer(void* start_event, void* stop_event);
+
+/*
  * BMU of every sample: bmu_out[i] = argmin_j |x_i - w_j|^2, 0 when every distance is NaN.
  * Replaces _find_bmus_kernel / _find_bmu_xpu (algo/som_abstract.py:736-783), called by get_winners (:670-695).
  */
@@ -109,6 +128,20 @@ int somgb_train_epoch_pass(const float* x, const double* rho, int64_t n, int d, 
 int somgb_train_epoch_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w,
                                const double* topo, int64_t m, double penalty, double* S, double* c, double* err3,
                                void* ws, size_t ws_bytes, somgb_stream_t stream);
+
+/*
+ * The two halves of somgb_train_epoch_pass as separate calls.
+ * somgb_train_bmu_pass: bmu_out[i] = training BMU of sample i (-1 when (float)rho_i <= 0 or no unit is valid),
+ *   plus the error sums of `w` into err3 when err3 != NULL. Workspace: SOMGB_OP_FIND_BMUS sizing.
+ * somgb_accumulate: S[b_i] += (double)(float)rho_i * x_i, c[b_i] += (double)(float)rho_i for b_i >= 0 ("+=").
+ */
+int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                         int64_t m, double penalty, int algo, int32_t* bmu_out, double* err3, void* ws,
+                         size_t ws_bytes, somgb_stream_t stream);
+int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
+                     double* c, somgb_stream_t stream);
+int somgb_accumulate_f64(const double* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
+                         double* S, double* c, somgb_stream_t stream);
 
 /*
  * Neighbourhood contraction and weight update of one epoch:

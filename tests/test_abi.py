@@ -17,7 +17,7 @@ HEADER = os.path.join(ROOT, 'include', 'somgb.h')
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
-    return sorted(set(re.findall(r'^\s*(?:int|size_t)\s+(somgb_\w+)\s*\(', text, flags=re.M)))
+    return sorted(set(re.findall(r'^\s*(?:int|size_t|int64_t)\s+(somgb_\w+)\s*\(', text, flags=re.M)))
 
 
 def test_header_declares_entry_points():

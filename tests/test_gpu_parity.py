@@ -17,7 +17,7 @@ from conftest import golden
 
 pytestmark = pytest.mark.gpu
 
-ALGOS = ['fp32', 'auto']
+ALGOS = ['fp32', 'auto', 'tc']
 W_RTOL = 1e-5          # trained weights vs the float64 oracle
 ERR_RTOL = 1e-9        # error sums: float64, summation order differs
 
@@ -39,6 +39,19 @@ def _som(m, n, d, w, topology='square', algo='auto', sigma=None, dtype=np.float3
     return som
 
 
+def _tc_ok(native, n, m, d):
+    return bool(native.lib().somgb_algo_supported(native.ALGO_TC, n, m, d))
+
+
+def _skip_unsupported_tc(native, algo, n, m, d, call):
+    """For algo 'tc' on a shape outside the tensor-core limits the call must fail loudly (no silent fallback)."""
+    if algo == 'tc' and not _tc_ok(native, n, m, d):
+        with pytest.raises(native.SomgbError) as ei:
+            call()
+        assert ei.value.status == native.SOMGB_ERR_UNSUPPORTED
+        pytest.skip('shape outside the tensor-core limits (checked that it is refused)')
+
+
 # ----------------------------------------------------------------------------------------------------------------------
 # projection calls
 # ----------------------------------------------------------------------------------------------------------------------
@@ -55,6 +68,7 @@ def test_winners_bit_exact(cuda, native, oracle, algo, m, n, d, N):
     x = _rand(rng, N, d, 'lognormal' if d >= 16 else 'uniform')
     w = x[rng.integers(0, N, m * n)] + 0.01 * rng.standard_normal((m * n, d)).astype(np.float32)
     som = _som(m, n, d, w, algo=algo)
+    _skip_unsupported_tc(native, algo, N, m * n, d, lambda: som.get_winners(x))
     got = som.get_winners(x)
     want = oracle.find_bmus(w.astype(np.float32), x, 'numba')
     assert got.dtype == np.int32
@@ -93,6 +107,8 @@ def test_errors_and_activation_vs_oracle(cuda, native, oracle, algo, topology):
 def test_edge_cases_golden(cuda, native, algo):
     """NaN features and rows, a NaN unit, exact ties between duplicated units, zero and negative densities."""
     g = golden('edge_projection')
+    if algo == 'tc':
+        pytest.skip('D=6 is outside the tensor-core limits; the padded variant below covers the same cases')
     som = _som(4, 5, 6, g['w0'], algo=algo)
     assert np.array_equal(som.get_winners(g['x']), g['winners'])
     assert np.array_equal(som.get_activation_map(g['x']), g['activation'])
@@ -109,10 +125,13 @@ def test_infinities_and_empty(cuda, native, oracle, algo):
     x[3, 1] = np.inf
     x[4] = [1e20, -1e20, 3e19]          # float32 squares overflow
     w[2, 0] = np.inf
-    som = _som(3, 3, 3, w, algo=algo)
+    if algo == 'tc':
+        w = np.concatenate([w, np.zeros((9, 1), np.float32)], axis=1)   # the tensor-core pass needs D % 4 == 0
+        x = np.concatenate([x, np.zeros((64, 1), np.float32)], axis=1)
+    som = _som(3, 3, w.shape[1], w, algo=algo)
     assert np.array_equal(som.get_winners(x), oracle.find_bmus(w, x, 'numba'))
-    assert som.get_winners(np.zeros((0, 3), np.float32)).shape == (0,)
-    assert np.all(som.get_activation_map(np.zeros((0, 3), np.float32)) == 0)
+    assert som.get_winners(np.zeros((0, w.shape[1]), np.float32)).shape == (0,)
+    assert np.all(som.get_activation_map(np.zeros((0, w.shape[1]), np.float32)) == 0)
 
 
 # ----------------------------------------------------------------------------------------------------------------------
@@ -247,3 +266,64 @@ def test_c_abi_epoch_pass_accumulators(cuda, native, oracle):
         native.call('somgb_train_epoch_pass', xd.data_ptr(), None, N, D, wd.data_ptr(), td.data_ptr(), M, 2.0,
                     native.ALGO_AUTO, S.data_ptr(), c.data_ptr(), None, None, wsp, nbytes - 1, s)
     assert ei.value.status == native.SOMGB_ERR_WORKSPACE
+
+
+def test_edge_cases_tc_padded(cuda, native):
+    """The golden edge cases through the tensor-core pass: two zero features pad D=6 to 8 without changing any
+    distance, so every output must equal the reference's."""
+    g = golden('edge_projection')
+    pad = lambda a: np.concatenate([a, np.zeros((a.shape[0], 2), a.dtype)], axis=1)
+    som = _som(4, 5, 8, pad(g['w0']), algo='tc')
+    x = pad(g['x'])
+    assert np.array_equal(som.get_winners(x), g['winners'])
+    assert np.array_equal(som.get_activation_map(x), g['activation'])
+    assert np.array_equal(som.get_activation_map(x, g['rho']), g['activation_weighted'])
+    np.testing.assert_allclose(som.compute_errors(x), g['errors'], rtol=1e-6)
+    np.testing.assert_allclose(som.compute_errors(x, g['rho']), g['errors_weighted'], rtol=1e-6)
+
+
+TC_STRESS = [
+    ('lognormal-outliers', 16, 32, 32, 200_000),
+    ('mixture', 8, 16, 16, 150_000),
+    ('near-ties', 16, 16, 16, 100_000),
+    ('far-offset', 4, 20, 20, 100_000),
+    ('uniform', 32, 8, 16, 60_000),
+    ('duplicates', 8, 10, 10, 50_000),
+]
+
+
+@pytest.mark.parametrize('kind,d,m,n,N', TC_STRESS)
+def test_tc_stress_vs_oracle(cuda, native, oracle, kind, d, m, n, N):
+    """BMUs, second BMUs (through the error sums) and activation counts of the tensor-core pass on inputs built to
+    stress its error bound: outliers, near-tied units, data far from the origin, duplicated units."""
+    from decontamination_gb300 import synthetic
+    rng = np.random.default_rng(hash(kind) % 2**32)
+    M = m * n
+    if kind == 'lognormal-outliers':
+        x = synthetic.correlated_lognormal(N, d, 7)
+        w = x[rng.integers(0, N, M)] * (1 + 0.01 * rng.standard_normal((M, d))).astype(np.float32)
+    elif kind == 'mixture':
+        x = synthetic.gaussian_mixture(N, d, 8)
+        w = x[rng.integers(0, N, M)].copy()
+    elif kind == 'near-ties':
+        x = rng.random((N, d), dtype=np.float32)
+        base = rng.random((M // 2, d), dtype=np.float32)
+        w = np.concatenate([base, base * (1 + 1e-6 * rng.standard_normal(base.shape)).astype(np.float32)])
+    elif kind == 'far-offset':
+        x = (1.0e4 + rng.standard_normal((N, d))).astype(np.float32)
+        w = (1.0e4 + 0.7 * rng.standard_normal((M, d))).astype(np.float32)
+    elif kind == 'uniform':
+        x = rng.random((N, d), dtype=np.float32)
+        w = rng.random((M, d), dtype=np.float32)
+    else:
+        x = synthetic.gaussian_mixture(N, d, 9)
+        w = x[rng.integers(0, N, M)].copy()
+        w[M // 2:] = w[:M - M // 2]
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    som = _som(m, n, d, w, algo='tc')
+    assert np.array_equal(som.get_winners(x), oracle.find_bmus(w, x, 'numba'))
+    h = oracle.count_bmus(w, x, None, 'numba')
+    assert np.array_equal(som.get_activation_map(x).ravel(), h.astype(np.float32))
+    topo = oracle.topography(m, n, 'square')
+    o = oracle.compute_errors_raw(w, topo, x, None, 2.0, 'numba')
+    np.testing.assert_allclose(som.compute_errors(x), o[:2] / o[2], rtol=ERR_RTOL)
