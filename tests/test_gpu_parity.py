@@ -91,7 +91,7 @@ def test_kat_activation_map_exact(cuda, native, algo):
 @pytest.mark.parametrize('topology', ['square', 'hexagonal'])
 def test_errors_and_activation_vs_oracle(cuda, native, oracle, algo, topology):
     rng = np.random.default_rng(3)
-    m, n, d, N = 12, 10, 6, 30_000
+    m, n, d, N = 12, 10, 8, 30_000
     x = _rand(rng, N, d, 'mixture')
     w = x[rng.integers(0, N, m * n)].copy()
     rho = rng.standard_normal(N)
