@@ -221,9 +221,11 @@ class EpochRunner:
         self.penalty = 2.0 if w['topology'] == 'square' else 1.0
         self.epoch = 0
 
-    def step(self, err_slot, timer=None):
+    def step(self, err_slot, timer=None, phases=None):
         t, nat = self.t, self.nat
         s = t.cuda.current_stream().cuda_stream
+        if phases is not None:
+            phases[0].record()
         self.S.zero_()
         self.c.zero_()
         if timer is not None:
@@ -233,12 +235,18 @@ class EpochRunner:
                  self.wsp, self.wsb, s)
         if timer is not None:
             nat.call('somgb_set_kernel_timer', None, None)
+        if phases is not None:
+            phases[1].record()
         nat.call('somgb_accumulate', self.xd.data_ptr(), None, self.bmu.data_ptr(), self.N, self.D, self.M,
                  self.S.data_ptr(), self.c.data_ptr(), s)
+        if phases is not None:
+            phases[2].record()
         e = self.epoch % self.w['schedule']
         sigma = float(np.float32(self.w['sigma0'])) / (1.0 + 2.0 * e / self.w['schedule'])
         nat.call('somgb_neighbourhood_update', self.S.data_ptr(), self.c.data_ptr(), self.topo.data_ptr(), self.M,
                  self.D, max(sigma, 1e-12), self.wnext.data_ptr(), None, None, s)
+        if phases is not None:
+            phases[3].record()
         self.wcur, self.wnext = self.wnext, self.wcur
         self.epoch += 1
 
@@ -263,7 +271,14 @@ def time_epochs(torch, runner, warmup, steps):
     launches = runner.nat.lib().somgb_kernel_launches() - launches0
     total_ms = start.elapsed_time(stop)
     kernel_ms = [a.elapsed_time(b) for a, b in kt]
-    return total_ms, kernel_ms, launches, errs.cpu().numpy()
+    # one more (untimed) epoch with events between its phases, for the breakdown
+    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    extra = torch.zeros(3, dtype=torch.float64, device=runner.dev)
+    runner.step(extra, phases=ph)
+    torch.cuda.synchronize()
+    phases = {'bmu_pass_ms': ph[0].elapsed_time(ph[1]), 'accumulate_ms': ph[1].elapsed_time(ph[2]),
+              'neighbourhood_update_ms': ph[2].elapsed_time(ph[3])}
+    return total_ms, kernel_ms, launches, errs.cpu().numpy(), phases
 
 
 def gpu_arm(args, ws, rank, local):
@@ -297,7 +312,7 @@ def gpu_arm(args, ws, rank, local):
         args.algo != 'fp32' else 'fp32'
     barrier()
     with ClockSampler(gpu_bus_id(torch, device)) as clk:
-        total_ms, kernel_ms, launches, errs = time_epochs(torch, runner, args.warmup, args.steps)
+        total_ms, kernel_ms, launches, errs, phases = time_epochs(torch, runner, args.warmup, args.steps)
     barrier()
     clocks = clk.summary()
     t_max = total_ms
@@ -330,7 +345,7 @@ def gpu_arm(args, ws, rank, local):
         'data': 'synthetic (seeded correlated log-normal, cond 100, 2% rows x10; weights U[-1,1])',
         'config': {'workload': w['name'], 'algo': used_algo, 'N_per_gpu': N, 'M': M, 'D': D,
                    'l2': 'catalogue 805 MB > 129 MB L2 per epoch; no flush', 'parallelism': f'replicas x{ws}'},
-        'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clocks,
+        'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clocks, 'phases': phases,
         'recheck_last_epoch': int(rechecks[0]),
         'qe_last': float(errs[-1][0] / errs[-1][2]) if errs[-1][2] > 0 else None,
     }
@@ -338,10 +353,10 @@ def gpu_arm(args, ws, rank, local):
     # --- plain FP32 form of the same epoch ------------------------------------------------------------------------------
     if not args.skip_fp32 and used_algo == 'tc':
         r32 = EpochRunner(torch, _native, xd, w0, topo, w, 'fp32', device)
-        t32, k32, _, _ = time_epochs(torch, r32, min(args.warmup, 3), max(3, args.steps // 4))
+        t32, k32, _, _, ph32 = time_epochs(torch, r32, min(args.warmup, 3), max(3, args.steps // 4))
         n32 = max(3, args.steps // 4)
         out['fp32_form'] = {'value': N * M / (t32 / n32 * 1e-3) / 1e9, 'ms_per_step': t32 / n32,
-                            'bmu_kernel_ms': statistics.mean(k32)}
+                            'bmu_kernel_ms': statistics.mean(k32), 'phases': ph32}
         out['speedup_vs_fp32_form'] = out['fp32_form']['ms_per_step'] / ms_per_step
 
     # --- end to end through the public API ------------------------------------------------------------------------------

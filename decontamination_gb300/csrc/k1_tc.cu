@@ -45,11 +45,13 @@ namespace {
 
 constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
-constexpr int CAP = 16;           // candidates kept per row
+constexpr int SLICES = 4;         // epilogue warps per TMEM lane quarter, each owning 64 of 256 columns
+constexpr int CAPS = 8;           // candidates kept per row and slice
 constexpr int XSTAGES = 3;
-constexpr int NUM_THREADS = 192;
-constexpr int MMA_WARP = 4;
-constexpr int TMA_WARP = 5;
+constexpr int EPI_WARPS = 4 * SLICES;
+constexpr int MMA_WARP = EPI_WARPS;
+constexpr int TMA_WARP = EPI_WARPS + 1;
+constexpr int NUM_THREADS = (EPI_WARPS + 2) * 32;
 constexpr float BIG = 3.0e38f;    // s~ of padding / invalid units
 constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go to the exact recheck
 constexpr uint32_t IDESC = ptx::idesc_bf16_f32(TM, TN);
@@ -59,7 +61,7 @@ struct TcShape {
     int64_t mpad = 0;
     int utiles = 0;
     size_t b_bytes = 0, a_bytes = 0, x_bytes = 0;
-    size_t off_a = 0, off_x = 0, off_cand = 0, off_xn = 0, off_flag = 0, off_center = 0, off_bar = 0, smem = 0;
+    size_t off_a = 0, off_x = 0, off_cand = 0, off_part = 0, off_res = 0, off_center = 0, off_bar = 0, smem = 0;
 };
 
 TcShape tc_shape(int64_t m, int d) {
@@ -78,11 +80,11 @@ TcShape tc_shape(int64_t m, int d) {
     s.off_x = off;
     off += XSTAGES * s.x_bytes;
     s.off_cand = off;
-    off += (size_t)CAP * TM * 4;
-    s.off_xn = off;
-    off += 2 * TM * 4;
-    s.off_flag = off;
-    off += 2 * TM * 4;
+    off += (size_t)SLICES * CAPS * TM * 4;
+    s.off_part = off;
+    off += (size_t)SLICES * TM * 8;
+    s.off_res = off;
+    off += (size_t)SLICES * 7 * TM * 4;
     s.off_center = off;
     off += align_up((size_t)d * 4, 16);
     s.off_bar = align_up(off, 8);
@@ -212,7 +214,7 @@ struct TcArgs {
     int kpad;
     int utiles;
     float alpha, beta;
-    size_t off_a, off_x, off_cand, off_xn, off_flag, off_center, off_bar, a_stride, x_stride;
+    size_t off_a, off_x, off_cand, off_part, off_res, off_center, off_bar, a_stride, x_stride;
     uint32_t b_bytes;
 };
 
@@ -247,9 +249,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
-    int32_t* sCand = (int32_t*)(smem + P.off_cand);
-    float* sXn = (float*)(smem + P.off_xn);
-    int* sFlag = (int*)(smem + P.off_flag);
+    int32_t* sCand = (int32_t*)(smem + P.off_cand);   // [slice][CAPS][TM]
+    float2* sPart = (float2*)(smem + P.off_part);     // [slice][TM]: (m1, m2) of the slice
+    float* sResD = (float*)(smem + P.off_res);        // [slice][3][TM]: best float32 distances of the slice
+    int32_t* sResJ = (int32_t*)(smem + P.off_res + (size_t)SLICES * 3 * TM * 4);
+    int32_t* sResN = (int32_t*)(smem + P.off_res + (size_t)SLICES * 6 * TM * 4);   // [slice][TM] candidate count
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
     uint64_t* x_full = bars + 1;    // [3]
@@ -274,13 +278,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         ptx::mbar_init(b_full, 1);
         for (int s = 0; s < XSTAGES; ++s) {
             ptx::mbar_init(x_full + s, 1);
-            ptx::mbar_init(x_empty + s, 4);
+            ptx::mbar_init(x_empty + s, EPI_WARPS);
         }
         for (int s = 0; s < 2; ++s) {
-            ptx::mbar_init(a_full + s, 4);
+            ptx::mbar_init(a_full + s, EPI_WARPS);
             ptx::mbar_init(a_empty + s, 1);
             ptx::mbar_init(t_full + s, 1);
-            ptx::mbar_init(t_empty + s, 4);
+            ptx::mbar_init(t_empty + s, EPI_WARPS);
         }
         ptx::mbar_init(drain, 1);
         ptx::fence_mbar_init();
@@ -367,30 +371,34 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             if (!ptx::mbar_wait(drain, 0)) fail(256u);
         }
     } else {
-        // ----------------------------------------- converter + epilogue (warps 0-3) -----------------------------------
-        const int row = tid;                    // == TMEM lane
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        // ------------------------------ converter + epilogue (warps 0..15) -----------------------------------------
+        // warp e: TMEM lane quarter q = e & 3 (rows 32q..32q+31), column slice sl = e >> 2 (64 of each 256 columns)
+        const int q = warp & 3, sl = warp >> 2;
+        const int row = q * 32 + lane;
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
         const float g32 = (float)(d + 2) * 5.9604645e-8f;
         const float fac = 1.0f + 8.0f * g32;
         double e0 = 0.0, e1 = 0.0, e2 = 0.0;
-        int64_t gcons = 0;                      // TMEM tiles consumed
+        int64_t gcons = 0;   // TMEM tiles consumed
 
+        auto qbar = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(1 + q) : "memory"); };
+
+        // centred split-BF16 A row: this thread writes the 16-byte chunks k0 = 8*(sl + 4c) of row `row`
         auto convert = [&](int64_t it) -> bool {
             const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
             if (it >= 2 && !ptx::mbar_wait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
             if (!ptx::mbar_wait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
             const float* xs = (const float*)(smem + P.off_x + s3 * P.x_stride) + row * d;
             uint8_t* at = smem + P.off_a + s2 * P.a_stride;
-            float xn = 0.0f;
             bool finite = true;
+            float xn = 0.0f;
             for (int k = 0; k < d; ++k) {
-                float t = xs[k] - sCenter[k];
+                const float t = xs[k] - sCenter[k];
                 finite = finite && isfinite(t);
                 xn = fmaf(t, t, xn);
             }
             finite = finite && (xn < HUGE_S);
-            // A row in 16-byte chunks of 8 BF16 values
-            for (int k0 = 0; k0 < kpad; k0 += 8) {
+            for (int k0 = 8 * sl; k0 < kpad; k0 += 8 * SLICES) {
                 __align__(16) __nv_bfloat16 v[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
@@ -410,136 +418,203 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 }
                 *(uint4*)(at + canon_off(row, k0, kpad)) = *(const uint4*)v;
             }
-            sXn[s2 * TM + row] = xn;
-            sFlag[s2 * TM + row] = finite ? 0 : 1;
             ptx::fence_proxy_async();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(a_full + s2);
             return true;
         };
 
+        // two 32-column chunks of this warp's slice of TMEM tile `buf`, loaded back to back
+        auto load64 = [&](int buf, float (&v0)[32], float (&v1)[32]) {
+            const uint32_t base = tbase + lane_base + (uint32_t)(buf * TN + sl * 64);
+            uint32_t r0[32], r1[32];
+            ptx::tmem_ld32_raw(base, r0);
+            ptx::tmem_ld32_raw(base + 32, r1);
+            ptx::tmem_wait_ld2(r0, r1);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                v0[i] = __uint_as_float(r0[i]);
+                v1[i] = __uint_as_float(r1[i]);
+            }
+        };
+
         bool ok = n_my > 0 ? convert(0) : true;
         for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
             if (it + 1 < n_my && !(ok = convert(it + 1))) break;
-            const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
+            const int s3 = (int)(it % XSTAGES);
             const int64_t tile = blockIdx.x + it * gridDim.x;
             const int64_t grow = tile * TM + row;
             const bool live = grow < a.n;
-            const float xn = sXn[s2 * TM + row];
-            bool flagged = sFlag[s2 * TM + row] != 0;
+            const float* xs = (const float*)(smem + P.off_x + s3 * P.x_stride) + row * d;
+            bool flagged = false;
+            float xn = 0.0f;
+            for (int k = 0; k < d; ++k) {
+                const float t = xs[k] - sCenter[k];
+                flagged = flagged || !isfinite(t);
+                xn = fmaf(t, t, xn);
+            }
+            flagged = flagged || !(xn < HUGE_S);
 
-            // sweep 1: best (and second best) s~ of the row
-            float m1 = INFINITY, m2 = INFINITY;
+            // ---- sweep 1: best (and second best) s~ of the row over this warp's columns -------------------------
+            float a1 = INFINITY, a2 = INFINITY, b1 = INFINITY, b2 = INFINITY;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
                 ptx::tc_fence_after();
-                for (int c = 0; c < TN; c += 32) {
-                    float v[32];
-                    ptx::tmem_ld32(tbase + lane_base + (uint32_t)(buf * TN + c), v);
-                    if (ERR) {
-#pragma unroll
-                        for (int i = 0; i < 32; i += 2) {
-                            const float lo = fminf(v[i], v[i + 1]), hi = fmaxf(v[i], v[i + 1]);
-                            m2 = fminf(fminf(m2, hi), fmaxf(m1, lo));
-                            m1 = fminf(m1, lo);
-                        }
-                    } else {
-                        float t0 = v[0], t1 = v[1], t2 = v[2], t3 = v[3];
-#pragma unroll
-                        for (int i = 4; i < 32; i += 4) {
-                            t0 = fminf(t0, v[i]);
-                            t1 = fminf(t1, v[i + 1]);
-                            t2 = fminf(t2, v[i + 2]);
-                            t3 = fminf(t3, v[i + 3]);
-                        }
-                        m1 = fminf(m1, fminf(fminf(t0, t1), fminf(t2, t3)));
-                    }
-                }
+                float v0[32], v1[32];
+                load64(buf, v0, v1);
                 ptx::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) ptx::mbar_arrive(t_empty + buf);
+                if (ERR) {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 2) {
+                        const float lo = fminf(v0[i], v0[i + 1]), hi = fmaxf(v0[i], v0[i + 1]);
+                        a2 = fminf(fminf(a2, hi), fmaxf(a1, lo));
+                        a1 = fminf(a1, lo);
+                        const float lo2 = fminf(v1[i], v1[i + 1]), hi2 = fmaxf(v1[i], v1[i + 1]);
+                        b2 = fminf(fminf(b2, hi2), fmaxf(b1, lo2));
+                        b1 = fminf(b1, lo2);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 2) {
+                        a1 = fminf(a1, fminf(v0[i], v0[i + 1]));
+                        b1 = fminf(b1, fminf(v1[i], v1[i + 1]));
+                    }
+                }
             }
             if (!ok) break;
-            const float mref = ERR ? m2 : m1;
-            if (!(m1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
+            {
+                const float m1 = fminf(a1, b1);
+                const float m2 = fminf(fmaxf(a1, b1), fminf(a2, b2));
+                sPart[sl * TM + row] = make_float2(m1, m2);
+            }
+            qbar();
+            float M1 = INFINITY, M2 = INFINITY;
+#pragma unroll
+            for (int t = 0; t < SLICES; ++t) {
+                const float2 p = sPart[t * TM + row];
+                M2 = fminf(fminf(M2, p.y), fmaxf(M1, p.x));
+                M1 = fminf(M1, p.x);
+            }
+            const float mref = ERR ? M2 : M1;
+            if (!(M1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
             const float dref = fmaxf(0.0f, mref + xn);
             const float thr = flagged ? -INFINITY
                                       : mref + 2.0f * (P.alpha * xn + P.beta * dref) / (1.0f - P.beta) + 1.0e-30f;
 
-            // sweep 2: every unit under the threshold, in ascending unit order
+            // ---- sweep 2: every unit of this warp's columns under the threshold, in ascending order --------------
             int cnt = 0;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
                 ptx::tc_fence_after();
-                for (int c = 0; c < TN; c += 32) {
-                    float v[32];
-                    ptx::tmem_ld32(tbase + lane_base + (uint32_t)(buf * TN + c), v);
+                float v0[32], v1[32];
+                load64(buf, v0, v1);
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(t_empty + buf);
+                const int jb = u * TN + sl * 64;
 #pragma unroll
-                    for (int g4 = 0; g4 < 32; g4 += 4) {
-                        const float gm = fminf(fminf(v[g4], v[g4 + 1]), fminf(v[g4 + 2], v[g4 + 3]));
+                for (int half = 0; half < 2; ++half) {
+                    const float* v = half ? v1 : v0;
+#pragma unroll
+                    for (int g8 = 0; g8 < 32; g8 += 8) {
+                        const float gm = fminf(fminf(fminf(v[g8], v[g8 + 1]), fminf(v[g8 + 2], v[g8 + 3])),
+                                               fminf(fminf(v[g8 + 4], v[g8 + 5]), fminf(v[g8 + 6], v[g8 + 7])));
                         if (gm <= thr) {
 #pragma unroll
-                            for (int i = 0; i < 4; ++i) {
-                                const int64_t j = (int64_t)u * TN + c + g4 + i;
-                                if (v[g4 + i] <= thr && j < a.m) {
-                                    if (cnt < CAP) sCand[cnt * TM + row] = (int32_t)j;
+                            for (int i = 0; i < 8; ++i) {
+                                const int j = jb + half * 32 + g8 + i;
+                                if (v[g8 + i] <= thr && j < (int)a.m) {
+                                    if (cnt < CAPS) sCand[(sl * CAPS + cnt) * TM + row] = j;
                                     ++cnt;
                                 }
                             }
                         }
                     }
                 }
-                ptx::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(t_empty + buf);
             }
             if (!ok) break;
 
-            // resolve the candidates exactly
-            if (live) {
-                if (flagged || cnt == 0 || cnt > CAP) {
-                    const unsigned long long slot = atomicAdd(P.row_count, 1ull);
-                    P.rows[slot] = (int32_t)grow;
-                } else {
-                    const float* xs = (const float*)(smem + P.off_x + s3 * P.x_stride) + row * d;
-                    // float32 screening: (df, j) order, best three
-                    float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
-                    int32_t c1 = -1, c2 = -1, c3 = -1;
-                    for (int q = 0; q < cnt; ++q) {
-                        const int32_t j = sCand[q * TM + row];
+            // ---- resolution: float32 distances of this slice's candidates, merged by slice 0 ---------------------
+            {
+                float f[3] = {INFINITY, INFINITY, INFINITY};
+                int32_t c[3] = {-1, -1, -1};
+                if (live && !flagged && cnt <= CAPS) {
+                    for (int k = 0; k < cnt; ++k) {
+                        const int32_t j = sCand[(sl * CAPS + k) * TM + row];
                         const float df = cand_dist32(a.w + (int64_t)j * d, xs, d);
-                        if (df < f3) {
-                            if (df < f2) {
-                                f3 = f2; c3 = c2;
-                                if (df < f1) { f2 = f1; c2 = c1; f1 = df; c1 = j; }
-                                else { f2 = df; c2 = j; }
-                            } else { f3 = df; c3 = j; }
+                        if (df < f[2]) {
+                            if (df < f[1]) {
+                                f[2] = f[1]; c[2] = c[1];
+                                if (df < f[0]) { f[1] = f[0]; c[1] = c[0]; f[0] = df; c[0] = j; }
+                                else { f[1] = df; c[1] = j; }
+                            } else { f[2] = df; c[2] = j; }
                         }
                     }
-                    bool certain = c1 >= 0 && (f2 > fmaf(f1, fac, 1.0e-37f));
-                    if (ERR) certain = certain && c2 >= 0 && (f3 > fmaf(f2, fac, 1.0e-37f));
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    sResD[(sl * 3 + k) * TM + row] = f[k];
+                    sResJ[(sl * 3 + k) * TM + row] = c[k];
+                }
+                sResN[sl * TM + row] = cnt;
+            }
+            qbar();
+            if (sl == 0 && live) {
+                // merge the slices' best three in (float32 distance, unit) order
+                float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
+                int32_t c1 = -1, c2 = -1, c3 = -1;
+                int total = 0;
+                bool overflow = false;
+                for (int t = 0; t < SLICES; ++t) {
+                    const int n_t = sResN[t * TM + row];
+                    total += n_t;
+                    overflow = overflow || n_t > CAPS;
+                    for (int k = 0; k < 3; ++k) {
+                        const float df = sResD[(t * 3 + k) * TM + row];
+                        const int32_t j = sResJ[(t * 3 + k) * TM + row];
+                        if (j < 0) continue;
+                        const bool lt3 = df < f3 || (df == f3 && (c3 < 0 || j < c3));
+                        if (!lt3) continue;
+                        const bool lt2 = df < f2 || (df == f2 && (c2 < 0 || j < c2));
+                        const bool lt1 = df < f1 || (df == f1 && (c1 < 0 || j < c1));
+                        if (lt1) { f3 = f2; c3 = c2; f2 = f1; c2 = c1; f1 = df; c1 = j; }
+                        else if (lt2) { f3 = f2; c3 = c2; f2 = df; c2 = j; }
+                        else { f3 = df; c3 = j; }
+                    }
+                }
+                // contenders: candidates the float32 distances cannot separate from the best (second best)
+                const float lim = ERR ? f2 : f1;
+                const float climit = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
+                const int ncont = (c1 >= 0 && f1 <= climit) + (c2 >= 0 && f2 <= climit) + (c3 >= 0 && f3 <= climit);
+                const int need = ERR ? 2 : 1;
+                if (flagged || overflow || total == 0 || (ncont == 3)) {
+                    const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
+                    P.rows[slotq] = (int32_t)grow;
+                } else {
                     SampleResult r;
-                    if (certain) {
+                    if (ncont <= need) {
                         r.i1 = c1;
                         r.i2 = ERR ? c2 : -1;
-                        r.d1 = ERR ? ref_dist_pair(a.w + (int64_t)c1 * d, xs, d) : 0.0;
+                        r.d1 = (ERR && c1 >= 0) ? ref_dist_pair(a.w + (int64_t)c1 * d, xs, d) : 0.0;
                     } else {
-                        // float64 reference arithmetic over the candidates that float32 cannot separate
-                        const float lim = ERR ? f2 : f1;
-                        const float thr2 = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
-                        Top2 t;
-                        t.init();
-                        for (int q = 0; q < cnt; ++q) {
-                            const int32_t j = sCand[q * TM + row];
-                            const float* wr = a.w + (int64_t)j * d;
-                            if (!(cand_dist32(wr, xs, d) <= thr2)) continue;
-                            t.push(ref_sqdist(wr, xs, d), j);
-                        }
-                        r.i1 = t.i1;
-                        r.i2 = t.i2;
-                        r.d1 = t.d1;
+                        // two or three contenders within float32 rounding: the reference's float64 sums, pushed in
+                        // ascending unit order (lowest index wins exact ties)
+                        int32_t cj[3] = {c1, c2, c3};
+                        int nc = ncont;
+                        for (int x1 = 0; x1 < nc; ++x1)
+                            for (int x2 = x1 + 1; x2 < nc; ++x2)
+                                if (cj[x2] < cj[x1]) { const int32_t tmp = cj[x1]; cj[x1] = cj[x2]; cj[x2] = tmp; }
+                        Top2 tt;
+                        tt.init();
+                        for (int x1 = 0; x1 < nc; ++x1) tt.push(ref_sqdist(a.w + (int64_t)cj[x1] * d, xs, d), cj[x1]);
+                        if (ERR && nc < 3 && c3 >= 0) tt.push(ref_sqdist(a.w + (int64_t)c3 * d, xs, d), c3);
+                        r.i1 = tt.i1;
+                        r.i2 = ERR ? tt.i2 : -1;
+                        r.d1 = tt.d1;
                     }
                     emit_sample(a, grow, r, e0, e1, e2);
                 }
@@ -744,8 +819,8 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     P.off_a = s.off_a;
     P.off_x = s.off_x;
     P.off_cand = s.off_cand;
-    P.off_xn = s.off_xn;
-    P.off_flag = s.off_flag;
+    P.off_part = s.off_part;
+    P.off_res = s.off_res;
     P.off_center = s.off_center;
     P.off_bar = s.off_bar;
     P.a_stride = align_up(s.a_bytes, 1024);

@@ -13,42 +13,70 @@ namespace somgb {
 namespace {
 
 // ---------------------------------------------------------------------------------------------------------------------
-// Segmented sums. CTA (chunk, range) owns the bins of units [lo, lo+cnt) in shared memory (float64) and adds every
-// sample of its chunk whose BMU falls in its range; at the end it flushes the non-zero bins with one float64 atomic
-// each. Ranges exist only when M*(D+1) float64 bins exceed one CTA's shared memory.
+// Segmented sums. CTA (chunk, range) owns float32 bins for units [lo, lo+cnt) in shared memory and adds every sample of
+// its chunk whose BMU falls in its range (shared-memory float32 atomics). Every `window` samples it flushes the
+// non-zero bins into the float64 sums in global memory (one float64 atomic per bin) and clears them, so that a
+// float32 bin never holds more than `window` terms: the relative rounding of a flushed partial sum stays below
+// window * 2^-24 / (samples per bin), and the float64 totals are exact to 1e-15. Ranges exist only when M*(D+1) bins
+// exceed the shared-memory budget.
 // ---------------------------------------------------------------------------------------------------------------------
 
 template <typename T>
 __global__ void __launch_bounds__(256) accumulate_kernel(const T* __restrict__ x, const double* __restrict__ rho,
                                                          const int32_t* __restrict__ bmu, int64_t n, int d,
                                                          int64_t units_per_range, int64_t m, int64_t chunk,
-                                                         double* __restrict__ S, double* __restrict__ c) {
-    extern __shared__ double bins[];   // cnt x (d + 1)
+                                                         int64_t window, double* __restrict__ S,
+                                                         double* __restrict__ c) {
+    extern __shared__ float fbins[];   // cnt x (d + 1)
     const int64_t lo = (int64_t)blockIdx.y * units_per_range;
     const int64_t cnt = min64(units_per_range, m - lo);
     const int stride = d + 1;
-    for (int64_t q = threadIdx.x; q < cnt * stride; q += blockDim.x) bins[q] = 0.0;
+    const int64_t nb = cnt * stride;
+    for (int64_t q = threadIdx.x; q < nb; q += blockDim.x) fbins[q] = 0.0f;
     __syncthreads();
     const int64_t s0 = (int64_t)blockIdx.x * chunk;
     const int64_t s1 = min64(n, s0 + chunk);
-    for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-        const int32_t b = bmu[i];
-        if (b < lo || b >= lo + cnt) continue;   // also skips b == -1
-        double r = rho ? rho[i] : 1.0;
-        if (sizeof(T) == 4) r = (double)(float)r;  // the training density is cast to the map dtype (som_batch.py:312)
-        double* bin = bins + (b - lo) * stride;
-        const T* xr = x + i * d;
-        for (int k = 0; k < d; ++k) atomicAdd(bin + k, r * (double)xr[k]);
-        atomicAdd(bin + d, r);
+    for (int64_t w0 = s0; w0 < s1; w0 += window) {
+        const int64_t w1 = min64(s1, w0 + window);
+        for (int64_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
+            const int32_t b = bmu[i];
+            if (b < lo || b >= lo + cnt) continue;   // also skips b == -1
+            double r = rho ? rho[i] : 1.0;
+            if (sizeof(T) == 4) r = (double)(float)r;  // the training density is cast to the map dtype (som_batch.py:312)
+            float* bin = fbins + (b - lo) * stride;
+            const T* xr = x + i * d;
+            if (r == 1.0) {
+                for (int k = 0; k < d; ++k) atomicAdd(bin + k, (float)xr[k]);
+            } else {
+                for (int k = 0; k < d; ++k) atomicAdd(bin + k, (float)(r * (double)xr[k]));
+            }
+            atomicAdd(bin + d, (float)r);
+        }
+        __syncthreads();
+        for (int64_t q = threadIdx.x; q < nb; q += blockDim.x) {
+            const float v = fbins[q];
+            if (v == 0.0f) continue;
+            fbins[q] = 0.0f;
+            const int64_t u = lo + q / stride;
+            const int k = (int)(q % stride);
+            if (k < d) atomicAdd(S + u * d + k, (double)v);
+            else atomicAdd(c + u, (double)v);
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int64_t q = threadIdx.x; q < cnt * stride; q += blockDim.x) {
-        const double v = bins[q];
-        if (v == 0.0) continue;
-        const int64_t u = lo + q / stride;
-        const int k = (int)(q % stride);
-        if (k < d) atomicAdd(S + u * d + k, v);
-        else atomicAdd(c + u, v);
+}
+
+// Float64 maps keep float64 bins (their sums must stay float64-accurate).
+__global__ void __launch_bounds__(256) accumulate_f64_kernel(const double* __restrict__ x,
+                                                             const double* __restrict__ rho,
+                                                             const int32_t* __restrict__ bmu, int64_t n, int d,
+                                                             double* __restrict__ S, double* __restrict__ c) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = bmu[i];
+        if (b < 0) continue;
+        const double r = rho ? rho[i] : 1.0;
+        for (int k = 0; k < d; ++k) atomicAdd(S + (int64_t)b * d + k, r * x[i * d + k]);
+        atomicAdd(c + b, r);
     }
 }
 
@@ -228,37 +256,36 @@ __global__ void divide_kernel(const double* __restrict__ num, const double* __re
     w_out[q] = dn > FLOAT_EPS ? (T)(num[q] / dn) : (T)0;
 }
 
-size_t max_dyn_smem() {
-    static size_t cached = 0;
-    if (!cached) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cached = v > 0 ? (size_t)v : 48 * 1024;
-    }
-    return cached;
-}
-
 }  // namespace
 
 template <typename T>
 int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
                       double* c, cudaStream_t stream) {
     if (n == 0 || m == 0) return SOMGB_OK;
-    const size_t budget = std::min<size_t>(max_dyn_smem(), 200 * 1024);
-    const int64_t per_unit = (int64_t)(d + 1) * 8;
+    if (sizeof(T) == 8) {
+        accumulate_f64_kernel<<<(unsigned)(4 * num_sms()), 256, 0, stream>>>((const double*)x, rho, bmu, n, d, S, c);
+        SOMGB_LAUNCH_CHECK();
+        return SOMGB_OK;
+    }
+    // float32 bins: up to ~96 KB per CTA so that two CTAs share an SM
+    const size_t budget = 96 * 1024;
+    const int64_t per_unit = (int64_t)(d + 1) * 4;
     int64_t upr = std::max<int64_t>(1, (int64_t)(budget / per_unit));
     upr = std::min(upr, m);
     const int64_t ranges = ceil_div(m, upr);
     upr = ceil_div(m, ranges);
     const size_t smem = (size_t)(upr * per_unit);
-    const int64_t ctas_wanted = 2 * (int64_t)num_sms();
+    const int64_t ctas_wanted = 4 * (int64_t)num_sms();
     int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
     int64_t chunk = std::max<int64_t>(1024, ceil_div(n, chunks));
     chunks = ceil_div(n, chunk);
-    auto kern = accumulate_kernel<T>;
-    SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<dim3((unsigned)chunks, (unsigned)ranges), 256, smem, stream>>>(x, rho, bmu, n, d, upr, m, chunk, S, c);
+    // at most ~64 float32 terms per bin between flushes on average
+    const int64_t window = std::max<int64_t>(2048, std::min<int64_t>(64 * upr, 1 << 16));
+    auto kern = accumulate_kernel<float>;
+    if (smem > 48 * 1024)
+        SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<dim3((unsigned)chunks, (unsigned)ranges), 256, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m,
+                                                                         chunk, window, S, c);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
