@@ -214,6 +214,10 @@ class EpochRunner:
         self.S = torch.empty((self.M, self.D), dtype=torch.float64, device=device)
         self.c = torch.empty(self.M, dtype=torch.float64, device=device)
         self.bmu = torch.empty(self.N, dtype=torch.int32, device=device)
+        # per-feature bounds of the fixed-point sums: a property of the resident catalogue, computed once
+        self.bounds = torch.zeros(self.D + 1, dtype=torch.float32, device=device)
+        native.call('somgb_feature_bounds', xd.data_ptr(), None, self.N, self.D, self.bounds.data_ptr(),
+                    torch.cuda.current_stream().cuda_stream)
         nbytes = native.workspace_bytes(native.OP_FIND_BMUS, self.N, self.M, self.D, self.algo)
         self.ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
         self.wsp = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
@@ -238,7 +242,7 @@ class EpochRunner:
         if phases is not None:
             phases[1].record()
         nat.call('somgb_accumulate', self.xd.data_ptr(), None, self.bmu.data_ptr(), self.N, self.D, self.M,
-                 self.S.data_ptr(), self.c.data_ptr(), s)
+                 self.bounds.data_ptr(), self.S.data_ptr(), self.c.data_ptr(), s)
         if phases is not None:
             phases[2].record()
         e = self.epoch % self.w['schedule']

@@ -45,7 +45,8 @@ SIGNATURES = {
     'somgb_device_status': [P, I32, P],
     'somgb_set_kernel_timer': [P, P],
     'somgb_train_bmu_pass': [P, P, I64, I32, P, P, I64, D, I32, P, P, P, SZ, P],
-    'somgb_accumulate': [P, P, P, I64, I32, I64, P, P, P],
+    'somgb_accumulate': [P, P, P, I64, I32, I64, P, P, P, P],
+    'somgb_feature_bounds': [P, P, I64, I32, P, P],
     'somgb_accumulate_f64': [P, P, P, I64, I32, I64, P, P, P],
     'somgb_find_bmus': [P, I64, I32, P, I64, I32, P, P, SZ, P],
     'somgb_find_bmus_f64': [P, I64, I32, P, I64, P, P],

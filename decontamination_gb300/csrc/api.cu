@@ -10,8 +10,9 @@
 namespace somgb {
 
 template <typename T>
-int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
-                      double* c, cudaStream_t stream);
+int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
+                      const float* bounds, double* S, double* c, cudaStream_t stream);
+int launch_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, cudaStream_t stream);
 template <typename T>
 int launch_neighbourhood(const double* S, const double* c, const T* topo, int64_t m, int d, double sigma, T* w_out,
                          double* num, double* den, cudaStream_t stream);
@@ -70,13 +71,14 @@ constexpr size_t WS_HEADER = 256;
 struct Workspace {
     unsigned long long* counter = nullptr;
     int32_t* train_bmu = nullptr;
+    float* bounds = nullptr;
     void* tc = nullptr;
     size_t tc_bytes = 0;
 };
 
 size_t ws_bytes_for(int op, int64_t n, int64_t m, int d, int algo, bool* tc_used) {
     size_t b = WS_HEADER;
-    if (op == SOMGB_OP_EPOCH) b += align_up((size_t)std::max<int64_t>(n, 1) * sizeof(int32_t), 256);
+    if (op == SOMGB_OP_EPOCH) b += align_up((size_t)std::max<int64_t>(n, 1) * sizeof(int32_t), 256) + 512;
     bool tc = tc_supported(n, m, d, algo);
     if (tc_used) *tc_used = tc;
     if (tc) b += align_up(tc_workspace_bytes(n, m, d), 256);
@@ -96,6 +98,8 @@ int carve(void* ws, size_t ws_bytes, int op, int64_t n, int64_t m, int d, int al
     if (op == SOMGB_OP_EPOCH) {
         out->train_bmu = (int32_t*)p;
         p += align_up((size_t)std::max<int64_t>(n, 1) * sizeof(int32_t), 256);
+        out->bounds = (float*)p;
+        p += 512;
     }
     if (*tc) {
         out->tc = p;
@@ -238,8 +242,11 @@ int somgb_train_epoch_pass(const float* x, const double* rho, int64_t n, int d, 
     a.err3 = err3; a.train_bmu = bmu_out ? bmu_out : W.train_bmu;
     a.outs = OUT_TRAIN | (err3 ? OUT_ERR : 0);
     cudaStream_t st = (cudaStream_t)stream;
+    if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "the float32 training pass supports D <= 64");
     if (int s = run_pass(a, algo, W, tc, st)) return s;
-    return launch_accumulate<float>(x, rho, a.train_bmu, n, d, m, S, c, st);
+    SOMGB_CUDA_TRY(cudaMemsetAsync(W.bounds, 0, (size_t)(d + 1) * 4, st));
+    if (int s = launch_feature_bounds(x, rho, n, d, W.bounds, st)) return s;
+    return launch_accumulate<float>(x, rho, a.train_bmu, n, d, m, W.bounds, S, c, st);
 }
 
 int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
@@ -259,12 +266,19 @@ int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, co
     return run_pass(a, algo, W, tc, (cudaStream_t)stream);
 }
 
-int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
-                     double* c, somgb_stream_t stream) {
+int somgb_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, somgb_stream_t stream) {
+    if (n < 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if ((n > 0 && !x) || !bounds) return set_error(SOMGB_ERR_INVALID, "x/bounds is NULL");
+    return launch_feature_bounds(x, rho, n, d, bounds, (cudaStream_t)stream);
+}
+
+int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
+                     const float* bounds, double* S, double* c, somgb_stream_t stream) {
     if (n < 0 || m <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "somgb_accumulate supports D <= 64");
     if (n > 0 && (!x || !bmu)) return set_error(SOMGB_ERR_INVALID, "x/bmu is NULL");
-    if (!S || !c) return set_error(SOMGB_ERR_INVALID, "S/c is NULL");
-    return launch_accumulate<float>(x, rho, bmu, n, d, m, S, c, (cudaStream_t)stream);
+    if (!S || !c || !bounds) return set_error(SOMGB_ERR_INVALID, "S/c/bounds is NULL");
+    return launch_accumulate<float>(x, rho, bmu, n, d, m, bounds, S, c, (cudaStream_t)stream);
 }
 
 int somgb_accumulate_f64(const double* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
@@ -272,7 +286,7 @@ int somgb_accumulate_f64(const double* x, const double* rho, const int32_t* bmu,
     if (n < 0 || m <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
     if (n > 0 && (!x || !bmu)) return set_error(SOMGB_ERR_INVALID, "x/bmu is NULL");
     if (!S || !c) return set_error(SOMGB_ERR_INVALID, "S/c is NULL");
-    return launch_accumulate<double>(x, rho, bmu, n, d, m, S, c, (cudaStream_t)stream);
+    return launch_accumulate<double>(x, rho, bmu, n, d, m, nullptr, S, c, (cudaStream_t)stream);
 }
 
 int somgb_neighbourhood_update(const double* S, const double* c, const float* topo, int64_t m, int d, double sigma,
@@ -345,7 +359,7 @@ int somgb_train_epoch_pass_f64(const double* x, const double* rho, int64_t n, in
     if (int s = launch_exact_pass_f64(x, rho, n, d, w, m, topo, penalty, OUT_TRAIN | (err3 ? OUT_ERR : 0), nullptr,
                                       nullptr, err3, W.train_bmu, st))
         return s;
-    return launch_accumulate<double>(x, rho, W.train_bmu, n, d, m, S, c, st);
+    return launch_accumulate<double>(x, rho, W.train_bmu, n, d, m, nullptr, S, c, st);
 }
 
 int somgb_neighbourhood_update_f64(const double* S, const double* c, const double* topo, int64_t m, int d,

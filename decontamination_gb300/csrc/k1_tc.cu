@@ -228,6 +228,21 @@ __device__ __forceinline__ float cand_dist32(const float* __restrict__ wr, const
     return acc;
 }
 
+template <int DT>
+__device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, const float (&xr)[DT]) {
+    float acc = 0.0f;
+    const float4* w4 = (const float4*)wr;
+#pragma unroll
+    for (int k4 = 0; k4 < DT / 4; ++k4) {
+        const float4 w = __ldg(w4 + k4);
+        float t = w.x - xr[4 * k4]; acc = fmaf(t, t, acc);
+        t = w.y - xr[4 * k4 + 1]; acc = fmaf(t, t, acc);
+        t = w.z - xr[4 * k4 + 2]; acc = fmaf(t, t, acc);
+        t = w.w - xr[4 * k4 + 3]; acc = fmaf(t, t, acc);
+    }
+    return acc;
+}
+
 // Reference distance (float64 sum of float32 squares) evaluated exactly in float32 pairs; used for d1 of QE.
 __device__ __forceinline__ double ref_dist_pair(const float* __restrict__ wr, const float* __restrict__ xs, int d) {
     float hi = 0.0f, lo = 0.0f;
@@ -243,7 +258,7 @@ __device__ __forceinline__ double ref_dist_pair(const float* __restrict__ wr, co
     return (double)hi + (double)lo;
 }
 
-template <bool ERR>
+template <bool ERR, int DT>
 __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs P) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -268,8 +283,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
     const PassArgs& a = P.a;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int d = a.d;
-    const int kpad = P.kpad;
+    constexpr int d = DT;
+    constexpr int kpad = (3 * DT + 2 + 15) / 16 * 16;
     const int U = P.utiles;
     const int64_t num_tiles = (a.n + TM - 1) / TM;
     const int64_t n_my = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
@@ -383,40 +398,50 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
         auto qbar = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(1 + q) : "memory"); };
 
-        // centred split-BF16 A row: this thread writes the 16-byte chunks k0 = 8*(sl + 4c) of row `row`
-        auto convert = [&](int64_t it) -> bool {
+        // centred split-BF16 A row of `row`: this thread writes the 16-byte chunks kc = sl, sl + 4, ... of kpad / 8;
+        // returns |x'|^2 (infinite when a feature is not finite)
+        auto convert = [&](int64_t it, float& xn_out) -> bool {
             const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
             if (it >= 2 && !ptx::mbar_wait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
             if (!ptx::mbar_wait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
-            const float* xs = (const float*)(smem + P.off_x + s3 * P.x_stride) + row * d;
-            uint8_t* at = smem + P.off_a + s2 * P.a_stride;
+            const float4* xs4 = (const float4*)(smem + P.off_x + s3 * P.x_stride) + row * (DT / 4);
+            float xp[DT];
             bool finite = true;
             float xn = 0.0f;
-            for (int k = 0; k < d; ++k) {
-                const float t = xs[k] - sCenter[k];
-                finite = finite && isfinite(t);
-                xn = fmaf(t, t, xn);
+#pragma unroll
+            for (int k4 = 0; k4 < DT / 4; ++k4) {
+                const float4 v = xs4[k4];
+                xp[4 * k4 + 0] = v.x - sCenter[4 * k4 + 0];
+                xp[4 * k4 + 1] = v.y - sCenter[4 * k4 + 1];
+                xp[4 * k4 + 2] = v.z - sCenter[4 * k4 + 2];
+                xp[4 * k4 + 3] = v.w - sCenter[4 * k4 + 3];
+            }
+#pragma unroll
+            for (int k = 0; k < DT; ++k) {
+                finite = finite && isfinite(xp[k]);
+                xn = fmaf(xp[k], xp[k], xn);
             }
             finite = finite && (xn < HUGE_S);
-            for (int k0 = 8 * sl; k0 < kpad; k0 += 8 * SLICES) {
+            xn_out = finite ? xn : INFINITY;
+            uint8_t* at = smem + P.off_a + s2 * P.a_stride;
+#pragma unroll
+            for (int kc = 0; kc < kpad / 8; ++kc) {
+                if (kc % SLICES != sl) continue;
                 __align__(16) __nv_bfloat16 v[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const int k = k0 + i;
+                    const int k = kc * 8 + i;
                     float val = 0.0f;
-                    if (finite) {
-                        if (k < 3 * d) {
-                            const int kk = k % d;
-                            const float t = xs[kk] - sCenter[kk];
-                            const __nv_bfloat16 hi = __float2bfloat16_rn(t);
-                            val = (k >= d && k < 2 * d) ? t - __bfloat162float(hi) : __bfloat162float(hi);
-                        } else if (k == 3 * d || k == 3 * d + 1) {
-                            val = 1.0f;
-                        }
+                    if (k < 3 * DT) {
+                        const float t = xp[k % DT];
+                        const float hi = __bfloat162float(__float2bfloat16_rn(t));
+                        val = (k >= DT && k < 2 * DT) ? t - hi : hi;
+                    } else if (k == 3 * DT || k == 3 * DT + 1) {
+                        val = 1.0f;
                     }
-                    v[i] = __float2bfloat16_rn(val);
+                    v[i] = __float2bfloat16_rn(finite ? val : 0.0f);
                 }
-                *(uint4*)(at + canon_off(row, k0, kpad)) = *(const uint4*)v;
+                *(uint4*)(at + canon_off(row, kc * 8, kpad)) = *(const uint4*)v;
             }
             ptx::fence_proxy_async();
             __syncwarp();
@@ -438,22 +463,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             }
         };
 
-        bool ok = n_my > 0 ? convert(0) : true;
+        float xn_next = 0.0f;
+        bool ok = n_my > 0 ? convert(0, xn_next) : true;
         for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
-            if (it + 1 < n_my && !(ok = convert(it + 1))) break;
+            const float xn = xn_next;
+            if (it + 1 < n_my && !(ok = convert(it + 1, xn_next))) break;
             const int s3 = (int)(it % XSTAGES);
             const int64_t tile = blockIdx.x + it * gridDim.x;
             const int64_t grow = tile * TM + row;
             const bool live = grow < a.n;
             const float* xs = (const float*)(smem + P.off_x + s3 * P.x_stride) + row * d;
-            bool flagged = false;
-            float xn = 0.0f;
-            for (int k = 0; k < d; ++k) {
-                const float t = xs[k] - sCenter[k];
-                flagged = flagged || !isfinite(t);
-                xn = fmaf(t, t, xn);
-            }
-            flagged = flagged || !(xn < HUGE_S);
+            bool flagged = !(xn < HUGE_S);
 
             // ---- sweep 1: best (and second best) s~ of the row over this warp's columns -------------------------
             float a1 = INFINITY, a2 = INFINITY, b1 = INFINITY, b2 = INFINITY;
@@ -466,21 +486,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 ptx::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) ptx::mbar_arrive(t_empty + buf);
-                if (ERR) {
 #pragma unroll
-                    for (int i = 0; i < 32; i += 2) {
-                        const float lo = fminf(v0[i], v0[i + 1]), hi = fmaxf(v0[i], v0[i + 1]);
-                        a2 = fminf(fminf(a2, hi), fmaxf(a1, lo));
-                        a1 = fminf(a1, lo);
-                        const float lo2 = fminf(v1[i], v1[i + 1]), hi2 = fmaxf(v1[i], v1[i + 1]);
-                        b2 = fminf(fminf(b2, hi2), fmaxf(b1, lo2));
-                        b1 = fminf(b1, lo2);
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 32; i += 2) {
-                        a1 = fminf(a1, fminf(v0[i], v0[i + 1]));
-                        b1 = fminf(b1, fminf(v1[i], v1[i + 1]));
+                for (int g8 = 0; g8 < 32; g8 += 8) {
+                    const float ga = fminf(fminf(fminf(v0[g8], v0[g8 + 1]), fminf(v0[g8 + 2], v0[g8 + 3])),
+                                           fminf(fminf(v0[g8 + 4], v0[g8 + 5]), fminf(v0[g8 + 6], v0[g8 + 7])));
+                    const float gb = fminf(fminf(fminf(v1[g8], v1[g8 + 1]), fminf(v1[g8 + 2], v1[g8 + 3])),
+                                           fminf(fminf(v1[g8 + 4], v1[g8 + 5]), fminf(v1[g8 + 6], v1[g8 + 7])));
+                    if (ERR) {
+                        a2 = fminf(a2, fmaxf(a1, ga));
+                        a1 = fminf(a1, ga);
+                        b2 = fminf(b2, fmaxf(b1, gb));
+                        b1 = fminf(b1, gb);
+                    } else {
+                        a1 = fminf(a1, ga);
+                        b1 = fminf(b1, gb);
                     }
                 }
             }
@@ -498,6 +517,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 M2 = fminf(fminf(M2, p.y), fmaxf(M1, p.x));
                 M1 = fminf(M1, p.x);
             }
+            // ERR: M2 is the second smallest 8-unit group minimum, an upper bound of the second smallest s~ (two
+            // groups have a unit at or below it), so the threshold derived from it keeps every possible second BMU
             const float mref = ERR ? M2 : M1;
             if (!(M1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
             const float dref = fmaxf(0.0f, mref + xn);
@@ -520,14 +541,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 for (int half = 0; half < 2; ++half) {
                     const float* v = half ? v1 : v0;
 #pragma unroll
-                    for (int g8 = 0; g8 < 32; g8 += 8) {
-                        const float gm = fminf(fminf(fminf(v[g8], v[g8 + 1]), fminf(v[g8 + 2], v[g8 + 3])),
-                                               fminf(fminf(v[g8 + 4], v[g8 + 5]), fminf(v[g8 + 6], v[g8 + 7])));
+                    for (int g4 = 0; g4 < 32; g4 += 4) {
+                        const float gm = fminf(fminf(v[g4], v[g4 + 1]), fminf(v[g4 + 2], v[g4 + 3]));
                         if (gm <= thr) {
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) {
-                                const int j = jb + half * 32 + g8 + i;
-                                if (v[g8 + i] <= thr && j < (int)a.m) {
+                            for (int i = 0; i < 4; ++i) {
+                                const int j = jb + half * 32 + g4 + i;
+                                if (v[g4 + i] <= thr && j < (int)a.m) {
                                     if (cnt < CAPS) sCand[(sl * CAPS + cnt) * TM + row] = j;
                                     ++cnt;
                                 }
@@ -542,10 +562,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             {
                 float f[3] = {INFINITY, INFINITY, INFINITY};
                 int32_t c[3] = {-1, -1, -1};
-                if (live && !flagged && cnt <= CAPS) {
+                if (live && !flagged && cnt <= CAPS && cnt > 0) {
+                    float xr[DT];
+                    const float4* xs4 = (const float4*)xs;
+#pragma unroll
+                    for (int k4 = 0; k4 < DT / 4; ++k4) {
+                        const float4 t = xs4[k4];
+                        xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
+                    }
                     for (int k = 0; k < cnt; ++k) {
                         const int32_t j = sCand[(sl * CAPS + k) * TM + row];
-                        const float df = cand_dist32(a.w + (int64_t)j * d, xs, d);
+                        const float df = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
                         if (df < f[2]) {
                             if (df < f[1]) {
                                 f[2] = f[1]; c[2] = c[1];
@@ -715,6 +742,16 @@ __global__ void __launch_bounds__(256) tc_recheck_kernel(PassArgs a, const int32
     }
 }
 
+template <bool ERR, int DT>
+int launch_main(const CUtensorMap& tmap, const TcArgs& P, unsigned grid, size_t smem, cudaStream_t stream) {
+    SOMGB_CUDA_TRY(cudaFuncSetAttribute(tc_pass_kernel<ERR, DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    timer_begin(stream);
+    tc_pass_kernel<ERR, DT><<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
+    timer_end(stream);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
@@ -753,7 +790,7 @@ size_t max_smem_optin() {
 }  // namespace
 
 bool tc_shape_ok(int64_t m, int d) {
-    if (d <= 0 || d % 4 != 0 || d > 64) return false;
+    if (d != 4 && d != 8 && d != 16 && d != 32) return false;
     if (m <= 0 || m > (int64_t)1 << 24) return false;
     return tc_shape(m, d).smem <= 227 * 1024;
 }
@@ -831,20 +868,25 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());
     // at least half of an SM's shared memory, so that one CTA (the sole TMEM owner) runs per SM
     const size_t smem = std::max<size_t>(s.smem, 120 * 1024);
+    int st = SOMGB_OK;
     if (a.outs & OUT_ERR) {
-        SOMGB_CUDA_TRY(cudaFuncSetAttribute(tc_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-        timer_begin(stream);
-        tc_pass_kernel<true><<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
-        timer_end(stream);
+        switch (a.d) {
+            case 4: st = launch_main<true, 4>(tmap, P, grid, smem, stream); break;
+            case 8: st = launch_main<true, 8>(tmap, P, grid, smem, stream); break;
+            case 16: st = launch_main<true, 16>(tmap, P, grid, smem, stream); break;
+            case 32: st = launch_main<true, 32>(tmap, P, grid, smem, stream); break;
+            default: return set_error(SOMGB_ERR_UNSUPPORTED, "tensor-core pass: D=%d not in {4, 8, 16, 32}", a.d);
+        }
     } else {
-        SOMGB_CUDA_TRY(cudaFuncSetAttribute(tc_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-        timer_begin(stream);
-        tc_pass_kernel<false><<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
-        timer_end(stream);
+        switch (a.d) {
+            case 4: st = launch_main<false, 4>(tmap, P, grid, smem, stream); break;
+            case 8: st = launch_main<false, 8>(tmap, P, grid, smem, stream); break;
+            case 16: st = launch_main<false, 16>(tmap, P, grid, smem, stream); break;
+            case 32: st = launch_main<false, 32>(tmap, P, grid, smem, stream); break;
+            default: return set_error(SOMGB_ERR_UNSUPPORTED, "tensor-core pass: D=%d not in {4, 8, 16, 32}", a.d);
+        }
     }
-    SOMGB_LAUNCH_CHECK();
+    if (st) return st;
     tc_recheck_kernel<<<(unsigned)(2 * num_sms()), 256, 0, stream>>>(a, W.rows, a.recheck_count);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;

@@ -13,54 +13,111 @@ namespace somgb {
 namespace {
 
 // ---------------------------------------------------------------------------------------------------------------------
-// Segmented sums. CTA (chunk, range) owns float32 bins for units [lo, lo+cnt) in shared memory and adds every sample of
-// its chunk whose BMU falls in its range (shared-memory float32 atomics). Every `window` samples it flushes the
-// non-zero bins into the float64 sums in global memory (one float64 atomic per bin) and clears them, so that a
-// float32 bin never holds more than `window` terms: the relative rounding of a flushed partial sum stays below
-// window * 2^-24 / (samples per bin), and the float64 totals are exact to 1e-15. Ranges exist only when M*(D+1) bins
-// exceed the shared-memory budget.
+// Segmented sums in exact fixed point. Every term v = (float)rho * x_k is quantised as q = rint(v * 2^(47 - e_k)), with
+// 2^e_k above the largest |v| of feature k over the dataset (somgb_feature_bounds), so |q| < 2^47 and the quantisation
+// error is below 2^-48 of that bound. q is split into three 16-bit limbs accumulated with shared-memory int32 atomics
+// (native and fast on sm_100-class GPUs, unlike float atomics); a window of at most 2^15 samples keeps every limb sum
+// inside int32. At the end of each window the limbs of every bin recombine exactly in int64 and are added to the
+// float64 sums in global memory. The result is the exact sum to ~1e-14 relative, independent of summation order.
+// CTA (chunk, range) owns the bins of units [lo, lo+cnt); ranges exist only when M*(D+1) bins exceed shared memory.
 // ---------------------------------------------------------------------------------------------------------------------
+
+constexpr int FX_BITS = 47;
+constexpr int64_t FX_WINDOW = 1 << 15;
+
+__device__ __forceinline__ int fx_exponent(float bound) {
+    int e = 0;
+    if (bound > 0.0f) frexpf(bound, &e);   // bound < 2^e
+    return max(e, -60);
+}
+
+__device__ __forceinline__ void fx_add(int32_t* limbs, int64_t nb, int64_t bin, long long q) {
+    atomicAdd(limbs + bin, (int32_t)(q & 0xFFFF));
+    atomicAdd(limbs + nb + bin, (int32_t)((q >> 16) & 0xFFFF));
+    atomicAdd(limbs + 2 * nb + bin, (int32_t)(q >> 32));
+}
+
+__global__ void __launch_bounds__(256) feature_bounds_kernel(const float* __restrict__ x, const double* __restrict__ rho,
+                                                             int64_t n, int d, unsigned int* __restrict__ bounds) {
+    extern __shared__ unsigned int smax[];   // d + 1
+    for (int k = threadIdx.x; k <= d; k += blockDim.x) smax[k] = 0u;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float r = rho ? (float)rho[i] : 1.0f;
+        if (!(r > 0.0f)) continue;
+        const float* xr = x + i * d;
+        bool finite = true;
+        for (int k = 0; k < d; ++k) finite = finite && isfinite(xr[k]);
+        if (!finite) continue;   // such a sample never has a training BMU
+        for (int k = 0; k < d; ++k) {
+            const float v = fabsf(r * xr[k]);
+            // the float product may round down: one ulp up keeps the bound above the exact product
+            atomicMax(smax + k, __float_as_uint(v) + (v > 0.0f ? 1u : 0u));
+        }
+        atomicMax(smax + d, __float_as_uint(r));
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k <= d; k += blockDim.x)
+        if (smax[k]) atomicMax(bounds + k, smax[k]);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) accumulate_kernel(const T* __restrict__ x, const double* __restrict__ rho,
                                                          const int32_t* __restrict__ bmu, int64_t n, int d,
                                                          int64_t units_per_range, int64_t m, int64_t chunk,
-                                                         int64_t window, double* __restrict__ S,
+                                                         const float* __restrict__ bounds, double* __restrict__ S,
                                                          double* __restrict__ c) {
-    extern __shared__ float fbins[];   // cnt x (d + 1)
+    extern __shared__ int32_t limbs[];   // [3][cnt * (d + 1)]
+    __shared__ float scale_s[65];
+    __shared__ int exp_s[65];
     const int64_t lo = (int64_t)blockIdx.y * units_per_range;
     const int64_t cnt = min64(units_per_range, m - lo);
     const int stride = d + 1;
     const int64_t nb = cnt * stride;
-    for (int64_t q = threadIdx.x; q < nb; q += blockDim.x) fbins[q] = 0.0f;
+    for (int64_t q = threadIdx.x; q < 3 * nb; q += blockDim.x) limbs[q] = 0;
+    for (int k = threadIdx.x; k <= d && k < 65; k += blockDim.x) {
+        const int e = fx_exponent(bounds[k]);
+        exp_s[k] = e;
+        scale_s[k] = ldexpf(1.0f, FX_BITS - e);
+    }
     __syncthreads();
     const int64_t s0 = (int64_t)blockIdx.x * chunk;
     const int64_t s1 = min64(n, s0 + chunk);
-    for (int64_t w0 = s0; w0 < s1; w0 += window) {
-        const int64_t w1 = min64(s1, w0 + window);
+    for (int64_t w0 = s0; w0 < s1; w0 += FX_WINDOW) {
+        const int64_t w1 = min64(s1, w0 + FX_WINDOW);
         for (int64_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
             const int32_t b = bmu[i];
             if (b < lo || b >= lo + cnt) continue;   // also skips b == -1
-            double r = rho ? rho[i] : 1.0;
-            if (sizeof(T) == 4) r = (double)(float)r;  // the training density is cast to the map dtype (som_batch.py:312)
-            float* bin = fbins + (b - lo) * stride;
-            const T* xr = x + i * d;
-            if (r == 1.0) {
-                for (int k = 0; k < d; ++k) atomicAdd(bin + k, (float)xr[k]);
+            const float r = rho ? (float)rho[i] : 1.0f;  // the training density is cast to float32 (som_batch.py:312)
+            const int64_t bin = (b - lo) * stride;
+            const float* xr = (const float*)x + i * d;
+            if (r == 1.0f) {
+                for (int k = 0; k < d; ++k) fx_add(limbs, nb, bin + k, __float2ll_rn(xr[k] * scale_s[k]));
+                fx_add(limbs, nb, bin + d, __float2ll_rn(scale_s[d]));
             } else {
-                for (int k = 0; k < d; ++k) atomicAdd(bin + k, (float)(r * (double)xr[k]));
+                for (int k = 0; k < d; ++k) {
+                    // r * x exactly as hi + lo, each quantised
+                    const float hi = r * xr[k];
+                    const float lo_ = fmaf(r, xr[k], -hi);
+                    fx_add(limbs, nb, bin + k,
+                           __float2ll_rn(hi * scale_s[k]) + __float2ll_rn(lo_ * scale_s[k]));
+                }
+                fx_add(limbs, nb, bin + d, __float2ll_rn(r * scale_s[d]));
             }
-            atomicAdd(bin + d, (float)r);
         }
         __syncthreads();
         for (int64_t q = threadIdx.x; q < nb; q += blockDim.x) {
-            const float v = fbins[q];
-            if (v == 0.0f) continue;
-            fbins[q] = 0.0f;
+            const long long v = (long long)limbs[q] + ((long long)limbs[nb + q] << 16) +
+                                ((long long)limbs[2 * nb + q] << 32);
+            limbs[q] = 0;
+            limbs[nb + q] = 0;
+            limbs[2 * nb + q] = 0;
+            if (v == 0) continue;
             const int64_t u = lo + q / stride;
             const int k = (int)(q % stride);
-            if (k < d) atomicAdd(S + u * d + k, (double)v);
-            else atomicAdd(c + u, (double)v);
+            const double val = ldexp((double)v, exp_s[k] - FX_BITS);
+            if (k < d) atomicAdd(S + u * d + k, val);
+            else atomicAdd(c + u, val);
         }
         __syncthreads();
     }
@@ -258,34 +315,42 @@ __global__ void divide_kernel(const double* __restrict__ num, const double* __re
 
 }  // namespace
 
+int launch_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, cudaStream_t stream) {
+    if (n == 0) return SOMGB_OK;
+    const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), 4 * (int64_t)num_sms());
+    feature_bounds_kernel<<<(unsigned)blocks, 256, (size_t)(d + 1) * 4, stream>>>(x, rho, n, d, (unsigned int*)bounds);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
 template <typename T>
-int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
-                      double* c, cudaStream_t stream) {
+int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
+                      const float* bounds, double* S, double* c, cudaStream_t stream) {
     if (n == 0 || m == 0) return SOMGB_OK;
     if (sizeof(T) == 8) {
         accumulate_f64_kernel<<<(unsigned)(4 * num_sms()), 256, 0, stream>>>((const double*)x, rho, bmu, n, d, S, c);
         SOMGB_LAUNCH_CHECK();
         return SOMGB_OK;
     }
-    // float32 bins: up to ~96 KB per CTA so that two CTAs share an SM
-    const size_t budget = 96 * 1024;
-    const int64_t per_unit = (int64_t)(d + 1) * 4;
+    if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "fixed-point segmented sums support D <= 64");
+    // three int32 limbs per bin; up to ~200 KB of bins per CTA
+    const size_t budget = 200 * 1024;
+    const int64_t per_unit = (int64_t)(d + 1) * 12;
     int64_t upr = std::max<int64_t>(1, (int64_t)(budget / per_unit));
     upr = std::min(upr, m);
     const int64_t ranges = ceil_div(m, upr);
     upr = ceil_div(m, ranges);
     const size_t smem = (size_t)(upr * per_unit);
-    const int64_t ctas_wanted = 4 * (int64_t)num_sms();
+    const int64_t ctas_per_sm = smem <= 100 * 1024 ? 2 : 1;
+    const int64_t ctas_wanted = ctas_per_sm * (int64_t)num_sms();
     int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
-    int64_t chunk = std::max<int64_t>(1024, ceil_div(n, chunks));
+    int64_t chunk = std::max<int64_t>(4096, ceil_div(n, chunks));
     chunks = ceil_div(n, chunk);
-    // at most ~64 float32 terms per bin between flushes on average
-    const int64_t window = std::max<int64_t>(2048, std::min<int64_t>(64 * upr, 1 << 16));
     auto kern = accumulate_kernel<float>;
     if (smem > 48 * 1024)
         SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<dim3((unsigned)chunks, (unsigned)ranges), 256, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m,
-                                                                         chunk, window, S, c);
+                                                                         chunk, bounds, S, c);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
@@ -337,10 +402,10 @@ int launch_divide(const double* num, const double* den, int64_t m, int d, T* w_o
     return SOMGB_OK;
 }
 
-template int launch_accumulate<float>(const float*, const double*, const int32_t*, int64_t, int, int64_t, double*,
-                                      double*, cudaStream_t);
-template int launch_accumulate<double>(const double*, const double*, const int32_t*, int64_t, int, int64_t, double*,
-                                       double*, cudaStream_t);
+template int launch_accumulate<float>(const float*, const double*, const int32_t*, int64_t, int, int64_t,
+                                      const float*, double*, double*, cudaStream_t);
+template int launch_accumulate<double>(const double*, const double*, const int32_t*, int64_t, int, int64_t,
+                                       const float*, double*, double*, cudaStream_t);
 template int launch_neighbourhood<float>(const double*, const double*, const float*, int64_t, int, double, float*,
                                          double*, double*, cudaStream_t);
 template int launch_neighbourhood<double>(const double*, const double*, const double*, int64_t, int, double, double*,

@@ -75,14 +75,31 @@ class SOM_Batch(SOM_Abstract):
         s = float(self._dtype(self._sigma)) * asymptotic_decay(epoch, total)
         return FLOAT_EPS if s < FLOAT_EPS else s
 
-    def _chunk_source(self, dataset, dataset_weights, device):
-        """Chunks for the epoch loop: arrays are uploaded once and reused by every epoch."""
-        if (dataset is None or is_array(dataset)) and (dataset_weights is None or is_array(dataset_weights)):
-            chunks = list(iterate_chunks(dataset, dataset_weights, self._dtype, device))
-            return lambda: iter(chunks)
-        return lambda: iterate_chunks(dataset, dataset_weights, self._dtype, device)
+    def _with_bounds(self, xc, rc, device):
+        """A chunk plus the per-feature bounds of its fixed-point sums (float32 maps), valid for every epoch."""
+        if self._is_f64:
+            return xc, rc, None
+        bounds = torch.zeros(self._dim + 1, dtype=torch.float32, device=device)
+        _native.call('somgb_feature_bounds', xc.data_ptr(), _device.ptr(rc), _device.rows(xc), self._dim,
+                     bounds.data_ptr(), _device.stream())
+        return xc, rc, bounds
 
-    def _epoch_pass(self, xc, rc, w, topo, S, c, err, device):
+    def _chunk_source(self, dataset, dataset_weights, device):
+        """Chunks for the epoch loop: arrays are uploaded once (with their bounds) and reused by every epoch."""
+        if (dataset is None or is_array(dataset)) and (dataset_weights is None or is_array(dataset_weights)):
+            chunks = [self._with_bounds(xc, rc, device)
+                      for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device)]
+            return lambda: iter(chunks)
+        return lambda: (self._with_bounds(xc, rc, device)
+                        for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device))
+
+    def _bmu_buffer(self, n, device):
+        buf = getattr(self, '_bmu_buf', None)
+        if buf is None or buf.numel() < n or buf.device != device:
+            buf = self._bmu_buf = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+        return buf
+
+    def _epoch_pass(self, xc, rc, bounds, w, topo, S, c, err, device):
         n = _device.rows(xc)
         M, D = self._m * self._n, self._dim
         if self._is_f64:
@@ -91,10 +108,13 @@ class SOM_Batch(SOM_Abstract):
                          topo.data_ptr(), M, self._penalty, S.data_ptr(), c.data_ptr(), _device.ptr(err), wsp, wsb,
                          _device.stream())
         else:
-            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, n, M, D, self._algo, device)
-            _native.call('somgb_train_epoch_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
-                         topo.data_ptr(), M, self._penalty, self._algo, S.data_ptr(), c.data_ptr(), _device.ptr(err),
-                         None, wsp, wsb, _device.stream())
+            bmu = self._bmu_buffer(n, device)
+            wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, n, M, D, self._algo, device)
+            _native.call('somgb_train_bmu_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
+                         topo.data_ptr(), M, self._penalty, self._algo, bmu.data_ptr(), _device.ptr(err), wsp, wsb,
+                         _device.stream())
+            _native.call('somgb_accumulate', xc.data_ptr(), _device.ptr(rc), bmu.data_ptr(), n, D, M,
+                         bounds.data_ptr(), S.data_ptr(), c.data_ptr(), _device.stream())
 
     def _update(self, S, c, topo, sigma, w_out):
         M, D = self._m * self._n, self._dim
@@ -152,7 +172,7 @@ class SOM_Batch(SOM_Abstract):
             c.zero_()
             err = errs[e] if with_errors else None
             last = e == n_epochs
-            for xc, rc in chunks():
+            for xc, rc, bounds in chunks():
                 if last:
                     if with_errors:
                         n = _device.rows(xc)
@@ -165,7 +185,7 @@ class SOM_Batch(SOM_Abstract):
                             _native.call(name, xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(),
                                          M, self._penalty, self._algo, err.data_ptr(), wsp, wsb, _device.stream())
                 else:
-                    self._epoch_pass(xc, rc, w, topo, S, c, err if e > 0 else None, device)
+                    self._epoch_pass(xc, rc, bounds, w, topo, S, c, err if e > 0 else None, device)
             if check_stop and e > 0 and with_errors:
                 qe, te = self._errors_of(errs[e].cpu().numpy())
                 if qe <= sq and te <= st:

@@ -133,13 +133,18 @@ int somgb_train_epoch_pass_f64(const double* x, const double* rho, int64_t n, in
  * The two halves of somgb_train_epoch_pass as separate calls.
  * somgb_train_bmu_pass: bmu_out[i] = training BMU of sample i (-1 when (float)rho_i <= 0 or no unit is valid),
  *   plus the error sums of `w` into err3 when err3 != NULL. Workspace: SOMGB_OP_FIND_BMUS sizing.
- * somgb_accumulate: S[b_i] += (double)(float)rho_i * x_i, c[b_i] += (double)(float)rho_i for b_i >= 0 ("+=").
+ * somgb_feature_bounds: bounds[k] = max(bounds[k], max_i |(float)rho_i * x_ik|) (k < d) and bounds[d] =
+ *   max(bounds[d], max_i (float)rho_i) over the samples with finite features and rho_i > 0, as float32 bit patterns
+ *   compared as unsigned integers ("max="; zero the d+1 floats first). A dataset's bounds stay valid for every epoch.
+ * somgb_accumulate: S[b_i] += (double)(float)rho_i * x_i, c[b_i] += (double)(float)rho_i for b_i >= 0 ("+="), summed
+ *   in exact 47-bit fixed point scaled by `bounds`; D <= 64.
  */
 int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
                          int64_t m, double penalty, int algo, int32_t* bmu_out, double* err3, void* ws,
                          size_t ws_bytes, somgb_stream_t stream);
-int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m, double* S,
-                     double* c, somgb_stream_t stream);
+int somgb_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, somgb_stream_t stream);
+int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
+                     const float* bounds, double* S, double* c, somgb_stream_t stream);
 int somgb_accumulate_f64(const double* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
                          double* S, double* c, somgb_stream_t stream);
 

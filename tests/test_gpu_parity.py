@@ -259,7 +259,7 @@ def test_c_abi_epoch_pass_accumulators(cuda, native, oracle):
     assert np.array_equal(bmu.cpu().numpy(), b)
     S_ref = np.zeros((M, D)); np.add.at(S_ref, b, x.astype(np.float64))
     c_ref = np.bincount(b, minlength=M).astype(np.float64)
-    np.testing.assert_allclose(S.cpu().numpy(), S_ref, rtol=1e-12)
+    np.testing.assert_allclose(S.cpu().numpy(), S_ref, rtol=1e-12)   # fixed-point sums are exact to ~1e-14
     assert np.array_equal(c.cpu().numpy(), c_ref)
     o = oracle.compute_errors_raw(w, topo, x, None, 2.0, 'numba')
     np.testing.assert_allclose(err.cpu().numpy(), o, rtol=ERR_RTOL)
