@@ -87,6 +87,21 @@ struct Top2 {
     }
 };
 
+// The same ranking for entries arriving in any order: (distance, index) compared lexicographically.
+struct Top2Lex {
+    double d1, d2;
+    int32_t i1, i2;
+    __device__ __forceinline__ void init() { d1 = 1.0e99; d2 = 1.0e99; i1 = -1; i2 = -1; }
+    __device__ __forceinline__ static bool before(double da, int32_t ja, double db, int32_t jb) {
+        return jb < 0 || da < db || (da == db && ja < jb);
+    }
+    __device__ __forceinline__ void push(double d, int32_t j) {
+        if (d != d || !(d < 1.0e99)) return;
+        if (before(d, j, d1, i1)) { d2 = d1; i2 = i1; d1 = d; i1 = j; }
+        else if (before(d, j, d2, i2)) { d2 = d; i2 = j; }
+    }
+};
+
 // Block-wide sum of three doubles into out[0..2] with one atomic per block and value.
 __device__ __forceinline__ void block_add3(double a, double b, double c, double* out) {
     __shared__ double red[3][32];

@@ -84,7 +84,7 @@ TcShape tc_shape(int64_t m, int d) {
     s.off_part = off;
     off += (size_t)SLICES * TM * 8;
     s.off_res = off;
-    off += (size_t)SLICES * 7 * TM * 4;
+    off += (size_t)SLICES * (CAPS + 1) * TM * 4;
     s.off_center = off;
     off += align_up((size_t)d * 4, 16);
     s.off_bar = align_up(off, 8);
@@ -266,9 +266,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     float* sCenter = (float*)(smem + P.off_center);
     int32_t* sCand = (int32_t*)(smem + P.off_cand);   // [slice][CAPS][TM]
     float2* sPart = (float2*)(smem + P.off_part);     // [slice][TM]: (m1, m2) of the slice
-    float* sResD = (float*)(smem + P.off_res);        // [slice][3][TM]: best float32 distances of the slice
-    int32_t* sResJ = (int32_t*)(smem + P.off_res + (size_t)SLICES * 3 * TM * 4);
-    int32_t* sResN = (int32_t*)(smem + P.off_res + (size_t)SLICES * 6 * TM * 4);   // [slice][TM] candidate count
+    float* sCandD = (float*)(smem + P.off_res);       // [slice][CAPS][TM]: float32 distance of each candidate
+    int32_t* sCandN = (int32_t*)(smem + P.off_res + (size_t)SLICES * CAPS * TM * 4);   // [slice][TM]: count
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
     uint64_t* x_full = bars + 1;    // [3]
@@ -558,87 +557,69 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             }
             if (!ok) break;
 
-            // ---- resolution: float32 distances of this slice's candidates, merged by slice 0 ---------------------
-            {
-                float f[3] = {INFINITY, INFINITY, INFINITY};
-                int32_t c[3] = {-1, -1, -1};
-                if (live && !flagged && cnt <= CAPS && cnt > 0) {
-                    float xr[DT];
-                    const float4* xs4 = (const float4*)xs;
+            // ---- resolution: float32 distances of this slice's candidates; slice 0 decides the row -------------------
+            if (live && !flagged && cnt <= CAPS && cnt > 0) {
+                float xr[DT];
+                const float4* xs4 = (const float4*)xs;
 #pragma unroll
-                    for (int k4 = 0; k4 < DT / 4; ++k4) {
-                        const float4 t = xs4[k4];
-                        xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
-                    }
-                    for (int k = 0; k < cnt; ++k) {
-                        const int32_t j = sCand[(sl * CAPS + k) * TM + row];
-                        const float df = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
-                        if (df < f[2]) {
-                            if (df < f[1]) {
-                                f[2] = f[1]; c[2] = c[1];
-                                if (df < f[0]) { f[1] = f[0]; c[1] = c[0]; f[0] = df; c[0] = j; }
-                                else { f[1] = df; c[1] = j; }
-                            } else { f[2] = df; c[2] = j; }
-                        }
-                    }
+                for (int k4 = 0; k4 < DT / 4; ++k4) {
+                    const float4 t = xs4[k4];
+                    xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
                 }
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    sResD[(sl * 3 + k) * TM + row] = f[k];
-                    sResJ[(sl * 3 + k) * TM + row] = c[k];
+                for (int k = 0; k < cnt; ++k) {
+                    const int32_t j = sCand[(sl * CAPS + k) * TM + row];
+                    sCandD[(sl * CAPS + k) * TM + row] = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
                 }
-                sResN[sl * TM + row] = cnt;
             }
+            sCandN[sl * TM + row] = cnt;
             qbar();
             if (sl == 0 && live) {
-                // merge the slices' best three in (float32 distance, unit) order
-                float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
-                int32_t c1 = -1, c2 = -1, c3 = -1;
+                // best two candidates in (float32 distance, unit) order
+                float f1 = INFINITY, f2 = INFINITY;
+                int32_t c1 = -1, c2 = -1;
                 int total = 0;
                 bool overflow = false;
                 for (int t = 0; t < SLICES; ++t) {
-                    const int n_t = sResN[t * TM + row];
+                    const int n_t = sCandN[t * TM + row];
                     total += n_t;
                     overflow = overflow || n_t > CAPS;
-                    for (int k = 0; k < 3; ++k) {
-                        const float df = sResD[(t * 3 + k) * TM + row];
-                        const int32_t j = sResJ[(t * 3 + k) * TM + row];
-                        if (j < 0) continue;
-                        const bool lt3 = df < f3 || (df == f3 && (c3 < 0 || j < c3));
-                        if (!lt3) continue;
-                        const bool lt2 = df < f2 || (df == f2 && (c2 < 0 || j < c2));
-                        const bool lt1 = df < f1 || (df == f1 && (c1 < 0 || j < c1));
-                        if (lt1) { f3 = f2; c3 = c2; f2 = f1; c2 = c1; f1 = df; c1 = j; }
-                        else if (lt2) { f3 = f2; c3 = c2; f2 = df; c2 = j; }
-                        else { f3 = df; c3 = j; }
+                    if (n_t > CAPS) continue;
+                    for (int k = 0; k < n_t; ++k) {
+                        const float df = sCandD[(t * CAPS + k) * TM + row];
+                        const int32_t j = sCand[(t * CAPS + k) * TM + row];
+                        if (df < f1 || (df == f1 && j < c1)) { f2 = f1; c2 = c1; f1 = df; c1 = j; }
+                        else if (df < f2 || (df == f2 && j < c2)) { f2 = df; c2 = j; }
                     }
                 }
-                // contenders: candidates the float32 distances cannot separate from the best (second best)
-                const float lim = ERR ? f2 : f1;
-                const float climit = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
-                const int ncont = (c1 >= 0 && f1 <= climit) + (c2 >= 0 && f2 <= climit) + (c3 >= 0 && f3 <= climit);
-                const int need = ERR ? 2 : 1;
-                if (flagged || overflow || total == 0 || (ncont == 3)) {
+                if (flagged || overflow || total == 0) {
                     const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                     P.rows[slotq] = (int32_t)grow;
                 } else {
+                    // contenders: candidates the float32 distances cannot separate from the best (second best)
+                    const float lim = ERR ? f2 : f1;
+                    const float climit = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
+                    int ncont = 0;
+                    for (int t = 0; t < SLICES; ++t) {
+                        const int n_t = sCandN[t * TM + row];
+                        for (int k = 0; k < n_t; ++k) ncont += sCandD[(t * CAPS + k) * TM + row] <= climit;
+                    }
                     SampleResult r;
-                    if (ncont <= need) {
+                    if (ncont <= (ERR ? 2 : 1)) {
                         r.i1 = c1;
                         r.i2 = ERR ? c2 : -1;
                         r.d1 = (ERR && c1 >= 0) ? ref_dist_pair(a.w + (int64_t)c1 * d, xs, d) : 0.0;
                     } else {
-                        // two or three contenders within float32 rounding: the reference's float64 sums, pushed in
-                        // ascending unit order (lowest index wins exact ties)
-                        int32_t cj[3] = {c1, c2, c3};
-                        int nc = ncont;
-                        for (int x1 = 0; x1 < nc; ++x1)
-                            for (int x2 = x1 + 1; x2 < nc; ++x2)
-                                if (cj[x2] < cj[x1]) { const int32_t tmp = cj[x1]; cj[x1] = cj[x2]; cj[x2] = tmp; }
-                        Top2 tt;
+                        // float64 reference sums of every contender, ranked in (distance, unit) order
+                        Top2Lex tt;
                         tt.init();
-                        for (int x1 = 0; x1 < nc; ++x1) tt.push(ref_sqdist(a.w + (int64_t)cj[x1] * d, xs, d), cj[x1]);
-                        if (ERR && nc < 3 && c3 >= 0) tt.push(ref_sqdist(a.w + (int64_t)c3 * d, xs, d), c3);
+                        for (int t = 0; t < SLICES; ++t) {
+                            const int n_t = sCandN[t * TM + row];
+                            for (int k = 0; k < n_t; ++k) {
+                                if (!(sCandD[(t * CAPS + k) * TM + row] <= climit)) continue;
+                                const int32_t j = sCand[(t * CAPS + k) * TM + row];
+                                tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
+                            }
+                        }
                         r.i1 = tt.i1;
                         r.i2 = ERR ? tt.i2 : -1;
                         r.d1 = tt.d1;

@@ -61,21 +61,23 @@ __global__ void __launch_bounds__(256) feature_bounds_kernel(const float* __rest
         if (smax[k]) atomicMax(bounds + k, smax[k]);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) accumulate_kernel(const T* __restrict__ x, const double* __restrict__ rho,
-                                                         const int32_t* __restrict__ bmu, int64_t n, int d,
-                                                         int64_t units_per_range, int64_t m, int64_t chunk,
-                                                         const float* __restrict__ bounds, double* __restrict__ S,
-                                                         double* __restrict__ c) {
+// DT > 0: the feature count known at compile time (rows loaded as float4); DT == 0: any d.
+template <int DT>
+__global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restrict__ x, const double* __restrict__ rho,
+                                                          const int32_t* __restrict__ bmu, int64_t n, int d_rt,
+                                                          int64_t units_per_range, int64_t m, int64_t chunk,
+                                                          const float* __restrict__ bounds, double* __restrict__ S,
+                                                          double* __restrict__ c) {
     extern __shared__ int32_t limbs[];   // [3][cnt * (d + 1)]
     __shared__ float scale_s[65];
     __shared__ int exp_s[65];
+    const int d = DT > 0 ? DT : d_rt;
     const int64_t lo = (int64_t)blockIdx.y * units_per_range;
     const int64_t cnt = min64(units_per_range, m - lo);
     const int stride = d + 1;
     const int64_t nb = cnt * stride;
     for (int64_t q = threadIdx.x; q < 3 * nb; q += blockDim.x) limbs[q] = 0;
-    for (int k = threadIdx.x; k <= d && k < 65; k += blockDim.x) {
+    for (int k = threadIdx.x; k <= d; k += blockDim.x) {
         const int e = fx_exponent(bounds[k]);
         exp_s[k] = e;
         scale_s[k] = ldexpf(1.0f, FX_BITS - e);
@@ -86,24 +88,39 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const T* __restrict__ x
     for (int64_t w0 = s0; w0 < s1; w0 += FX_WINDOW) {
         const int64_t w1 = min64(s1, w0 + FX_WINDOW);
         for (int64_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
-            const int32_t b = bmu[i];
+            const int32_t b = __ldg(bmu + i);
             if (b < lo || b >= lo + cnt) continue;   // also skips b == -1
-            const float r = rho ? (float)rho[i] : 1.0f;  // the training density is cast to float32 (som_batch.py:312)
+            const float r = rho ? (float)__ldg(rho + i) : 1.0f;  // float32 training density (som_batch.py:312)
             const int64_t bin = (b - lo) * stride;
-            const float* xr = (const float*)x + i * d;
-            if (r == 1.0f) {
-                for (int k = 0; k < d; ++k) fx_add(limbs, nb, bin + k, __float2ll_rn(xr[k] * scale_s[k]));
-                fx_add(limbs, nb, bin + d, __float2ll_rn(scale_s[d]));
+            const float* xr = x + i * d;
+            if constexpr (DT > 0) {
+                float xv[DT];
+                const float4* x4 = (const float4*)xr;
+#pragma unroll
+                for (int k4 = 0; k4 < DT / 4; ++k4) {
+                    const float4 t = __ldg(x4 + k4);
+                    xv[4 * k4] = t.x; xv[4 * k4 + 1] = t.y; xv[4 * k4 + 2] = t.z; xv[4 * k4 + 3] = t.w;
+                }
+                if (r == 1.0f) {
+#pragma unroll
+                    for (int k = 0; k < DT; ++k) fx_add(limbs, nb, bin + k, __float2ll_rn(xv[k] * scale_s[k]));
+                } else {
+#pragma unroll
+                    for (int k = 0; k < DT; ++k) {
+                        const float hi = r * xv[k];
+                        const float lo_ = fmaf(r, xv[k], -hi);   // r * x exactly as hi + lo
+                        fx_add(limbs, nb, bin + k, __float2ll_rn(hi * scale_s[k]) + __float2ll_rn(lo_ * scale_s[k]));
+                    }
+                }
             } else {
                 for (int k = 0; k < d; ++k) {
-                    // r * x exactly as hi + lo, each quantised
-                    const float hi = r * xr[k];
-                    const float lo_ = fmaf(r, xr[k], -hi);
-                    fx_add(limbs, nb, bin + k,
-                           __float2ll_rn(hi * scale_s[k]) + __float2ll_rn(lo_ * scale_s[k]));
+                    const float xv = __ldg(xr + k);
+                    const float hi = r * xv;
+                    const float lo_ = fmaf(r, xv, -hi);
+                    fx_add(limbs, nb, bin + k, __float2ll_rn(hi * scale_s[k]) + __float2ll_rn(lo_ * scale_s[k]));
                 }
-                fx_add(limbs, nb, bin + d, __float2ll_rn(r * scale_s[d]));
             }
+            fx_add(limbs, nb, bin + d, __float2ll_rn(r * scale_s[d]));
         }
         __syncthreads();
         for (int64_t q = threadIdx.x; q < nb; q += blockDim.x) {
@@ -346,11 +363,17 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
     int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
     int64_t chunk = std::max<int64_t>(4096, ceil_div(n, chunks));
     chunks = ceil_div(n, chunk);
-    auto kern = accumulate_kernel<float>;
+    auto kern = accumulate_kernel<0>;
+    if (((uintptr_t)x) % 16 == 0) {
+        if (d == 4) kern = accumulate_kernel<4>;
+        else if (d == 8) kern = accumulate_kernel<8>;
+        else if (d == 16) kern = accumulate_kernel<16>;
+        else if (d == 32) kern = accumulate_kernel<32>;
+    }
     if (smem > 48 * 1024)
         SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<dim3((unsigned)chunks, (unsigned)ranges), 256, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m,
-                                                                         chunk, bounds, S, c);
+    kern<<<dim3((unsigned)chunks, (unsigned)ranges), 1024, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m,
+                                                                          chunk, bounds, S, c);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
