@@ -54,12 +54,28 @@ __device__ SampleResult exact_top2(const PassArgs& a, const float* __restrict__ 
 }
 
 template <int DMAX, bool TOP3>
-__global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a) {
+__device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live);
+
+// rows == NULL: thread t of block b handles sample b*128 + t. Otherwise the blocks stride over the first *count
+// entries of `rows` (a list of sample indices), 128 per block and iteration.
+template <int DMAX, bool TOP3>
+__global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a, const int32_t* __restrict__ rows,
+                                                             const unsigned long long* __restrict__ count) {
+    const int64_t total = rows ? (int64_t)*count : a.n;
+    const int64_t step = rows ? (int64_t)gridDim.x * K0_THREADS : total + 1;
+    for (int64_t base = (int64_t)blockIdx.x * K0_THREADS; base < total; base += step) {
+        const int64_t e = base + threadIdx.x;
+        const bool live = e < total;
+        const int64_t i = !live ? 0 : (rows ? (int64_t)rows[e] : e);
+        k0_block<DMAX, TOP3>(a, i, live);
+    }
+}
+
+template <int DMAX, bool TOP3>
+__device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live) {
     constexpr int DS = DMAX > 0 ? DMAX : 4;
     __shared__ __align__(16) float wsh[K0_TILE * DS];
     const int d = a.d;
-    const int64_t i = (int64_t)blockIdx.x * K0_THREADS + threadIdx.x;
-    const bool live = i < a.n;
     const float* xg = a.x + (live ? i : 0) * d;
 
     float xr[DMAX > 0 ? DMAX : 1];
@@ -129,17 +145,18 @@ __global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a) {
         emit_sample(a, i, r, e0, e1, e2);
     }
     if (a.outs & OUT_ERR) block_add3(e0, e1, e2, a.err3);
+    __syncthreads();   // the shared tile and reduction buffers are reused by the next row block
 }
 
 template <int DMAX>
-int launch_dmax(const PassArgs& a, cudaStream_t stream) {
-    dim3 grid((unsigned)ceil_div(a.n, K0_THREADS));
-    timer_begin(stream);
+int launch_dmax(const PassArgs& a, const int32_t* rows, const unsigned long long* count, cudaStream_t stream) {
+    dim3 grid(rows ? (unsigned)(2 * num_sms()) : (unsigned)ceil_div(a.n, K0_THREADS));
+    if (!rows) timer_begin(stream);
     if (a.outs & OUT_ERR)
-        k0_pass_kernel<DMAX, true><<<grid, K0_THREADS, 0, stream>>>(a);
+        k0_pass_kernel<DMAX, true><<<grid, K0_THREADS, 0, stream>>>(a, rows, count);
     else
-        k0_pass_kernel<DMAX, false><<<grid, K0_THREADS, 0, stream>>>(a);
-    timer_end(stream);
+        k0_pass_kernel<DMAX, false><<<grid, K0_THREADS, 0, stream>>>(a, rows, count);
+    if (!rows) timer_end(stream);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
@@ -173,14 +190,14 @@ __global__ void __launch_bounds__(128) exact_pass_f64_kernel(const double* __res
 
 }  // namespace
 
-int launch_k0_pass(const PassArgs& a, cudaStream_t stream) {
+int launch_k0_pass(const PassArgs& a, cudaStream_t stream, const int32_t* rows, const unsigned long long* count) {
     if (a.n == 0) return SOMGB_OK;
-    if (a.d <= 4) return launch_dmax<4>(a, stream);
-    if (a.d <= 8) return launch_dmax<8>(a, stream);
-    if (a.d <= 16) return launch_dmax<16>(a, stream);
-    if (a.d <= 32) return launch_dmax<32>(a, stream);
-    if (a.d <= 64) return launch_dmax<64>(a, stream);
-    return launch_dmax<0>(a, stream);
+    if (a.d <= 4) return launch_dmax<4>(a, rows, count, stream);
+    if (a.d <= 8) return launch_dmax<8>(a, rows, count, stream);
+    if (a.d <= 16) return launch_dmax<16>(a, rows, count, stream);
+    if (a.d <= 32) return launch_dmax<32>(a, rows, count, stream);
+    if (a.d <= 64) return launch_dmax<64>(a, rows, count, stream);
+    return launch_dmax<0>(a, rows, count, stream);
 }
 
 int launch_exact_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,

@@ -46,7 +46,7 @@ namespace {
 constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
 constexpr int SLICES = 4;         // epilogue warps per TMEM lane quarter, each owning 64 of 256 columns
-constexpr int CAPS = 8;           // candidates kept per row and slice
+constexpr int CAPR = 32;          // candidates kept per row (a pool shared by the row's four slices)
 constexpr int XSTAGES = 3;
 constexpr int EPI_WARPS = 4 * SLICES;
 constexpr int MMA_WARP = EPI_WARPS;
@@ -80,11 +80,11 @@ TcShape tc_shape(int64_t m, int d) {
     s.off_x = off;
     off += XSTAGES * s.x_bytes;
     s.off_cand = off;
-    off += (size_t)SLICES * CAPS * TM * 4;
+    off += (size_t)CAPR * TM * 4;
     s.off_part = off;
     off += (size_t)SLICES * TM * 8;
     s.off_res = off;
-    off += (size_t)SLICES * (CAPS + 1) * TM * 4;
+    off += (size_t)(CAPR + 1) * TM * 4;
     s.off_center = off;
     off += align_up((size_t)d * 4, 16);
     s.off_bar = align_up(off, 8);
@@ -264,10 +264,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
-    int32_t* sCand = (int32_t*)(smem + P.off_cand);   // [slice][CAPS][TM]
+    int32_t* sCand = (int32_t*)(smem + P.off_cand);   // [CAPR][TM]: candidate units of each row
     float2* sPart = (float2*)(smem + P.off_part);     // [slice][TM]: (m1, m2) of the slice
-    float* sCandD = (float*)(smem + P.off_res);       // [slice][CAPS][TM]: float32 distance of each candidate
-    int32_t* sCandN = (int32_t*)(smem + P.off_res + (size_t)SLICES * CAPS * TM * 4);   // [slice][TM]: count
+    float* sCandD = (float*)(smem + P.off_res);       // [CAPR][TM]: float32 distance of each candidate
+    int* sCandN = (int*)(smem + P.off_res + (size_t)CAPR * TM * 4);   // [TM]: candidates claimed by the row
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
     uint64_t* x_full = bars + 1;    // [3]
@@ -519,13 +519,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             // ERR: M2 is the second smallest 8-unit group minimum, an upper bound of the second smallest s~ (two
             // groups have a unit at or below it), so the threshold derived from it keeps every possible second BMU
             const float mref = ERR ? M2 : M1;
+            // every slice has read sPart; the previous row tile's resolution finished before this tile's qbar
+            if (sl == 0) sCandN[row] = 0;
             if (!(M1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
             const float dref = fmaxf(0.0f, mref + xn);
             const float thr = flagged ? -INFINITY
                                       : mref + 2.0f * (P.alpha * xn + P.beta * dref) / (1.0f - P.beta) + 1.0e-30f;
 
-            // ---- sweep 2: every unit of this warp's columns under the threshold, in ascending order --------------
-            int cnt = 0;
+            qbar();   // the pool count is reset before any slice claims a slot
+            // ---- sweep 2: every unit of this warp's columns under the threshold --------------------------------
+
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
@@ -547,8 +550,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                             for (int i = 0; i < 4; ++i) {
                                 const int j = jb + half * 32 + g4 + i;
                                 if (v[g4 + i] <= thr && j < (int)a.m) {
-                                    if (cnt < CAPS) sCand[(sl * CAPS + cnt) * TM + row] = j;
-                                    ++cnt;
+                                    const int slot = atomicAdd(sCandN + row, 1);
+                                    if (slot < CAPR) sCand[slot * TM + row] = j;
                                 }
                             }
                         }
@@ -557,8 +560,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             }
             if (!ok) break;
 
-            // ---- resolution: float32 distances of this slice's candidates; slice 0 decides the row -------------------
-            if (live && !flagged && cnt <= CAPS && cnt > 0) {
+            // ---- resolution: float32 distances of the row's candidates (slot k by slice k % 4), then slice 0 decides
+            qbar();
+            const int total = sCandN[row];
+            if (live && !flagged && total <= CAPR) {
                 float xr[DT];
                 const float4* xs4 = (const float4*)xs;
 #pragma unroll
@@ -566,30 +571,23 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     const float4 t = xs4[k4];
                     xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
                 }
-                for (int k = 0; k < cnt; ++k) {
-                    const int32_t j = sCand[(sl * CAPS + k) * TM + row];
-                    sCandD[(sl * CAPS + k) * TM + row] = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
+                for (int k = sl; k < total; k += SLICES) {
+                    const int32_t j = sCand[k * TM + row];
+                    sCandD[k * TM + row] = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
                 }
             }
-            sCandN[sl * TM + row] = cnt;
             qbar();
             if (sl == 0 && live) {
                 // best two candidates in (float32 distance, unit) order
                 float f1 = INFINITY, f2 = INFINITY;
                 int32_t c1 = -1, c2 = -1;
-                int total = 0;
-                bool overflow = false;
-                for (int t = 0; t < SLICES; ++t) {
-                    const int n_t = sCandN[t * TM + row];
-                    total += n_t;
-                    overflow = overflow || n_t > CAPS;
-                    if (n_t > CAPS) continue;
-                    for (int k = 0; k < n_t; ++k) {
-                        const float df = sCandD[(t * CAPS + k) * TM + row];
-                        const int32_t j = sCand[(t * CAPS + k) * TM + row];
-                        if (df < f1 || (df == f1 && j < c1)) { f2 = f1; c2 = c1; f1 = df; c1 = j; }
-                        else if (df < f2 || (df == f2 && j < c2)) { f2 = df; c2 = j; }
-                    }
+                const bool overflow = total > CAPR;
+                const int nlist = overflow ? 0 : total;
+                for (int k = 0; k < nlist; ++k) {
+                    const float df = sCandD[k * TM + row];
+                    const int32_t j = sCand[k * TM + row];
+                    if (df < f1 || (df == f1 && j < c1)) { f2 = f1; c2 = c1; f1 = df; c1 = j; }
+                    else if (df < f2 || (df == f2 && j < c2)) { f2 = df; c2 = j; }
                 }
                 if (flagged || overflow || total == 0) {
                     const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
@@ -599,10 +597,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     const float lim = ERR ? f2 : f1;
                     const float climit = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
                     int ncont = 0;
-                    for (int t = 0; t < SLICES; ++t) {
-                        const int n_t = sCandN[t * TM + row];
-                        for (int k = 0; k < n_t; ++k) ncont += sCandD[(t * CAPS + k) * TM + row] <= climit;
-                    }
+                    for (int k = 0; k < nlist; ++k) ncont += sCandD[k * TM + row] <= climit;
                     SampleResult r;
                     if (ncont <= (ERR ? 2 : 1)) {
                         r.i1 = c1;
@@ -612,13 +607,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         // float64 reference sums of every contender, ranked in (distance, unit) order
                         Top2Lex tt;
                         tt.init();
-                        for (int t = 0; t < SLICES; ++t) {
-                            const int n_t = sCandN[t * TM + row];
-                            for (int k = 0; k < n_t; ++k) {
-                                if (!(sCandD[(t * CAPS + k) * TM + row] <= climit)) continue;
-                                const int32_t j = sCand[(t * CAPS + k) * TM + row];
-                                tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
-                            }
+                        for (int k = 0; k < nlist; ++k) {
+                            if (!(sCandD[k * TM + row] <= climit)) continue;
+                            const int32_t j = sCand[k * TM + row];
+                            tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
                         }
                         r.i1 = tt.i1;
                         r.i2 = ERR ? tt.i2 : -1;
@@ -650,76 +642,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     if (warp == MMA_WARP) {
         ptx::tc_fence_after();
         ptx::tmem_dealloc(tbase, 512);
-    }
-}
-
-// Exact per-row recheck: one warp per listed row, lanes split the units.
-__global__ void __launch_bounds__(256) tc_recheck_kernel(PassArgs a, const int32_t* __restrict__ rows,
-                                                         const unsigned long long* __restrict__ count) {
-    const int lane = threadIdx.x & 31;
-    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t total = (int64_t)*count;
-    const int d = a.d;
-    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
-    for (int64_t q = wid; q < total; q += nw) {
-        const int64_t i = rows[q];
-        const float* xg = a.x + i * d;
-        // float32 screening per lane, then the float64 reference distance for the units under the threshold
-        float f1 = INFINITY, f2 = INFINITY;
-        for (int64_t j = lane; j < a.m; j += 32) {
-            const float df = cand_dist32(a.w + j * d, xg, d);
-            if (df < f2) {
-                if (df < f1) { f2 = f1; f1 = df; }
-                else f2 = df;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const float o1 = __shfl_xor_sync(0xffffffffu, f1, o), o2 = __shfl_xor_sync(0xffffffffu, f2, o);
-            const float n1 = fminf(f1, o1);
-            const float n2 = fminf(fmaxf(f1, o1), fminf(f2, o2));
-            f1 = n1;
-            f2 = n2;
-        }
-        const float g32 = (float)(d + 2) * 5.9604645e-8f;
-        const float fac = 1.0f + 8.0f * g32;
-        const float lim = (a.outs & OUT_ERR) ? f2 : f1;
-        const float thr = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
-        Top2 t;
-        t.init();
-        for (int64_t j = lane; j < a.m; j += 32) {
-            const float* wr = a.w + j * d;
-            if (!(cand_dist32(wr, xg, d) <= thr)) continue;
-            t.push(ref_sqdist(wr, xg, d), (int32_t)j);
-        }
-        // merge the per-lane exact top-2 lists in (distance, index) order
-        for (int o = 16; o > 0; o >>= 1) {
-            const double od1 = __shfl_xor_sync(0xffffffffu, t.d1, o), od2 = __shfl_xor_sync(0xffffffffu, t.d2, o);
-            const int32_t oi1 = __shfl_xor_sync(0xffffffffu, t.i1, o), oi2 = __shfl_xor_sync(0xffffffffu, t.i2, o);
-            double cd[4] = {t.d1, t.d2, od1, od2};
-            int32_t ci[4] = {t.i1, t.i2, oi1, oi2};
-            double bd1 = 1.0e99, bd2 = 1.0e99;
-            int32_t bi1 = -1, bi2 = -1;
-            for (int k = 0; k < 4; ++k) {
-                if (ci[k] < 0 || ci[k] == bi1) continue;
-                const bool lt1 = bi1 < 0 || cd[k] < bd1 || (cd[k] == bd1 && ci[k] < bi1);
-                if (lt1) { bd2 = bd1; bi2 = bi1; bd1 = cd[k]; bi1 = ci[k]; }
-                else if (ci[k] != bi2 && (bi2 < 0 || cd[k] < bd2 || (cd[k] == bd2 && ci[k] < bi2))) { bd2 = cd[k]; bi2 = ci[k]; }
-            }
-            t.d1 = bd1; t.d2 = bd2; t.i1 = bi1; t.i2 = bi2;
-        }
-        if (lane == 0) {
-            SampleResult r;
-            r.i1 = t.i1;
-            r.i2 = t.i2;
-            r.d1 = t.d1;
-            emit_sample(a, i, r, e0, e1, e2);
-        }
-    }
-    if ((a.outs & OUT_ERR) && lane == 0) {
-        if (e0 != 0.0) atomicAdd(a.err3 + 0, e0);
-        if (e1 != 0.0) atomicAdd(a.err3 + 1, e1);
-        if (e2 != 0.0) atomicAdd(a.err3 + 2, e2);
     }
 }
 
@@ -868,9 +790,11 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
         }
     }
     if (st) return st;
-    tc_recheck_kernel<<<(unsigned)(2 * num_sms()), 256, 0, stream>>>(a, W.rows, a.recheck_count);
-    SOMGB_LAUNCH_CHECK();
-    return SOMGB_OK;
+    // rows the tensor-core pass could not decide: the exact CUDA-core pass over the listed rows (it must not count
+    // into the list length it reads)
+    PassArgs b = a;
+    b.recheck_count = nullptr;
+    return launch_k0_pass(b, stream, W.rows, a.recheck_count);
 }
 
 }  // namespace somgb

@@ -56,7 +56,9 @@ __device__ __forceinline__ void emit_sample(const PassArgs& a, int64_t i, const 
 }
 
 // Launches (defined in the .cu files).
-int launch_k0_pass(const PassArgs& a, cudaStream_t stream);
+// The CUDA-core pass over all samples, or over the first *count samples listed in `rows` (device memory).
+int launch_k0_pass(const PassArgs& a, cudaStream_t stream, const int32_t* rows = nullptr,
+                   const unsigned long long* count = nullptr);
 int launch_exact_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,
                           const double* topo, double penalty, int outs, int32_t* bmu_out, double* hist,
                           double* err3, int32_t* train_bmu, cudaStream_t stream);
