@@ -50,6 +50,8 @@ SIGNATURES = {
     'somgb_accumulate_f64': [P, P, P, I64, I32, I64, P, P, P],
     'somgb_find_bmus': [P, I64, I32, P, I64, I32, P, P, SZ, P],
     'somgb_find_bmus_f64': [P, I64, I32, P, I64, P, P],
+    'somgb_find_bmus_noalloc': [P, I64, I32, P, I64, I32, P, P],
+    'somgb_find_bmus_noalloc_scratch_bytes': [],
     'somgb_count_bmus': [P, P, I64, I32, P, I64, I32, P, P, SZ, P],
     'somgb_count_bmus_f64': [P, P, I64, I32, P, I64, P, P],
     'somgb_compute_errors': [P, P, I64, I32, P, P, I64, D, I32, P, P, SZ, P],
@@ -63,7 +65,8 @@ SIGNATURES = {
     'somgb_divide': [P, P, I64, I32, P, P],
     'somgb_divide_f64': [P, P, I64, I32, P, P],
 }
-_RESTYPES = {'somgb_last_error': SZ, 'somgb_workspace_bytes': SZ, 'somgb_kernel_launches': I64}
+_RESTYPES = {'somgb_last_error': SZ, 'somgb_workspace_bytes': SZ, 'somgb_kernel_launches': I64,
+             'somgb_find_bmus_noalloc_scratch_bytes': SZ}
 
 
 class SomgbError(RuntimeError):

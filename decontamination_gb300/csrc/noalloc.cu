@@ -1,0 +1,81 @@
+// BMU search that allocates nothing: somgb_find_bmus with its scratch in a fixed, file-scope device array.
+//
+// Some callers cannot allocate device memory when they need BMUs: code running inside a CUDA stream capture (no
+// cudaMalloc in captured regions), a host framework with a fixed device-memory budget handed out up front, or a C/
+// Fortran pipeline that only passes the catalogue and output buffers it already owns. For them this entry point keeps
+// its working memory in one static device array instead of a caller workspace. That array is part of the library's
+// module: every GPU that loads libsomgb holds it from module load until the process exits.
+//
+// The array is shared by every call on a device. The pass rewrites everything it reads before reading it (the unit
+// operand, the centre, the recheck list) and clears the recheck counter at the start of each pass, so results never
+// depend on what an earlier call left there; two calls that overlap on the GPU (for example on two streams) race on it.
+#include "common.cuh"
+
+#include <algorithm>
+#include <mutex>
+
+namespace somgb {
+namespace {
+
+// Large enough for the tensor-core unit operand of any supported shape (at most ~230 KB) plus the recheck list of a
+// chunk of about a million rows; inputs with more rows are processed in chunks.
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(4) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+struct ScratchAddress {
+    std::once_flag once;
+    void* ptr = nullptr;
+    cudaError_t err = cudaSuccess;
+};
+ScratchAddress g_addr[64];
+
+// Device address of the scratch array on the current device, looked up once per device with that device current.
+int scratch_address(void** out) {
+    int dev = 0;
+    SOMGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(SOMGB_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    ScratchAddress& a = g_addr[dev];
+    std::call_once(a.once, [&a] { a.err = cudaGetSymbolAddress(&a.ptr, g_noalloc_scratch); });
+    if (a.err != cudaSuccess || !a.ptr)
+        return set_error(SOMGB_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed: %s",
+                         cudaGetErrorString(a.err));
+    *out = a.ptr;
+    return SOMGB_OK;
+}
+
+}  // namespace
+}  // namespace somgb
+
+using namespace somgb;
+
+extern "C" {
+
+size_t somgb_find_bmus_noalloc_scratch_bytes(void) { return NOALLOC_SCRATCH_BYTES; }
+
+int somgb_find_bmus_noalloc(const float* x, int64_t n, int d, const float* w, int64_t m, int algo, int32_t* bmu_out,
+                            somgb_stream_t stream) {
+    if (n < 0 || m <= 0 || d <= 0)
+        return set_error(SOMGB_ERR_INVALID, "invalid sizes n=%lld m=%lld d=%d", (long long)n, (long long)m, d);
+    // the largest row chunk whose workspace fits the static array
+    int64_t chunk = std::max<int64_t>(n, 1);
+    while (chunk > 128 && somgb_workspace_bytes(SOMGB_OP_FIND_BMUS, chunk, m, d, algo) > NOALLOC_SCRATCH_BYTES)
+        chunk = std::max<int64_t>(128, chunk / 2);
+    if (somgb_workspace_bytes(SOMGB_OP_FIND_BMUS, std::min<int64_t>(chunk, std::max<int64_t>(n, 1)), m, d, algo) >
+        NOALLOC_SCRATCH_BYTES)
+        return set_error(SOMGB_ERR_WORKSPACE,
+                         "m=%lld d=%d needs more scratch than the %zu-byte static array of somgb_find_bmus_noalloc",
+                         (long long)m, d, NOALLOC_SCRATCH_BYTES);
+    void* scratch = nullptr;
+    if (int s = scratch_address(&scratch)) return s;
+    if (n == 0) return somgb_find_bmus(x, 0, d, w, m, algo, bmu_out, scratch, NOALLOC_SCRATCH_BYTES, stream);
+    for (int64_t s0 = 0; s0 < n; s0 += chunk) {
+        const int64_t len = std::min<int64_t>(chunk, n - s0);
+        const int st = somgb_find_bmus(x + s0 * d, len, d, w, m, algo, bmu_out + s0, scratch, NOALLOC_SCRATCH_BYTES,
+                                       stream);
+        if (st) return st;
+    }
+    return SOMGB_OK;
+}
+
+}  // extern "C"
