@@ -243,19 +243,22 @@ __device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, cons
     return acc;
 }
 
-// Reference distance (float64 sum of float32 squares) evaluated exactly in float32 pairs; used for d1 of QE.
-__device__ __forceinline__ double ref_dist_pair(const float* __restrict__ wr, const float* __restrict__ xs, int d) {
-    float hi = 0.0f, lo = 0.0f;
-    for (int k = 0; k < d; ++k) {
-        float t = __fsub_rn(wr[k], xs[k]);
-        float s = __fmul_rn(t, t);
-        float sum = __fadd_rn(hi, s);
-        float bb = __fsub_rn(sum, hi);
-        float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(s, bb));
-        hi = sum;
-        lo = __fadd_rn(lo, err);
+// Reference distance (float64 sum of float32 squares) as an exact float32 pair; used for d1 of QE.
+template <int DT>
+__device__ __forceinline__ DFloat ref_dist_pair(const float* __restrict__ wr, const float (&xr)[DT]) {
+    DFAcc acc;
+    const float4* w4 = (const float4*)wr;
+#pragma unroll
+    for (int k4 = 0; k4 < DT / 4; ++k4) {
+        const float4 w = __ldg(w4 + k4);
+        const float t0 = __fsub_rn(w.x, xr[4 * k4]), t1 = __fsub_rn(w.y, xr[4 * k4 + 1]);
+        const float t2 = __fsub_rn(w.z, xr[4 * k4 + 2]), t3 = __fsub_rn(w.w, xr[4 * k4 + 3]);
+        acc.add(__fmul_rn(t0, t0));
+        acc.add(__fmul_rn(t1, t1));
+        acc.add(__fmul_rn(t2, t2));
+        acc.add(__fmul_rn(t3, t3));
     }
-    return (double)hi + (double)lo;
+    return DFloat{acc.hi, acc.lo};
 }
 
 template <bool ERR, int DT>
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         const uint32_t lane_base = (uint32_t)(q * 32) << 16;
         const float g32 = (float)(d + 2) * 5.9604645e-8f;
         const float fac = 1.0f + 8.0f * g32;
-        double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+        DFAcc e0, e1, e2;
         int64_t gcons = 0;   // TMEM tiles consumed
 
         auto qbar = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(1 + q) : "memory"); };
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 #pragma unroll
                     for (int g4 = 0; g4 < 32; g4 += 4) {
                         const float gm = fminf(fminf(v[g4], v[g4 + 1]), fminf(v[g4 + 2], v[g4 + 3]));
-                        if (gm <= thr) {
+                        if (__any_sync(0xffffffffu, gm <= thr)) {
 #pragma unroll
                             for (int i = 0; i < 4; ++i) {
                                 const int j = jb + half * 32 + g4 + i;
@@ -598,11 +601,21 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     const float climit = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
                     int ncont = 0;
                     for (int k = 0; k < nlist; ++k) ncont += sCandD[k * TM + row] <= climit;
-                    SampleResult r;
+                    int32_t r1, r2;
+                    DFloat rd1{0.0f, 0.0f};
                     if (ncont <= (ERR ? 2 : 1)) {
-                        r.i1 = c1;
-                        r.i2 = ERR ? c2 : -1;
-                        r.d1 = (ERR && c1 >= 0) ? ref_dist_pair(a.w + (int64_t)c1 * d, xs, d) : 0.0;
+                        r1 = c1;
+                        r2 = ERR ? c2 : -1;
+                        if (ERR && c1 >= 0) {
+                            float xr[DT];
+                            const float4* xs4 = (const float4*)xs;
+#pragma unroll
+                            for (int k4 = 0; k4 < DT / 4; ++k4) {
+                                const float4 t = xs4[k4];
+                                xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
+                            }
+                            rd1 = ref_dist_pair<DT>(a.w + (int64_t)c1 * DT, xr);
+                        }
                     } else {
                         // float64 reference sums of every contender, ranked in (distance, unit) order
                         Top2Lex tt;
@@ -612,26 +625,28 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                             const int32_t j = sCand[k * TM + row];
                             tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
                         }
-                        r.i1 = tt.i1;
-                        r.i2 = ERR ? tt.i2 : -1;
-                        r.d1 = tt.d1;
+                        r1 = tt.i1;
+                        r2 = ERR ? tt.i2 : -1;
+                        rd1.hi = (float)tt.d1;
+                        rd1.lo = (float)(tt.d1 - (double)rd1.hi);
                     }
-                    emit_sample(a, grow, r, e0, e1, e2);
+                    emit_sample32(a, grow, r1, r2, rd1, e0, e1, e2);
                 }
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(x_empty + s3);
         }
         if (ERR) {
+            double v0 = e0.value(), v1 = e1.value(), v2 = e2.value();
             for (int o = 16; o > 0; o >>= 1) {
-                e0 += __shfl_xor_sync(0xffffffffu, e0, o);
-                e1 += __shfl_xor_sync(0xffffffffu, e1, o);
-                e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+                v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                v2 += __shfl_xor_sync(0xffffffffu, v2, o);
             }
             if (lane == 0 && (a.outs & OUT_ERR)) {
-                if (e0 != 0.0) atomicAdd(a.err3 + 0, e0);
-                if (e1 != 0.0) atomicAdd(a.err3 + 1, e1);
-                if (e2 != 0.0) atomicAdd(a.err3 + 2, e2);
+                if (v0 != 0.0) atomicAdd(a.err3 + 0, v0);
+                if (v1 != 0.0) atomicAdd(a.err3 + 1, v1);
+                if (v2 != 0.0) atomicAdd(a.err3 + 2, v2);
             }
         }
     }

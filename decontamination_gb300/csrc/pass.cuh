@@ -55,6 +55,84 @@ __device__ __forceinline__ void emit_sample(const PassArgs& a, int64_t i, const 
     }
 }
 
+// ---------------------------------------------------------------------------------------------------------------------
+// Float32 double-float helpers: exact sums and products without the (slow on this GPU) float64 pipe.
+// ---------------------------------------------------------------------------------------------------------------------
+
+struct DFloat {
+    float hi, lo;
+};
+
+// hi + lo == a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ DFloat two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return DFloat{s, e};
+}
+
+// running sum with a compensation term (error of the order of 2^-48 of the total)
+struct DFAcc {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const DFloat t = two_sum(hi, v);
+        hi = t.hi;
+        lo = __fadd_rn(lo, t.lo);
+    }
+    __device__ __forceinline__ void add(DFloat v) {
+        add(v.hi);
+        lo = __fadd_rn(lo, v.lo);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// sqrt of the double-float hi + lo (hi >= 0), to about 2^-46 relative: one Newton step on the float32 root
+__device__ __forceinline__ DFloat df_sqrt(float hi, float lo) {
+    if (!(hi > 0.0f)) return DFloat{0.0f, 0.0f};
+    const float s = sqrtf(hi);
+    const float r = __fadd_rn(fmaf(-s, s, hi), lo);
+    return DFloat{s, __fdiv_rn(r, __fmul_rn(2.0f, s))};
+}
+
+// (a.hi + a.lo) * (b.hi + b.lo) to about 2^-46 relative
+__device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = fmaf(a.hi, b.hi, -p);
+    return DFloat{p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e))};
+}
+
+// Is the reference's float64 sum of the float32 squares of the float32 topographic differences above `penalty`
+// (exactly representable)? The two squares are summed exactly in float32 pairs.
+__device__ __forceinline__ bool topo_far32(const float* __restrict__ topo, int64_t a, int64_t b, float penalty) {
+    const float t0 = __fsub_rn(topo[2 * a], topo[2 * b]);
+    const float t1 = __fsub_rn(topo[2 * a + 1], topo[2 * b + 1]);
+    const DFloat s = two_sum(__fmul_rn(t0, t0), __fmul_rn(t1, t1));
+    return s.hi > penalty || (s.hi == penalty && s.lo > 0.0f);
+}
+
+// Per-sample outputs from float32 quantities; d1 is the reference distance of b1 as a double-float.
+__device__ __forceinline__ void emit_sample32(const PassArgs& a, int64_t i, int32_t i1, int32_t i2, DFloat d1,
+                                              DFAcc& e0, DFAcc& e1, DFAcc& e2) {
+    const int outs = a.outs;
+    DFloat rho{1.0f, 0.0f};
+    bool pos = true;
+    if (a.rho) {
+        const double r = a.rho[i];
+        const long long bits = __double_as_longlong(r);
+        pos = bits > 0 && bits <= 0x7FF0000000000000LL;   // r > 0 (NaN excluded)
+        rho.hi = (float)r;
+        rho.lo = (float)(r - (double)rho.hi);
+    }
+    if (outs & OUT_BMU) a.bmu_out[i] = i1 < 0 ? 0 : i1;
+    if ((outs & OUT_HIST) && pos) atomicAdd(a.hist + (i1 < 0 ? 0 : i1), (double)rho.hi + (double)rho.lo);
+    if (outs & OUT_TRAIN) a.train_bmu[i] = (rho.hi > 0.0f && i1 >= 0) ? i1 : -1;
+    if ((outs & OUT_ERR) && pos && i1 >= 0 && i2 >= 0 && i1 != i2) {
+        e0.add(df_mul(rho, df_sqrt(d1.hi, d1.lo)));
+        if (topo_far32(a.topo, i1, i2, (float)a.penalty)) e1.add(rho);
+        e2.add(rho);
+    }
+}
+
 // Launches (defined in the .cu files).
 // The CUDA-core pass over all samples, or over the first *count samples listed in `rows` (device memory).
 int launch_k0_pass(const PassArgs& a, cudaStream_t stream, const int32_t* rows = nullptr,
