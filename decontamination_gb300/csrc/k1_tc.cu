@@ -41,6 +41,27 @@ namespace somgb {
 // Sticky device status: bit set by any bounded wait of the tensor-core pass that gave up (0 = healthy).
 __device__ unsigned int g_tc_status;
 
+// Optional per-phase cycle counters of the epilogue warps (compiled in only with -DSOMGB_TC_PHASE_TIMING; read with
+// cudaMemcpyFromSymbol). Phases: 0 wait for TMEM (sweep 1), 1 sweep 1, 2 wait (sweep 2), 3 sweep 2, 4 convert,
+// 5 row barriers, 6 resolution, 7 slice-0 decision.
+#ifdef SOMGB_TC_PHASE_TIMING
+__device__ unsigned long long g_tc_phase_cycles[8];
+#define TC_T0() _tc_t0 = clock64()
+#define TC_T(ph)                                    \
+    do {                                            \
+        const long long _tc_t1 = clock64();         \
+        _tc_acc[ph] += (unsigned long long)(_tc_t1 - _tc_t0); \
+        _tc_t0 = _tc_t1;                            \
+    } while (0)
+#else
+#define TC_T0() \
+    do {        \
+    } while (0)
+#define TC_T(ph) \
+    do {         \
+    } while (0)
+#endif
+
 namespace {
 
 constexpr int TM = 128;           // samples per row tile (MMA M)
@@ -219,15 +240,6 @@ struct TcArgs {
 };
 
 // float32 distance over the reference's float32 differences (FMA chain): |df - d_ref| <= (D+2) 2^-24 d_ref
-__device__ __forceinline__ float cand_dist32(const float* __restrict__ wr, const float* __restrict__ xs, int d) {
-    float acc = 0.0f;
-    for (int k = 0; k < d; ++k) {
-        float t = wr[k] - xs[k];
-        acc = fmaf(t, t, acc);
-    }
-    return acc;
-}
-
 template <int DT>
 __device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, const float (&xr)[DT]) {
     float acc = 0.0f;
@@ -397,6 +409,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         const float fac = 1.0f + 8.0f * g32;
         DFAcc e0, e1, e2;
         int64_t gcons = 0;   // TMEM tiles consumed
+#ifdef SOMGB_TC_PHASE_TIMING
+        unsigned long long _tc_acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        long long _tc_t0 = 0;
+#endif
 
         auto qbar = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(1 + q) : "memory"); };
 
@@ -469,7 +485,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         bool ok = n_my > 0 ? convert(0, xn_next) : true;
         for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
             const float xn = xn_next;
+            TC_T0();
             if (it + 1 < n_my && !(ok = convert(it + 1, xn_next))) break;
+            TC_T(4);
             const int s3 = (int)(it % XSTAGES);
             const int64_t tile = blockIdx.x + it * gridDim.x;
             const int64_t grow = tile * TM + row;
@@ -482,6 +500,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
+                TC_T(0);
                 ptx::tc_fence_after();
                 float v0[32], v1[32];
                 load64(buf, v0, v1);
@@ -504,6 +523,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         b1 = fminf(b1, gb);
                     }
                 }
+                TC_T(1);
             }
             if (!ok) break;
             {
@@ -512,6 +532,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 sPart[sl * TM + row] = make_float2(m1, m2);
             }
             qbar();
+            TC_T(5);
             float M1 = INFINITY, M2 = INFINITY;
 #pragma unroll
             for (int t = 0; t < SLICES; ++t) {
@@ -530,11 +551,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                                       : mref + 2.0f * (P.alpha * xn + P.beta * dref) / (1.0f - P.beta) + 1.0e-30f;
 
             qbar();   // the pool count is reset before any slice claims a slot
+            TC_T(5);
             // ---- sweep 2: every unit of this warp's columns under the threshold --------------------------------
 
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
+                TC_T(2);
                 ptx::tc_fence_after();
                 float v0[32], v1[32];
                 load64(buf, v0, v1);
@@ -560,11 +583,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         }
                     }
                 }
+                TC_T(3);
             }
             if (!ok) break;
 
             // ---- resolution: float32 distances of the row's candidates (slot k by slice k % 4), then slice 0 decides
             qbar();
+            TC_T(5);
             const int total = sCandN[row];
             if (live && !flagged && total <= CAPR) {
                 float xr[DT];
@@ -579,7 +604,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     sCandD[k * TM + row] = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
                 }
             }
+            TC_T(6);
             qbar();
+            TC_T(5);
             if (sl == 0 && live) {
                 // best two candidates in (float32 distance, unit) order
                 float f1 = INFINITY, f2 = INFINITY;
@@ -635,7 +662,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(x_empty + s3);
+            TC_T(7);
         }
+#ifdef SOMGB_TC_PHASE_TIMING
+        if (lane == 0)
+            for (int ph = 0; ph < 8; ++ph) atomicAdd(&g_tc_phase_cycles[ph], _tc_acc[ph]);
+#endif
         if (ERR) {
             double v0 = e0.value(), v1 = e1.value(), v2 = e2.value();
             for (int o = 16; o > 0; o >>= 1) {
@@ -723,6 +755,19 @@ bool tc_supported(int64_t n, int64_t m, int d, int algo) {
     if (algo == SOMGB_ALGO_AUTO && n * m < ((int64_t)1 << 22)) return false;   // small passes: K0 has no prep cost
     return device_is_sm103() && encode_fn() != nullptr && max_smem_optin() >= tc_shape(m, d).smem;
 }
+
+#ifdef SOMGB_TC_PHASE_TIMING
+// Instrumented builds only: copies out (and optionally clears) the eight phase counters.
+extern "C" int somgb_tc_phase_cycles(unsigned long long* out8, int reset) {
+    SOMGB_CUDA_TRY(cudaDeviceSynchronize());
+    SOMGB_CUDA_TRY(cudaMemcpyFromSymbol(out8, g_tc_phase_cycles, 8 * sizeof(unsigned long long)));
+    if (reset) {
+        unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        SOMGB_CUDA_TRY(cudaMemcpyToSymbol(g_tc_phase_cycles, z, sizeof(z)));
+    }
+    return SOMGB_OK;
+}
+#endif
 
 int read_device_status(unsigned int* status, bool clear, cudaStream_t stream) {
     SOMGB_CUDA_TRY(cudaMemcpyFromSymbolAsync(status, g_tc_status, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost,
