@@ -56,19 +56,12 @@ __device__ SampleResult exact_top2(const PassArgs& a, const float* __restrict__ 
 template <int DMAX, bool TOP3>
 __device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live);
 
-// rows == NULL: thread t of block b handles sample b*128 + t. Otherwise the blocks stride over the first *count
-// entries of `rows` (a list of sample indices), 128 per block and iteration.
+// Thread t of block b handles sample b*128 + t.
 template <int DMAX, bool TOP3>
-__global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a, const int32_t* __restrict__ rows,
-                                                             const unsigned long long* __restrict__ count) {
-    const int64_t total = rows ? (int64_t)*count : a.n;
-    const int64_t step = rows ? (int64_t)gridDim.x * K0_THREADS : total + 1;
-    for (int64_t base = (int64_t)blockIdx.x * K0_THREADS; base < total; base += step) {
-        const int64_t e = base + threadIdx.x;
-        const bool live = e < total;
-        const int64_t i = !live ? 0 : (rows ? (int64_t)rows[e] : e);
-        k0_block<DMAX, TOP3>(a, i, live);
-    }
+__global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a) {
+    const int64_t e = (int64_t)blockIdx.x * K0_THREADS + threadIdx.x;
+    const bool live = e < a.n;
+    k0_block<DMAX, TOP3>(a, live ? e : 0, live);
 }
 
 template <int DMAX, bool TOP3>
@@ -149,14 +142,157 @@ __device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live
 }
 
 template <int DMAX>
-int launch_dmax(const PassArgs& a, const int32_t* rows, const unsigned long long* count, cudaStream_t stream) {
-    dim3 grid(rows ? (unsigned)(2 * num_sms()) : (unsigned)ceil_div(a.n, K0_THREADS));
-    if (!rows) timer_begin(stream);
+int launch_dmax(const PassArgs& a, cudaStream_t stream) {
+    const dim3 grid((unsigned)ceil_div(a.n, K0_THREADS));
+    timer_begin(stream);
     if (a.outs & OUT_ERR)
-        k0_pass_kernel<DMAX, true><<<grid, K0_THREADS, 0, stream>>>(a, rows, count);
+        k0_pass_kernel<DMAX, true><<<grid, K0_THREADS, 0, stream>>>(a);
     else
-        k0_pass_kernel<DMAX, false><<<grid, K0_THREADS, 0, stream>>>(a, rows, count);
-    if (!rows) timer_end(stream);
+        k0_pass_kernel<DMAX, false><<<grid, K0_THREADS, 0, stream>>>(a);
+    timer_end(stream);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------------
+// Listed rows: one warp per sample. The rows the tensor-core pass leaves undecided are few (typically 1e-4 of a
+// catalogue) and scattered, so a thread per sample would leave most SMs idle and run each sample's unit scan as one
+// latency-bound chain. Here lane l scans units l, l+32, ...; the per-lane rankings are merged across the warp in
+// (distance, unit) order, which is the order the one-thread scan ranks in (strict comparisons in ascending unit
+// order keep the lowest unit among equal distances).
+// ---------------------------------------------------------------------------------------------------------------------
+
+constexpr int KR_THREADS = 256;
+
+// (da, ja) ranks before (db, jb): lexicographic, empty entries (unit < 0) last
+__device__ __forceinline__ bool lex_before32(float da, int32_t ja, float db, int32_t jb) {
+    return ja >= 0 && (jb < 0 || da < db || (da == db && ja < jb));
+}
+__device__ __forceinline__ bool lex_before64(double da, int32_t ja, double db, int32_t jb) {
+    return ja >= 0 && (jb < 0 || da < db || (da == db && ja < jb));
+}
+
+// float32 FMA-chain distance in feature order (the chain of k0_block)
+template <int DMAX>
+__device__ __forceinline__ float row_dist32(const float* __restrict__ wr, const float* __restrict__ xr, int d) {
+    float acc = 0.0f;
+    if constexpr (DMAX > 0) {
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) {
+            const float t = __ldg(wr + k) - xr[k];
+            acc = fmaf(t, t, acc);
+        }
+    } else {
+        for (int k = 0; k < d; ++k) {
+            const float t = __ldg(wr + k) - xr[k];
+            acc = fmaf(t, t, acc);
+        }
+    }
+    return acc;
+}
+
+template <int DMAX, bool TOP3>
+__global__ void __launch_bounds__(KR_THREADS) k0_rows_kernel(PassArgs a, const int32_t* __restrict__ rows,
+                                                             const unsigned long long* __restrict__ count) {
+    const int lane = threadIdx.x & 31;
+    const int64_t total = (int64_t)*count;
+    const int64_t nwarps = (int64_t)gridDim.x * (KR_THREADS / 32);
+    const int d = a.d;
+    const float g = (float)(d + 2) * 5.9604645e-8f;
+    const float fac = 1.0f + 8.0f * g;
+    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+    for (int64_t r = (int64_t)blockIdx.x * (KR_THREADS / 32) + (threadIdx.x >> 5); r < total; r += nwarps) {
+        const int64_t i = rows[r];
+        const float* xg = a.x + i * d;
+        float xl[DMAX > 0 ? DMAX : 1];
+        if constexpr (DMAX > 0) {
+#pragma unroll
+            for (int k = 0; k < DMAX; ++k) xl[k] = __ldg(xg + k);
+        }
+        const float* xr = DMAX > 0 ? xl : xg;
+
+        // float32 top-3 of this lane's units, then of the warp
+        float m1 = INFINITY, m2 = INFINITY, m3 = INFINITY;
+        int32_t u1 = -1, u2 = -1, u3 = -1;
+        for (int64_t j = lane; j < a.m; j += 32) {
+            const float df = row_dist32<DMAX>(a.w + j * d, xr, d);
+            if (df < m3) {
+                if (df < m2) {
+                    m3 = m2; u3 = u2;
+                    if (df < m1) { m2 = m1; u2 = u1; m1 = df; u1 = (int32_t)j; }
+                    else { m2 = df; u2 = (int32_t)j; }
+                } else { m3 = df; u3 = (int32_t)j; }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float p1 = __shfl_xor_sync(0xffffffffu, m1, o), p2 = __shfl_xor_sync(0xffffffffu, m2, o),
+                        p3 = __shfl_xor_sync(0xffffffffu, m3, o);
+            const int32_t q1 = __shfl_xor_sync(0xffffffffu, u1, o), q2 = __shfl_xor_sync(0xffffffffu, u2, o),
+                          q3 = __shfl_xor_sync(0xffffffffu, u3, o);
+            const float pv[3] = {p1, p2, p3};
+            const int32_t qv[3] = {q1, q2, q3};
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                const float dv = pv[t];
+                const int32_t jv = qv[t];
+                if (lex_before32(dv, jv, m3, u3)) {
+                    if (lex_before32(dv, jv, m2, u2)) {
+                        m3 = m2; u3 = u2;
+                        if (lex_before32(dv, jv, m1, u1)) { m2 = m1; u2 = u1; m1 = dv; u1 = jv; }
+                        else { m2 = dv; u2 = jv; }
+                    } else { m3 = dv; u3 = jv; }
+                }
+            }
+        }
+
+        bool ok = m1 < 1.0e37f && m2 < 1.0e37f && m2 > fmaf(m1, fac, 1.0e-37f);
+        if (TOP3) ok = ok && m3 < 1.0e37f && m3 > fmaf(m2, fac, 1.0e-37f);
+        SampleResult res;
+        if (ok) {
+            res.i1 = u1;
+            res.i2 = TOP3 ? u2 : -1;
+            res.d1 = (a.outs & OUT_ERR) ? ref_sqdist(a.w + (int64_t)u1 * d, xg, d) : 0.0;
+        } else {
+            // exact path: the reference's float64 sum for every unit the float32 screen cannot exclude
+            if (a.recheck_count && lane == 0) atomicAdd(a.recheck_count, 1ull);
+            const float thr = m2 < 1.0e37f ? fmaf(m2, fac, 1.0e-37f) : INFINITY;
+            Top2 t;
+            t.init();
+            for (int64_t j = lane; j < a.m; j += 32) {
+                const float* wr = a.w + j * d;
+                const float df = row_dist32<DMAX>(wr, xr, d);
+                if (!(df <= thr)) continue;   // also drops NaN, whose reference distance is NaN as well
+                t.push(ref_sqdist(wr, xg, d), (int32_t)j);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double p1 = __shfl_xor_sync(0xffffffffu, t.d1, o), p2 = __shfl_xor_sync(0xffffffffu, t.d2, o);
+                const int32_t q1 = __shfl_xor_sync(0xffffffffu, t.i1, o), q2 = __shfl_xor_sync(0xffffffffu, t.i2, o);
+                const double pv[2] = {p1, p2};
+                const int32_t qv[2] = {q1, q2};
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    if (lex_before64(pv[k], qv[k], t.d2, t.i2)) {
+                        if (lex_before64(pv[k], qv[k], t.d1, t.i1)) { t.d2 = t.d1; t.i2 = t.i1; t.d1 = pv[k]; t.i1 = qv[k]; }
+                        else { t.d2 = pv[k]; t.i2 = qv[k]; }
+                    }
+                }
+            }
+            res.i1 = t.i1;
+            res.i2 = t.i2;
+            res.d1 = t.d1;
+        }
+        if (lane == 0) emit_sample(a, i, res, e0, e1, e2);
+    }
+    if (a.outs & OUT_ERR) block_add3(e0, e1, e2, a.err3);
+}
+
+template <int DMAX>
+int launch_rows(const PassArgs& a, const int32_t* rows, const unsigned long long* count, cudaStream_t stream) {
+    const dim3 grid((unsigned)(4 * num_sms()));
+    if (a.outs & OUT_ERR)
+        k0_rows_kernel<DMAX, true><<<grid, KR_THREADS, 0, stream>>>(a, rows, count);
+    else
+        k0_rows_kernel<DMAX, false><<<grid, KR_THREADS, 0, stream>>>(a, rows, count);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
@@ -192,12 +328,21 @@ __global__ void __launch_bounds__(128) exact_pass_f64_kernel(const double* __res
 
 int launch_k0_pass(const PassArgs& a, cudaStream_t stream, const int32_t* rows, const unsigned long long* count) {
     if (a.n == 0) return SOMGB_OK;
-    if (a.d <= 4) return launch_dmax<4>(a, rows, count, stream);
-    if (a.d <= 8) return launch_dmax<8>(a, rows, count, stream);
-    if (a.d <= 16) return launch_dmax<16>(a, rows, count, stream);
-    if (a.d <= 32) return launch_dmax<32>(a, rows, count, stream);
-    if (a.d <= 64) return launch_dmax<64>(a, rows, count, stream);
-    return launch_dmax<0>(a, rows, count, stream);
+    if (rows) {
+        switch (a.d) {
+            case 4: return launch_rows<4>(a, rows, count, stream);
+            case 8: return launch_rows<8>(a, rows, count, stream);
+            case 16: return launch_rows<16>(a, rows, count, stream);
+            case 32: return launch_rows<32>(a, rows, count, stream);
+            default: return launch_rows<0>(a, rows, count, stream);
+        }
+    }
+    if (a.d <= 4) return launch_dmax<4>(a, stream);
+    if (a.d <= 8) return launch_dmax<8>(a, stream);
+    if (a.d <= 16) return launch_dmax<16>(a, stream);
+    if (a.d <= 32) return launch_dmax<32>(a, stream);
+    if (a.d <= 64) return launch_dmax<64>(a, stream);
+    return launch_dmax<0>(a, stream);
 }
 
 int launch_exact_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,
