@@ -123,9 +123,13 @@ int check_common(const void* x, int64_t n, int d, const void* w, int64_t m, int 
 int run_pass(PassArgs a, int algo, const Workspace& ws, bool tc, cudaStream_t stream) {
     SOMGB_CUDA_TRY(cudaMemsetAsync(ws.counter, 0, sizeof(unsigned long long), stream));
     a.recheck_count = ws.counter;
-    if (tc && ((uintptr_t)a.x) % 16 == 0) return launch_tc_pass(a, ws.tc, ws.tc_bytes, stream);
+    // the tensor-core pass reads sample and unit rows as float4 and topographic coordinates as float2
+    const bool aligned = ((uintptr_t)a.x) % 16 == 0 && ((uintptr_t)a.w) % 16 == 0 &&
+                         (!(a.outs & OUT_ERR) || ((uintptr_t)a.topo) % 8 == 0);
+    if (tc && aligned) return launch_tc_pass(a, ws.tc, ws.tc_bytes, stream);
     if (tc && algo == SOMGB_ALGO_TC)
-        return set_error(SOMGB_ERR_INVALID, "the tensor-core pass needs x 16-byte aligned");
+        return set_error(SOMGB_ERR_INVALID,
+                         "the tensor-core pass needs x and w 16-byte aligned and the topography 8-byte aligned");
     if (algo == SOMGB_ALGO_TC)
         return set_error(SOMGB_ERR_UNSUPPORTED, "tensor-core path unsupported for n=%lld m=%lld d=%d on this device",
                          (long long)a.n, (long long)a.m, a.d);

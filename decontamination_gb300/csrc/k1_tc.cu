@@ -1,37 +1,46 @@
-// K1: BMU search on the tcgen05 tensor cores (split-BF16 distance GEMM), exact by construction.
+// K1: BMU search on the tcgen05 tensor cores (split-FP16 distance GEMM), exact by construction.
 //
-// Distances are expanded as |x - w_j|^2 = |x'|^2 + s_j with s_j = |w'_j|^2 - 2 x'.w'_j, where x' = x - c and
-// w' = w - c are centred on the mean unit c (the centring shrinks every error term below). One GEMM per 128-sample
-// row tile and 256-unit column tile produces s~_j in TMEM:
-//   A row (sample)  = [ x'_hi | x'_lo | x'_hi | 1 | 1 | 0 ... ]            (BF16, K padded to a multiple of 16)
-//   B row (unit j)  = [ -2w'_hi | -2w'_hi | -2w'_lo | q_hi | q_lo | 0 ... ] with q = |w'_j|^2
-// so that sum_k A.B = -2 (x_hi w_hi + x_lo w_hi + x_hi w_lo) + q ~ s_j, accumulated in FP32.
+// Distances are expanded as |x - w_j|^2 = |x'|^2 + s_j with s_j = |w'_j|^2 - 2 x'.w'_j, where x' = (x - c) S and
+// w' = (w - c) S are centred on the mean unit c (the centring shrinks every error term below) and scaled by a power
+// of two S that puts the largest unit coordinate in [2^9, 2^10) (FP16 range; exact in float32). One GEMM per
+// 128-sample row tile and 256-unit column tile produces s~_j in TMEM:
+//   A row (sample)  = [ x'_hi | x'_lo | x'_hi | 2^11 | 2^11 | 0 ... ]             (FP16, K padded to a multiple of 16)
+//   B row (unit j)  = [ -2w'_hi | -2w'_hi | -2w'_lo | q_hi | q_lo | 0 ... ] with q_hi + q_lo = 2^-11 |w'_j|^2
+// so that sum_k A.B = -2 (x_hi w_hi + x_lo w_hi + x_hi w_lo) + |w'|^2 ~ s_j, accumulated in FP32. Invalid and padding
+// units carry q_hi = +inf (s~ = +inf); rows with a coordinate at or above 2^15 after scaling, or non-finite, go to
+// the exact recheck.
 //
-// Error bound. With BF16 unit roundoff 2^-8, dropping x_lo w_lo and the two-term residuals costs at most
-// 3.01 * 2^-16 |x'_k||w'_k| per product; q's split and float32 evaluation cost 2.5 * 2^-16 |w'|^2; the FP32 accumulation of
-// the K non-zero products is bounded by K * 2^-23 * sum|terms| (one rounding per product, the worst case).
+// Error bound. With FP16 unit roundoff 2^-11, dropping x_lo w_lo and the two-term residuals costs at most
+// 3.01 * 2^-22 |x'_k||w'_k| per product; q's split and float32 evaluation cost 2.5 * 2^-22 |w'|^2 + (D+2) 2^-24 |w'|^2;
+// the FP32 accumulation of the K non-zero products is bounded by K * 2^-23 * sum|terms| (one rounding per product,
+// the worst case); FP16 subnormals add an absolute 2^-8 at most.
 // Using |w'_j|^2 <= 2|x'|^2 + 2 d'_j (d'_j = |x' - w'_j|^2) every term is bounded by
-//   |s~_j - s_j| <= alpha |x'|^2 + beta d'_j,
+//   |s~_j - s_j| <= alpha |x'|^2 + beta d'_j + gamma,
 // with alpha, beta computed on the host (tc_error_coefficients). A unit can beat the tile's best (or, for the
-// error sums, the second best) only if s~_j <= m + 2 (alpha |x'|^2 + beta (m + |x'|^2)) / (1 - beta), m being the
-// best (second-best) s~ of the row.
+// error sums, the second best) only if s~_j <= m + 2 (alpha |x'|^2 + beta (m + |x'|^2) + gamma) / (1 - beta), m
+// being the best (second-best) s~ of the row.
 //
 // Epilogue, per row tile: sweep 1 streams the TMEM tiles and keeps the best (and second-best) s~ per row with
 // FP32 min/max (full-rate ALU); sweep 2 recomputes the same MMAs (the tensor pipe has slack) and collects every
 // unit under that threshold — the only units that can be the reference's BMU (or second BMU). Each candidate's
 // distance is then evaluated on CUDA cores with float32 differences (the reference's terms) and, when two
 // candidates are within float32 rounding of each other, with the reference's float64 sum. Rows with more than
-// CAP candidates, non-finite features or overflowing distances go to an exact per-row recheck kernel.
+// CAPR candidates, non-finite features or overflowing distances go to an exact per-row recheck.
 //
-// Pipeline (one persistent CTA per SM, 192 threads):
-//   warp 5      TMA producer: the unit operand B once (bulk copy), sample tiles (2-D tiled TMA, 3-stage ring);
-//   warp 4      TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
-//   warps 0-3   converter (FP32 tile -> centred split-BF16 A tile) and epilogue; thread r owns TMEM lane r.
-#include <cuda_bf16.h>
+// Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
+//   warp 13     TMA producer: the unit operand B once (bulk copy), sample tiles (2-D tiled TMA, 3-stage ring);
+//   warp 12     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
+//   warps 0-7   converters (FP32 tile -> centred split-BF16 A tile) and sweeps; warp e reads TMEM lanes
+//               32(e&3).. and column half e>>2, and writes the candidates of its rows into a double buffer;
+//   warps 8-11  resolvers: thread r of warp 8+q decides row 32q+r of row tile t (distances from the unit rows in
+//               L2, ranking, outputs) while the sweeps already work on row tile t+1, so that the L2 latency of
+//               the candidate rows overlaps the tensor and sweep work.
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "tc.cuh"
 #include "tc_ptx.cuh"
@@ -42,10 +51,11 @@ namespace somgb {
 __device__ unsigned int g_tc_status;
 
 // Optional per-phase cycle counters of the epilogue warps (compiled in only with -DSOMGB_TC_PHASE_TIMING; read with
-// cudaMemcpyFromSymbol). Phases: 0 wait for TMEM (sweep 1), 1 sweep 1, 2 wait (sweep 2), 3 sweep 2, 4 convert,
-// 5 row barriers, 6 resolution, 7 slice-0 decision.
+// cudaMemcpyFromSymbol). Sweep warps: 0 wait for TMEM (sweep 1), 1 sweep 1, 2 wait (sweep 2), 3 sweep 2, 4 convert,
+// 5 half exchange and candidate-buffer wait; resolver warps: 6 wait for candidates, 7 resolution and outputs.
 #ifdef SOMGB_TC_PHASE_TIMING
-__device__ unsigned long long g_tc_phase_cycles[8];
+constexpr int TC_PHASES = 12;
+__device__ unsigned long long g_tc_phase_cycles[TC_PHASES];
 #define TC_T0() _tc_t0 = clock64()
 #define TC_T(ph)                                    \
     do {                                            \
@@ -66,23 +76,28 @@ namespace {
 
 constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
-constexpr int SLICES = 4;         // epilogue warps per TMEM lane quarter, each owning 64 of 256 columns
-constexpr int CAPR = 32;          // candidates kept per row (a pool shared by the row's four slices)
+constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
+constexpr int CAPR = 32;          // candidates a resolver keeps per row (unit indices as uint16)
+constexpr int MAX_U = 8;          // column tiles per row tile (the candidate summary is a 32-bit word per half)
 constexpr int XSTAGES = 3;
-constexpr int EPI_WARPS = 4 * SLICES;
-constexpr int MMA_WARP = EPI_WARPS;
-constexpr int TMA_WARP = EPI_WARPS + 1;
-constexpr int NUM_THREADS = (EPI_WARPS + 2) * 32;
-constexpr float BIG = 3.0e38f;    // s~ of padding / invalid units
+constexpr int SWEEP_WARPS = 4 * HALVES;
+constexpr int RES_WARPS = 4;
+constexpr int MMA_WARP = SWEEP_WARPS + RES_WARPS;
+constexpr int TMA_WARP = MMA_WARP + 1;
+constexpr int NUM_THREADS = (TMA_WARP + 1) * 32;
+constexpr float X_LIMIT = 32768.0f;   // scaled sample coordinates at or above this go to the exact recheck
+constexpr float Q_COLUMN = 2048.0f;   // A's value in the two q columns (B holds q / 2^11)
+constexpr float GAMMA = 0.00390625f;  // 2^-8: absolute error bound of the FP16 subnormal range, in scaled units
 constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go to the exact recheck
-constexpr uint32_t IDESC = ptx::idesc_bf16_f32(TM, TN);
+constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN);
 
 struct TcShape {
     int d = 0, kpad = 0, knz = 0;
     int64_t mpad = 0;
     int utiles = 0;
     size_t b_bytes = 0, a_bytes = 0, x_bytes = 0;
-    size_t off_a = 0, off_x = 0, off_cand = 0, off_part = 0, off_res = 0, off_center = 0, off_bar = 0, smem = 0;
+    size_t off_a = 0, off_x = 0, off_mask = 0, off_sum = 0, off_flag = 0, off_rlist = 0, off_part = 0, off_center = 0,
+           off_bar = 0, smem = 0;
 };
 
 TcShape tc_shape(int64_t m, int d) {
@@ -100,21 +115,25 @@ TcShape tc_shape(int64_t m, int d) {
     off += 2 * align_up(s.a_bytes, 1024);
     s.off_x = off;
     off += XSTAGES * s.x_bytes;
-    s.off_cand = off;
-    off += (size_t)CAPR * TM * 4;
+    s.off_mask = off;
+    off += (size_t)HALVES * s.utiles * 4 * TM * 4;
+    s.off_sum = off;
+    off += (size_t)HALVES * TM * 4;
+    s.off_flag = off;
+    off += TM;
+    s.off_rlist = off;
+    off += (size_t)(CAPR + 1) * TM * 2;
     s.off_part = off;
-    off += (size_t)SLICES * TM * 8;
-    s.off_res = off;
-    off += (size_t)(CAPR + 1) * TM * 4;
+    off += (size_t)2 * HALVES * TM * 8;
     s.off_center = off;
-    off += align_up((size_t)d * 4, 16);
+    off += align_up((size_t)(d + 1) * 4, 16);
     s.off_bar = align_up(off, 8);
-    off = s.off_bar + 16 * 8;
+    off = s.off_bar + 32 * 8;
     s.smem = off + 1024;   // slack for aligning the dynamic base to 1024
     return s;
 }
 
-// Scratch: [B operand | centre (d floats) | recheck row list (n int32)]
+// Scratch: [B operand | centre (d floats) and scale | recheck row list (n int32)]
 struct TcWs {
     uint8_t* b = nullptr;
     float* center = nullptr;
@@ -127,7 +146,7 @@ size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
     size_t ob = off;
     off += align_up(s.b_bytes, 256);
     size_t oc = off;
-    off += align_up((size_t)d * 4, 256);
+    off += align_up((size_t)(d + 1) * 4, 256);   // centre and scale
     size_t orow = off;
     off += align_up((size_t)std::max<int64_t>(n, 1) * 4, 256);
     if (out && base) {
@@ -140,12 +159,14 @@ size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
 }
 
 void tc_error_coefficients(int d, float* alpha, float* beta) {
-    const double u16 = std::ldexp(1.0, -16);
+    const double u22 = std::ldexp(1.0, -22);
     const double knz = 3.0 * d + 2.0;
     const double acc = knz * std::ldexp(1.0, -23);       // one rounding per product, worst case
-    // representation: 3.01*2^-16 (|x'|^2 + |w'|^2) from -2 x'.w'; 2.5*2^-16 |w'|^2 from q; |w'|^2 <= 2|x'|^2 + 2d'
-    double a = 3.01 * u16 * 3.0 + 2.5 * u16 * 2.0 + acc * 5.05;
-    double b = 3.01 * u16 * 2.0 + 2.5 * u16 * 2.0 + acc * 4.04;
+    // representation: 3.01*2^-22 (|x'|^2 + |w'|^2) from -2 x'.w'; 2.5*2^-22 |w'|^2 from q's split and (D+2) 2^-24 |w'|^2
+    // from its float32 evaluation; |w'|^2 <= 2|x'|^2 + 2d'
+    const double qe = 2.5 * u22 + (d + 2.0) * std::ldexp(1.0, -24);
+    double a = 3.01 * u22 * 3.0 + qe * 2.0 + acc * 5.05;
+    double b = 3.01 * u22 * 2.0 + qe * 2.0 + acc * 4.04;
     // centring rounding and the reference's own float32 rounding of each term
     a += std::ldexp(1.0, -21);
     b += std::ldexp(1.0, -21);
@@ -158,10 +179,12 @@ void tc_error_coefficients(int d, float* alpha, float* beta) {
 // ---------------------------------------------------------------------------------------------------------------------
 
 __global__ void tc_center_kernel(const float* __restrict__ w, int64_t m, int d, float* __restrict__ center) {
-    // mean of the finite unit rows, per feature, in float64
+    // mean of the finite unit rows, per feature, in float64; then center[d] = the power-of-two scale S that puts the
+    // largest |w - c| coordinate of those rows in [2^9, 2^10)
     __shared__ double part[256];
     __shared__ unsigned long long cnt_s;
-    if (threadIdx.x == 0) cnt_s = 0;
+    __shared__ unsigned int maxbits_s;
+    if (threadIdx.x == 0) { cnt_s = 0; maxbits_s = 0u; }
     __syncthreads();
     for (int k = 0; k < d; ++k) {
         double s = 0.0;
@@ -181,6 +204,20 @@ __global__ void tc_center_kernel(const float* __restrict__ w, int64_t m, int d, 
         if (threadIdx.x == 0) center[k] = cnt_s ? (float)(part[0] / (double)cnt_s) : 0.0f;
         __syncthreads();
     }
+    for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
+        bool ok = true;
+        for (int q = 0; q < d; ++q) ok = ok && isfinite(w[j * d + q]);
+        if (!ok) continue;
+        for (int k = 0; k < d; ++k) atomicMax(&maxbits_s, __float_as_uint(fabsf(w[j * d + k] - center[k])));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const float mx = __uint_as_float(maxbits_s);
+        int e = 0;
+        if (mx > 0.0f && isfinite(mx)) frexpf(mx, &e);   // mx < 2^e
+        else e = 10;
+        center[d] = ldexpf(1.0f, min(max(10 - e, -100), 100));
+    }
 }
 
 __device__ __forceinline__ size_t canon_off(int64_t row, int k, int kpad) {
@@ -191,35 +228,36 @@ __global__ void tc_prep_b_kernel(const float* __restrict__ w, int64_t m, int d, 
                                  const float* __restrict__ center, uint8_t* __restrict__ b) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= mpad) return;
-    __nv_bfloat16* out = (__nv_bfloat16*)b;
-    auto put = [&](int k, float v) { *(__nv_bfloat16*)((uint8_t*)out + canon_off(j, k, kpad)) = __float2bfloat16_rn(v); };
+    auto put = [&](int k, float v) { *(__half*)(b + canon_off(j, k, kpad)) = __float2half_rn(v); };
+    const float scale = center[d];
     bool valid = j < m;
     float q = 0.0f;
     if (valid) {
         for (int k = 0; k < d; ++k) {
-            float v = w[j * d + k];
+            const float v = w[j * d + k];
             if (!isfinite(v)) valid = false;
-            float t = v - center[k];
+            const float t = (v - center[k]) * scale;
             q = fmaf(t, t, q);
         }
-        if (!(q < HUGE_S)) valid = false;
+        if (!(q < 1.0e30f)) valid = false;
     }
     for (int k = 0; k < kpad; ++k) put(k, 0.0f);
     if (!valid) {
-        put(3 * d, BIG);   // never the minimum; s~ = BIG
+        put(3 * d, INFINITY);   // never the minimum, never under a threshold: s~ = +inf
         return;
     }
     for (int k = 0; k < d; ++k) {
-        float t = w[j * d + k] - center[k];
-        __nv_bfloat16 hi = __float2bfloat16_rn(t);
-        __nv_bfloat16 lo = __float2bfloat16_rn(t - __bfloat162float(hi));
-        put(k, -2.0f * __bfloat162float(hi));
-        put(d + k, -2.0f * __bfloat162float(hi));
-        put(2 * d + k, -2.0f * __bfloat162float(lo));
+        const float t = (w[j * d + k] - center[k]) * scale;
+        const __half hi = __float2half_rn(t);
+        const __half lo = __float2half_rn(t - __half2float(hi));
+        put(k, -2.0f * __half2float(hi));
+        put(d + k, -2.0f * __half2float(hi));
+        put(2 * d + k, -2.0f * __half2float(lo));
     }
-    __nv_bfloat16 qh = __float2bfloat16_rn(q);
-    put(3 * d, __bfloat162float(qh));
-    put(3 * d + 1, q - __bfloat162float(qh));
+    const float qs = q * (1.0f / Q_COLUMN);
+    const __half qh = __float2half_rn(qs);
+    put(3 * d, __half2float(qh));
+    put(3 * d + 1, qs - __half2float(qh));
 }
 
 // ---------------------------------------------------------------------------------------------------------------------
@@ -235,7 +273,7 @@ struct TcArgs {
     int kpad;
     int utiles;
     float alpha, beta;
-    size_t off_a, off_x, off_cand, off_part, off_res, off_center, off_bar, a_stride, x_stride;
+    size_t off_a, off_x, off_mask, off_sum, off_flag, off_rlist, off_part, off_center, off_bar, a_stride, x_stride;
     uint32_t b_bytes;
 };
 
@@ -253,6 +291,42 @@ __device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, cons
         t = w.w - xr[4 * k4 + 3]; acc = fmaf(t, t, acc);
     }
     return acc;
+}
+
+// Bit 31-i set when v[i] - thr_up < 0, i.e. v[i] < thr_up (false for NaN): a subtraction and a shift-or per value.
+__device__ __forceinline__ uint32_t sign_mask32(const uint32_t (&v)[32], float thr_up) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) m = (m << 1) | (__float_as_uint(__fsub_rn(__uint_as_float(v[i]), thr_up)) >> 31);
+    return m;
+}
+
+// NQ candidates at once (every row's loads issued before any chain): the same chain as cand_dist32v.
+template <int DT, int NQ>
+__device__ __forceinline__ void cand_dist32_multi(const float* __restrict__ w, const int32_t (&jj)[NQ],
+                                                  const float (&xr)[DT], float (&dd)[NQ]) {
+    float4 r[NQ][DT / 4];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i)
+#pragma unroll
+        for (int k4 = 0; k4 < DT / 4; ++k4) r[i][k4] = __ldg((const float4*)(w + (int64_t)jj[i] * DT) + k4);
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int k4 = 0; k4 < DT / 4; ++k4) {
+            float t = r[i][k4].x - xr[4 * k4]; acc = fmaf(t, t, acc);
+            t = r[i][k4].y - xr[4 * k4 + 1]; acc = fmaf(t, t, acc);
+            t = r[i][k4].z - xr[4 * k4 + 2]; acc = fmaf(t, t, acc);
+            t = r[i][k4].w - xr[4 * k4 + 3]; acc = fmaf(t, t, acc);
+        }
+        dd[i] = acc;
+    }
+}
+
+// (da, ja) ranks before (db, jb): lexicographic, empty entries (unit < 0) last
+__device__ __forceinline__ bool lex_before(float da, int32_t ja, float db, int32_t jb) {
+    return ja >= 0 && (jb < 0 || da < db || (da == db && ja < jb));
 }
 
 // Reference distance (float64 sum of float32 squares) as an exact float32 pair; used for d1 of QE.
@@ -279,19 +353,23 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
-    int32_t* sCand = (int32_t*)(smem + P.off_cand);   // [CAPR][TM]: candidate units of each row
-    float2* sPart = (float2*)(smem + P.off_part);     // [slice][TM]: (m1, m2) of the slice
-    float* sCandD = (float*)(smem + P.off_res);       // [CAPR][TM]: float32 distance of each candidate
-    int* sCandN = (int*)(smem + P.off_res + (size_t)CAPR * TM * 4);   // [TM]: candidates claimed by the row
+    uint32_t* sMask = (uint32_t*)(smem + P.off_mask);   // [half][u][4][TM]: bit 31-i of word w: column 32w+i is a candidate
+    uint32_t* sSum = (uint32_t*)(smem + P.off_sum);     // [half][TM]: bit 4u+w set when mask word (u, w) is non-zero
+    uint8_t* sFlag = smem + P.off_flag;                 // [TM]: the row goes to the exact recheck
+    uint16_t* sList = (uint16_t*)(smem + P.off_rlist);  // [CAPR + 1][TM]: the resolvers' candidate lists (+ scratch)
+    float2* sPart = (float2*)(smem + P.off_part);       // [buf][half][TM]: (m1, m2) of the half
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
-    uint64_t* x_full = bars + 1;    // [3]
-    uint64_t* x_empty = bars + 4;   // [3]
+    uint64_t* x_full = bars + 1;    // [XSTAGES]
+    uint64_t* x_empty = bars + 4;   // [XSTAGES]
     uint64_t* a_full = bars + 7;    // [2]
     uint64_t* a_empty = bars + 9;   // [2]
     uint64_t* t_full = bars + 11;   // [2]
     uint64_t* t_empty = bars + 13;  // [2]
-    uint64_t* drain = bars + 15;
+    uint64_t* m_full = bars + 15;   // the sweeps have written the candidate masks of a row tile
+    uint64_t* m_empty = bars + 16;  // the resolvers have read them
+    uint64_t* drain = bars + 19;
+    uint64_t* p_full = bars + 20;   // [2][4]: both halves of a lane quarter have published (m1, m2)
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_s;
 
@@ -307,19 +385,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         ptx::mbar_init(b_full, 1);
         for (int s = 0; s < XSTAGES; ++s) {
             ptx::mbar_init(x_full + s, 1);
-            ptx::mbar_init(x_empty + s, EPI_WARPS);
+            ptx::mbar_init(x_empty + s, SWEEP_WARPS);
         }
         for (int s = 0; s < 2; ++s) {
-            ptx::mbar_init(a_full + s, EPI_WARPS);
+            ptx::mbar_init(a_full + s, SWEEP_WARPS);
             ptx::mbar_init(a_empty + s, 1);
             ptx::mbar_init(t_full + s, 1);
-            ptx::mbar_init(t_empty + s, EPI_WARPS);
+            ptx::mbar_init(t_empty + s, SWEEP_WARPS);
+            for (int qq = 0; qq < 4; ++qq) ptx::mbar_init(p_full + s * 4 + qq, HALVES);
         }
+        ptx::mbar_init(m_full, SWEEP_WARPS);
+        ptx::mbar_init(m_empty, RES_WARPS);
         ptx::mbar_init(drain, 1);
         ptx::fence_mbar_init();
         abort_s = 0;
     }
-    for (int k = tid; k < d; k += NUM_THREADS) sCenter[k] = P.center[k];
+    for (int k = tid; k <= d; k += NUM_THREADS) sCenter[k] = P.center[k];   // centre and scale
     if (warp == MMA_WARP) {
         ptx::tmem_alloc(&tmem_base_s, 512);
         ptx::tmem_relinquish();
@@ -334,6 +415,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         atomicOr(&g_tc_status, code);
         *abort_v = 1;
     };
+#ifdef SOMGB_TC_PHASE_TIMING
+    unsigned long long _tc_acc[TC_PHASES] = {};
+    long long _tc_t0 = 0;
+#endif
 
     if (warp == TMA_WARP) {
         if (lane == 0 && n_my > 0) {
@@ -388,7 +473,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         for (int kb = 0; kb < kpad / 16; ++kb) {
                             const uint64_t ad = ptx::smem_desc(a_addr + kb * 256, 128, sbo);
                             const uint64_t bd = ptx::smem_desc(bu + kb * 256, 128, sbo);
-                            ptx::mma_bf16(dt, ad, bd, IDESC, kb > 0);
+                            ptx::mma_f16(dt, ad, bd, IDESC, kb > 0);
                         }
                         ptx::mma_commit(t_full + buf);
                     }
@@ -399,275 +484,310 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             ptx::mma_commit(drain);
             if (!ptx::mbar_wait(drain, 0)) fail(256u);
         }
-    } else {
-        // ------------------------------ converter + epilogue (warps 0..15) -----------------------------------------
-        // warp e: TMEM lane quarter q = e & 3 (rows 32q..32q+31), column slice sl = e >> 2 (64 of each 256 columns)
-        const int q = warp & 3, sl = warp >> 2;
+    } else if (warp < SWEEP_WARPS) {
+        // ------------------------------ converter + sweeps (warps 0..7) ---------------------------------------------
+        // warp e: TMEM lane quarter q = e & 3 (rows 32q..32q+31), column half h = e >> 2 (128 of each 256 columns)
+        const int q = warp & 3, h = warp >> 2;
         const int row = q * 32 + lane;
         const uint32_t lane_base = (uint32_t)(q * 32) << 16;
-        const float g32 = (float)(d + 2) * 5.9604645e-8f;
-        const float fac = 1.0f + 8.0f * g32;
-        DFAcc e0, e1, e2;
-        int64_t gcons = 0;   // TMEM tiles consumed
-#ifdef SOMGB_TC_PHASE_TIMING
-        unsigned long long _tc_acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        long long _tc_t0 = 0;
-#endif
 
-        auto qbar = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(1 + q) : "memory"); };
-
-        // centred split-BF16 A row of `row`: this thread writes the 16-byte chunks kc = sl, sl + 4, ... of kpad / 8;
-        // returns |x'|^2 (infinite when a feature is not finite)
+        // centred, scaled split-FP16 A row of `row`: this thread writes the 16-byte chunks kc = h, h + 2, ... of
+        // kpad / 8; returns |x'|^2 (infinite when a coordinate is not finite or outside the FP16 split's range)
         auto convert = [&](int64_t it, float& xn_out) -> bool {
             const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
             if (it >= 2 && !ptx::mbar_wait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
             if (!ptx::mbar_wait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
             const float4* xs4 = (const float4*)(smem + P.off_x + s3 * P.x_stride) + row * (DT / 4);
+            const float scale = sCenter[DT];
             float xp[DT];
             bool finite = true;
             float xn = 0.0f;
 #pragma unroll
             for (int k4 = 0; k4 < DT / 4; ++k4) {
                 const float4 v = xs4[k4];
-                xp[4 * k4 + 0] = v.x - sCenter[4 * k4 + 0];
-                xp[4 * k4 + 1] = v.y - sCenter[4 * k4 + 1];
-                xp[4 * k4 + 2] = v.z - sCenter[4 * k4 + 2];
-                xp[4 * k4 + 3] = v.w - sCenter[4 * k4 + 3];
+                xp[4 * k4 + 0] = (v.x - sCenter[4 * k4 + 0]) * scale;
+                xp[4 * k4 + 1] = (v.y - sCenter[4 * k4 + 1]) * scale;
+                xp[4 * k4 + 2] = (v.z - sCenter[4 * k4 + 2]) * scale;
+                xp[4 * k4 + 3] = (v.w - sCenter[4 * k4 + 3]) * scale;
             }
 #pragma unroll
             for (int k = 0; k < DT; ++k) {
-                finite = finite && isfinite(xp[k]);
+                finite = finite && fabsf(xp[k]) < X_LIMIT;   // false for inf and NaN as well
                 xn = fmaf(xp[k], xp[k], xn);
             }
-            finite = finite && (xn < HUGE_S);
             xn_out = finite ? xn : INFINITY;
             uint8_t* at = smem + P.off_a + s2 * P.a_stride;
+            // chunks kc = H, H + HALVES, ... with H the warp's half as a compile-time constant (one branch per call)
+            auto write_chunks = [&](auto hc) {
+                constexpr int H = decltype(hc)::value;
 #pragma unroll
-            for (int kc = 0; kc < kpad / 8; ++kc) {
-                if (kc % SLICES != sl) continue;
-                __align__(16) __nv_bfloat16 v[8];
+                for (int kc = H; kc < kpad / 8; kc += HALVES) {
+                    __align__(16) __half v[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int k = kc * 8 + i;
-                    float val = 0.0f;
-                    if (k < 3 * DT) {
-                        const float t = xp[k % DT];
-                        const float hi = __bfloat162float(__float2bfloat16_rn(t));
-                        val = (k >= DT && k < 2 * DT) ? t - hi : hi;
-                    } else if (k == 3 * DT || k == 3 * DT + 1) {
-                        val = 1.0f;
+                    for (int i = 0; i < 8; ++i) {
+                        const int k = kc * 8 + i;
+                        float val = 0.0f;
+                        if (k < 3 * DT) {
+                            const float t = xp[k % DT];
+                            const float hi = __half2float(__float2half_rn(t));
+                            val = (k >= DT && k < 2 * DT) ? t - hi : hi;
+                        } else if (k == 3 * DT || k == 3 * DT + 1) {
+                            val = Q_COLUMN;
+                        }
+                        v[i] = __float2half_rn(finite ? val : 0.0f);
                     }
-                    v[i] = __float2bfloat16_rn(finite ? val : 0.0f);
+                    *(uint4*)(at + canon_off(row, kc * 8, kpad)) = *(const uint4*)v;
                 }
-                *(uint4*)(at + canon_off(row, kc * 8, kpad)) = *(const uint4*)v;
-            }
+            };
+            if (h == 0) write_chunks(std::integral_constant<int, 0>{});
+            else write_chunks(std::integral_constant<int, 1>{});
             ptx::fence_proxy_async();
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(a_full + s2);
+            if (lane == 0) {
+                ptx::mbar_arrive(a_full + s2);
+                ptx::mbar_arrive(x_empty + s3);   // the sample tile is no longer read from shared memory
+            }
             return true;
         };
 
-        // two 32-column chunks of this warp's slice of TMEM tile `buf`, loaded back to back
-        auto load64 = [&](int buf, float (&v0)[32], float (&v1)[32]) {
-            const uint32_t base = tbase + lane_base + (uint32_t)(buf * TN + sl * 64);
-            uint32_t r0[32], r1[32];
-            ptx::tmem_ld32_raw(base, r0);
-            ptx::tmem_ld32_raw(base + 32, r1);
-            ptx::tmem_wait_ld2(r0, r1);
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                v0[i] = __uint_as_float(r0[i]);
-                v1[i] = __uint_as_float(r1[i]);
-            }
+        // the warp's last read of TMEM tile `buf` is complete: hand the accumulator back to the MMA issuer
+        auto release = [&](int buf) {
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(t_empty + buf);
         };
 
+        // This warp's 128 columns of TMEM tile `buf` in four 32-column chunks, software-pipelined: chunk c + 1 is
+        // loading while chunk c is processed (tcgen05.wait::ld waits for every load issued before it, so one load is
+        // in flight at a time). The accumulator is handed back as soon as the last load has landed.
+        auto stream_tile = [&](int buf, auto&& process) {
+            const uint32_t base = tbase + lane_base + (uint32_t)(buf * TN + h * 128);
+            uint32_t ra[32], rb[32];
+            ptx::tmem_ld32_raw(base, ra);
+            ptx::tmem_wait_ld1(ra);
+            ptx::tmem_ld32_raw(base + 32, rb);
+            process(0, ra);
+            ptx::tmem_wait_ld1(rb);
+            ptx::tmem_ld32_raw(base + 64, ra);
+            process(1, rb);
+            ptx::tmem_wait_ld1(ra);
+            ptx::tmem_ld32_raw(base + 96, rb);
+            process(2, ra);
+            ptx::tmem_wait_ld1(rb);
+            release(buf);
+            process(3, rb);
+        };
+
+        int64_t gcons = 0;   // TMEM tiles consumed
         float xn_next = 0.0f;
         bool ok = n_my > 0 ? convert(0, xn_next) : true;
         for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
             const float xn = xn_next;
+            const int cb = (int)(it & 1);
             TC_T0();
             if (it + 1 < n_my && !(ok = convert(it + 1, xn_next))) break;
             TC_T(4);
-            const int s3 = (int)(it % XSTAGES);
-            const int64_t tile = blockIdx.x + it * gridDim.x;
-            const int64_t grow = tile * TM + row;
-            const bool live = grow < a.n;
-            const float* xs = (const float*)(smem + P.off_x + s3 * P.x_stride) + row * d;
             bool flagged = !(xn < HUGE_S);
 
-            // ---- sweep 1: best (and second best) s~ of the row over this warp's columns -------------------------
+            // ---- sweep 1: smallest (and second-smallest 8-unit group minimum of) s~ over this warp's columns -----
             float a1 = INFINITY, a2 = INFINITY, b1 = INFINITY, b2 = INFINITY;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
                 TC_T(0);
                 ptx::tc_fence_after();
-                float v0[32], v1[32];
-                load64(buf, v0, v1);
-                ptx::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(t_empty + buf);
+                // groups of 8 columns: chunks 0 and 2 feed (a1, a2), chunks 1 and 3 feed (b1, b2)
+                stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
 #pragma unroll
-                for (int g8 = 0; g8 < 32; g8 += 8) {
-                    const float ga = fminf(fminf(fminf(v0[g8], v0[g8 + 1]), fminf(v0[g8 + 2], v0[g8 + 3])),
-                                           fminf(fminf(v0[g8 + 4], v0[g8 + 5]), fminf(v0[g8 + 6], v0[g8 + 7])));
-                    const float gb = fminf(fminf(fminf(v1[g8], v1[g8 + 1]), fminf(v1[g8 + 2], v1[g8 + 3])),
-                                           fminf(fminf(v1[g8 + 4], v1[g8 + 5]), fminf(v1[g8 + 6], v1[g8 + 7])));
-                    if (ERR) {
-                        a2 = fminf(a2, fmaxf(a1, ga));
-                        a1 = fminf(a1, ga);
-                        b2 = fminf(b2, fmaxf(b1, gb));
-                        b1 = fminf(b1, gb);
-                    } else {
-                        a1 = fminf(a1, ga);
-                        b1 = fminf(b1, gb);
+                    for (int g8 = 0; g8 < 32; g8 += 8) {
+                        const float g = fminf(
+                            fminf(fminf(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1])),
+                                  fminf(__uint_as_float(r[g8 + 2]), __uint_as_float(r[g8 + 3]))),
+                            fminf(fminf(__uint_as_float(r[g8 + 4]), __uint_as_float(r[g8 + 5])),
+                                  fminf(__uint_as_float(r[g8 + 6]), __uint_as_float(r[g8 + 7]))));
+                        if (c & 1) {
+                            if (ERR) b2 = fminf(b2, fmaxf(b1, g));
+                            b1 = fminf(b1, g);
+                        } else {
+                            if (ERR) a2 = fminf(a2, fmaxf(a1, g));
+                            a1 = fminf(a1, g);
+                        }
                     }
-                }
+                });
                 TC_T(1);
             }
             if (!ok) break;
-            {
-                const float m1 = fminf(a1, b1);
-                const float m2 = fminf(fmaxf(a1, b1), fminf(a2, b2));
-                sPart[sl * TM + row] = make_float2(m1, m2);
-            }
-            qbar();
-            TC_T(5);
+            sPart[(cb * HALVES + h) * TM + row] =
+                make_float2(fminf(a1, b1), fminf(fmaxf(a1, b1), fminf(a2, b2)));
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(p_full + cb * 4 + q);
+            if (!ptx::mbar_wait(p_full + cb * 4 + q, (uint32_t)((it >> 1) & 1))) { fail(2048u); break; }
             float M1 = INFINITY, M2 = INFINITY;
 #pragma unroll
-            for (int t = 0; t < SLICES; ++t) {
-                const float2 p = sPart[t * TM + row];
+            for (int t = 0; t < HALVES; ++t) {
+                const float2 p = sPart[(cb * HALVES + t) * TM + row];
                 M2 = fminf(fminf(M2, p.y), fmaxf(M1, p.x));
                 M1 = fminf(M1, p.x);
             }
             // ERR: M2 is the second smallest 8-unit group minimum, an upper bound of the second smallest s~ (two
             // groups have a unit at or below it), so the threshold derived from it keeps every possible second BMU
             const float mref = ERR ? M2 : M1;
-            // every slice has read sPart; the previous row tile's resolution finished before this tile's qbar
-            if (sl == 0) sCandN[row] = 0;
             if (!(M1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
             const float dref = fmaxf(0.0f, mref + xn);
-            const float thr = flagged ? -INFINITY
-                                      : mref + 2.0f * (P.alpha * xn + P.beta * dref) / (1.0f - P.beta) + 1.0e-30f;
-
-            qbar();   // the pool count is reset before any slice claims a slot
+            const float thr =
+                flagged ? -INFINITY : mref + 2.0f * (P.alpha * xn + P.beta * dref + GAMMA) / (1.0f - P.beta) + GAMMA;
+            // the resolvers have taken the candidate masks of the previous row tile
+            if (it >= 1 && !ptx::mbar_wait(m_empty, (uint32_t)((it - 1) & 1))) { fail(512u); break; }
             TC_T(5);
-            // ---- sweep 2: every unit of this warp's columns under the threshold --------------------------------
 
+            // ---- sweep 2: mask of this warp's columns at or under the threshold -------------------------------------
+            // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
+            // floats never rounds to zero), so each value costs one subtraction and one shift-or of its sign bit.
+            const float thr_up = nextafterf(thr, INFINITY);
+            uint32_t summary = 0;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
                 TC_T(2);
                 ptx::tc_fence_after();
-                float v0[32], v1[32];
-                load64(buf, v0, v1);
-                ptx::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(t_empty + buf);
-                const int jb = u * TN + sl * 64;
-#pragma unroll
-                for (int half = 0; half < 2; ++half) {
-                    const float* v = half ? v1 : v0;
-#pragma unroll
-                    for (int g4 = 0; g4 < 32; g4 += 4) {
-                        const float gm = fminf(fminf(v[g4], v[g4 + 1]), fminf(v[g4 + 2], v[g4 + 3]));
-                        if (__any_sync(0xffffffffu, gm <= thr)) {
-#pragma unroll
-                            for (int i = 0; i < 4; ++i) {
-                                const int j = jb + half * 32 + g4 + i;
-                                if (v[g4 + i] <= thr && j < (int)a.m) {
-                                    const int slot = atomicAdd(sCandN + row, 1);
-                                    if (slot < CAPR) sCand[slot * TM + row] = j;
-                                }
-                            }
-                        }
-                    }
-                }
+                uint32_t* mrow = sMask + (size_t)((h * U + u) * 4) * TM + row;
+                stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                    const uint32_t mw = sign_mask32(r, thr_up);
+                    mrow[c * TM] = mw;
+                    summary |= (mw != 0u ? 1u : 0u) << (u * 4 + c);
+                });
                 TC_T(3);
             }
             if (!ok) break;
-
-            // ---- resolution: float32 distances of the row's candidates (slot k by slice k % 4), then slice 0 decides
-            qbar();
-            TC_T(5);
-            const int total = sCandN[row];
-            if (live && !flagged && total <= CAPR) {
-                float xr[DT];
-                const float4* xs4 = (const float4*)xs;
-#pragma unroll
-                for (int k4 = 0; k4 < DT / 4; ++k4) {
-                    const float4 t = xs4[k4];
-                    xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
-                }
-                for (int k = sl; k < total; k += SLICES) {
-                    const int32_t j = sCand[k * TM + row];
-                    sCandD[k * TM + row] = cand_dist32v<DT>(a.w + (int64_t)j * DT, xr);
-                }
-            }
+            sSum[h * TM + row] = flagged ? 0u : summary;
+            if (h == 0) sFlag[row] = flagged ? 1 : 0;
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(m_full);
+        }
+    } else if (warp < SWEEP_WARPS + RES_WARPS) {
+        // ------------------------------ resolvers (warps 8..11): row tile it while the sweeps run it + 1 -------------
+        // thread r of resolver warp q owns row 32q + r: float32 distances of its candidates, the decision, the outputs
+        const int q = warp - SWEEP_WARPS;
+        const int row = q * 32 + lane;
+        const float g32 = (float)(d + 2) * 5.9604645e-8f;
+        const float fac = 1.0f + 8.0f * g32;
+        DFAcc e0, e1, e2;
+        uint16_t* list = sList + row;
+        for (int64_t it = 0; it < n_my && !*abort_v; ++it) {
+            TC_T0();
+            if (!ptx::mbar_wait(m_full, (uint32_t)(it & 1))) { fail(1024u); break; }
             TC_T(6);
-            qbar();
-            TC_T(5);
-            if (sl == 0 && live) {
-                // best two candidates in (float32 distance, unit) order
-                float f1 = INFINITY, f2 = INFINITY;
-                int32_t c1 = -1, c2 = -1;
-                const bool overflow = total > CAPR;
-                const int nlist = overflow ? 0 : total;
-                for (int k = 0; k < nlist; ++k) {
-                    const float df = sCandD[k * TM + row];
-                    const int32_t j = sCand[k * TM + row];
-                    if (df < f1 || (df == f1 && j < c1)) { f2 = f1; c2 = c1; f1 = df; c1 = j; }
-                    else if (df < f2 || (df == f2 && j < c2)) { f2 = df; c2 = j; }
-                }
-                if (flagged || overflow || total == 0) {
-                    const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
-                    P.rows[slotq] = (int32_t)grow;
-                } else {
-                    // contenders: candidates the float32 distances cannot separate from the best (second best)
-                    const float lim = ERR ? f2 : f1;
-                    const float climit = lim < 1.0e37f ? fmaf(lim, fac, 1.0e-37f) : INFINITY;
-                    int ncont = 0;
-                    for (int k = 0; k < nlist; ++k) ncont += sCandD[k * TM + row] <= climit;
-                    int32_t r1, r2;
-                    DFloat rd1{0.0f, 0.0f};
-                    if (ncont <= (ERR ? 2 : 1)) {
-                        r1 = c1;
-                        r2 = ERR ? c2 : -1;
-                        if (ERR && c1 >= 0) {
-                            float xr[DT];
-                            const float4* xs4 = (const float4*)xs;
-#pragma unroll
-                            for (int k4 = 0; k4 < DT / 4; ++k4) {
-                                const float4 t = xs4[k4];
-                                xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
-                            }
-                            rd1 = ref_dist_pair<DT>(a.w + (int64_t)c1 * DT, xr);
-                        }
-                    } else {
-                        // float64 reference sums of every contender, ranked in (distance, unit) order
-                        Top2Lex tt;
-                        tt.init();
-                        for (int k = 0; k < nlist; ++k) {
-                            if (!(sCandD[k * TM + row] <= climit)) continue;
-                            const int32_t j = sCand[k * TM + row];
-                            tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
-                        }
-                        r1 = tt.i1;
-                        r2 = ERR ? tt.i2 : -1;
-                        rd1.hi = (float)tt.d1;
-                        rd1.lo = (float)(tt.d1 - (double)rd1.hi);
-                    }
-                    emit_sample32(a, grow, r1, r2, rd1, e0, e1, e2);
-                }
+            const int64_t grow = (blockIdx.x + it * gridDim.x) * TM + row;
+            const bool live = grow < a.n;
+            const double rho_v = (live && a.rho) ? __ldg(a.rho + grow) : 1.0;   // issued early, used at the end
+            // the sample row from global memory (just read by the tile load, so in L2): the shared-memory stage is
+            // released by the converters, which decouples the resolvers from the sample-tile ring
+            const float* xg = a.x + (live ? grow : 0) * DT;
+            // candidate list of the row from the two halves' masks: one candidate per lane and iteration, the next
+            // non-zero mask word (from the summary bits) fetched in the same iteration; no divergent branches
+            const bool flagged = sFlag[row] != 0;
+            uint64_t S = flagged ? 0ull : ((uint64_t)sSum[row] | ((uint64_t)sSum[TM + row] << 32));
+            uint32_t word = 0;
+            int jtop = 0, cnt = 0;
+            bool more = S != 0ull;
+            while (__any_sync(0xffffffffu, more)) {
+                const bool need = word == 0u;
+                const int b = __ffsll((long long)S) - 1;
+                const int bb = b < 0 ? 0 : b;
+                const int hh = bb >> 5, ub = (bb & 31) >> 2, wb = bb & 3;
+                const uint32_t nw = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
+                word = need ? (b >= 0 ? nw : 0u) : word;
+                jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
+                S = need ? (S & (S - 1ull)) : S;
+                const int j = jtop - (__ffs(word) - 1);
+                const bool take = word != 0u && j < (int)a.m;
+                word &= word - 1u;
+                list[(take && cnt < CAPR ? cnt : CAPR) * TM] = (uint16_t)j;
+                cnt += take ? 1 : 0;
+                more = word != 0u || S != 0ull;
             }
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(x_empty + s3);
+            if (lane == 0) ptx::mbar_arrive(m_empty);
+            TC_T(9);
+            if (live && (flagged || cnt == 0 || cnt > CAPR)) {
+                const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
+                P.rows[slotq] = (int32_t)grow;
+            } else if (live) {
+                float xr[DT];
+#pragma unroll
+                for (int k4 = 0; k4 < DT / 4; ++k4) {
+                    const float4 t = __ldg((const float4*)xg + k4);
+                    xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
+                }
+                // float32 top-3 of the candidates in (distance, unit) order, NQ candidates' loads in flight at once
+                // (with their topographic coordinates, which the error sums need for the best two)
+                float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
+                int32_t j1 = -1, j2 = -1, j3 = -1;
+                float2 t1 = make_float2(0.0f, 0.0f), t2 = t1, t3 = t1;
+                auto push = [&](float df, int32_t j, float2 tj) {
+                    if (!lex_before(df, j, f3, j3)) return;
+                    if (lex_before(df, j, f2, j2)) {
+                        f3 = f2; j3 = j2; t3 = t2;
+                        if (lex_before(df, j, f1, j1)) { f2 = f1; j2 = j1; t2 = t1; f1 = df; j1 = j; t1 = tj; }
+                        else { f2 = df; j2 = j; t2 = tj; }
+                    } else { f3 = df; j3 = j; t3 = tj; }
+                };
+                constexpr int NQ = DT <= 16 ? 4 : 2;
+                const float2* topo2 = (const float2*)a.topo;
+                for (int k = 0; k < cnt; k += NQ) {
+                    int32_t jj[NQ];
+#pragma unroll
+                    for (int i = 0; i < NQ; ++i) jj[i] = list[(k + i < cnt ? k + i : k) * TM];
+                    float2 tt[NQ];
+#pragma unroll
+                    for (int i = 0; i < NQ; ++i) tt[i] = ERR ? __ldg(topo2 + jj[i]) : make_float2(0.0f, 0.0f);
+                    float dd[NQ];
+                    cand_dist32_multi<DT, NQ>(a.w, jj, xr, dd);
+#pragma unroll
+                    for (int i = 0; i < NQ; ++i)
+                        if (k + i < cnt) push(dd[i], jj[i], tt[i]);
+                }
+                TC_T(8);
+                // The float32 ranking decides when every rank that matters is separated by more than the float32
+                // rounding bound: best vs second (both modes) and, for the error sums, second vs third. Otherwise the
+                // contenders, the candidates within that bound of the best (second best), are ranked by the
+                // reference's float64 sums.
+                const float c1lim = f1 < 1.0e37f ? fmaf(f1, fac, 1.0e-37f) : INFINITY;
+                const float c2lim = f2 < 1.0e37f ? fmaf(f2, fac, 1.0e-37f) : INFINITY;
+                const bool gap12 = j2 < 0 || !(f2 <= c1lim);
+                const bool separated = ERR ? (gap12 && (j3 < 0 || !(f3 <= c2lim))) : gap12;
+                const float climit = ERR ? c2lim : c1lim;
+                int32_t r1, r2;
+                float2 tr1 = t1, tr2 = t2;
+                DFloat rd1{0.0f, 0.0f};
+                if (separated) {
+                    r1 = j1;
+                    r2 = ERR ? j2 : -1;
+                    if (ERR && j1 >= 0) rd1 = ref_dist_pair<DT>(a.w + (int64_t)j1 * DT, xr);
+                } else {
+                    // float64 reference sums of every contender, ranked in (distance, unit) order
+                    const float* xs = xg;
+                    Top2Lex tt;
+                    tt.init();
+                    for (int k = 0; k < cnt; ++k) {
+                        const int32_t j = list[k * TM];
+                        if (!(cand_dist32v<DT>(a.w + (int64_t)j * DT, xr) <= climit)) continue;
+                        tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
+                    }
+                    r1 = tt.i1;
+                    r2 = ERR ? tt.i2 : -1;
+                    rd1.hi = (float)tt.d1;
+                    rd1.lo = (float)(tt.d1 - (double)rd1.hi);
+                    if (ERR && r1 >= 0 && r2 >= 0) {
+                        tr1 = topo2[r1];
+                        tr2 = topo2[r2];
+                    }
+                }
+                TC_T(10);
+                emit_sample32(a, grow, rho_v, r1, r2, rd1, tr1, tr2, e0, e1, e2);
+            }
             TC_T(7);
         }
-#ifdef SOMGB_TC_PHASE_TIMING
-        if (lane == 0)
-            for (int ph = 0; ph < 8; ++ph) atomicAdd(&g_tc_phase_cycles[ph], _tc_acc[ph]);
-#endif
         if (ERR) {
             double v0 = e0.value(), v1 = e1.value(), v2 = e2.value();
             for (int o = 16; o > 0; o >>= 1) {
@@ -682,6 +802,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             }
         }
     }
+#ifdef SOMGB_TC_PHASE_TIMING
+    if (lane == 0 && warp < SWEEP_WARPS + RES_WARPS)
+        for (int ph = 0; ph < TC_PHASES; ++ph) atomicAdd(&g_tc_phase_cycles[ph], _tc_acc[ph]);
+#endif
 
     // teardown: the MMA thread has drained its MMAs and, after an abort, the producer its copies (both bounded)
     ptx::tc_fence_before();
@@ -741,7 +865,7 @@ size_t max_smem_optin() {
 
 bool tc_shape_ok(int64_t m, int d) {
     if (d != 4 && d != 8 && d != 16 && d != 32) return false;
-    if (m <= 0 || m > (int64_t)1 << 24) return false;
+    if (m <= 0 || m > (int64_t)MAX_U * TN) return false;   // the per-half candidate summary covers MAX_U column tiles
     return tc_shape(m, d).smem <= 227 * 1024;
 }
 
@@ -760,9 +884,9 @@ bool tc_supported(int64_t n, int64_t m, int d, int algo) {
 // Instrumented builds only: copies out (and optionally clears) the eight phase counters.
 extern "C" int somgb_tc_phase_cycles(unsigned long long* out8, int reset) {
     SOMGB_CUDA_TRY(cudaDeviceSynchronize());
-    SOMGB_CUDA_TRY(cudaMemcpyFromSymbol(out8, g_tc_phase_cycles, 8 * sizeof(unsigned long long)));
+    SOMGB_CUDA_TRY(cudaMemcpyFromSymbol(out8, g_tc_phase_cycles, TC_PHASES * sizeof(unsigned long long)));
     if (reset) {
-        unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        unsigned long long z[TC_PHASES] = {};
         SOMGB_CUDA_TRY(cudaMemcpyToSymbol(g_tc_phase_cycles, z, sizeof(z)));
     }
     return SOMGB_OK;
@@ -784,7 +908,8 @@ int read_device_status(unsigned int* status, bool clear, cudaStream_t stream) {
 size_t tc_workspace_bytes(int64_t n, int64_t m, int d) { return tc_ws_layout(n, m, d, nullptr, nullptr); }
 
 int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t stream) {
-    if (((uintptr_t)a.x) % 16) return set_error(SOMGB_ERR_INVALID, "tensor-core pass needs 16-byte aligned x");
+    if (((uintptr_t)a.x) % 16 || ((uintptr_t)a.w) % 16 || ((a.outs & OUT_ERR) && ((uintptr_t)a.topo) % 8))
+        return set_error(SOMGB_ERR_INVALID, "tensor-core pass needs 16-byte aligned x and w, 8-byte aligned topo");
     const TcShape s = tc_shape(a.m, a.d);
     TcWs W;
     if (tc_ws_layout(a.n, a.m, a.d, &W, ws) > ws_bytes) return set_error(SOMGB_ERR_WORKSPACE, "tc workspace too small");
@@ -818,9 +943,11 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     tc_error_coefficients(a.d, &P.alpha, &P.beta);
     P.off_a = s.off_a;
     P.off_x = s.off_x;
-    P.off_cand = s.off_cand;
+    P.off_mask = s.off_mask;
+    P.off_sum = s.off_sum;
+    P.off_flag = s.off_flag;
+    P.off_rlist = s.off_rlist;
     P.off_part = s.off_part;
-    P.off_res = s.off_res;
     P.off_center = s.off_center;
     P.off_bar = s.off_bar;
     P.a_stride = align_up(s.a_bytes, 1024);

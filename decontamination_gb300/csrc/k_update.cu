@@ -350,8 +350,9 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
         return SOMGB_OK;
     }
     if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "fixed-point segmented sums support D <= 64");
-    // three int32 limbs per bin; up to ~200 KB of bins per CTA
-    const size_t budget = 200 * 1024;
+    // three int32 limbs per bin; up to ~220 KB of bins per CTA, so that a 32x32 map with D = 16 (17 bins a unit) fits
+    // one CTA and every sample is read once
+    const size_t budget = 220 * 1024;
     const int64_t per_unit = (int64_t)(d + 1) * 12;
     int64_t upr = std::max<int64_t>(1, (int64_t)(budget / per_unit));
     upr = std::min(upr, m);

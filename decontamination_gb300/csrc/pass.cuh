@@ -102,33 +102,31 @@ __device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
 }
 
 // Is the reference's float64 sum of the float32 squares of the float32 topographic differences above `penalty`
-// (exactly representable)? The two squares are summed exactly in float32 pairs.
-__device__ __forceinline__ bool topo_far32(const float* __restrict__ topo, int64_t a, int64_t b, float penalty) {
-    const float t0 = __fsub_rn(topo[2 * a], topo[2 * b]);
-    const float t1 = __fsub_rn(topo[2 * a + 1], topo[2 * b + 1]);
+// (exactly representable)? The two squares are summed exactly in float32 pairs. ta, tb: the two units' coordinates.
+__device__ __forceinline__ bool topo_far32(float2 ta, float2 tb, float penalty) {
+    const float t0 = __fsub_rn(ta.x, tb.x);
+    const float t1 = __fsub_rn(ta.y, tb.y);
     const DFloat s = two_sum(__fmul_rn(t0, t0), __fmul_rn(t1, t1));
     return s.hi > penalty || (s.hi == penalty && s.lo > 0.0f);
 }
 
-// Per-sample outputs from float32 quantities; d1 is the reference distance of b1 as a double-float.
-__device__ __forceinline__ void emit_sample32(const PassArgs& a, int64_t i, int32_t i1, int32_t i2, DFloat d1,
-                                              DFAcc& e0, DFAcc& e1, DFAcc& e2) {
+// Per-sample outputs from float32 quantities; d1 is the reference distance of b1 as a double-float, r the sample's
+// weight (a.rho[i], or 1 when a.rho is NULL) and t1, t2 the topographic coordinates of b1 and b2, all loaded by the
+// caller.
+__device__ __forceinline__ void emit_sample32(const PassArgs& a, int64_t i, double r, int32_t i1, int32_t i2, DFloat d1,
+                                              float2 t1, float2 t2, DFAcc& e0, DFAcc& e1, DFAcc& e2) {
     const int outs = a.outs;
-    DFloat rho{1.0f, 0.0f};
-    bool pos = true;
-    if (a.rho) {
-        const double r = a.rho[i];
-        const long long bits = __double_as_longlong(r);
-        pos = bits > 0 && bits <= 0x7FF0000000000000LL;   // r > 0 (NaN excluded)
-        rho.hi = (float)r;
-        rho.lo = (float)(r - (double)rho.hi);
-    }
+    const long long bits = __double_as_longlong(r);
+    const bool pos = bits > 0 && bits <= 0x7FF0000000000000LL;   // r > 0 (NaN excluded)
+    DFloat rho;
+    rho.hi = (float)r;
+    rho.lo = (float)(r - (double)rho.hi);
     if (outs & OUT_BMU) a.bmu_out[i] = i1 < 0 ? 0 : i1;
     if ((outs & OUT_HIST) && pos) atomicAdd(a.hist + (i1 < 0 ? 0 : i1), (double)rho.hi + (double)rho.lo);
     if (outs & OUT_TRAIN) a.train_bmu[i] = (rho.hi > 0.0f && i1 >= 0) ? i1 : -1;
     if ((outs & OUT_ERR) && pos && i1 >= 0 && i2 >= 0 && i1 != i2) {
         e0.add(df_mul(rho, df_sqrt(d1.hi, d1.lo)));
-        if (topo_far32(a.topo, i1, i2, (float)a.penalty)) e1.add(rho);
+        if (topo_far32(t1, t2, (float)a.penalty)) e1.add(rho);
         e2.add(rho);
     }
 }

@@ -94,12 +94,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
-// Instruction descriptor of kind::f16 with BF16 A and B, FP32 accumulator, both K-major, shape M x N.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t m, uint32_t n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+// Instruction descriptor of kind::f16 with FP16 A and B (format code 0 in bits 7-9 and 10-12), FP32 accumulator
+// (bits 4-5 = 1), both K-major, shape M x N (N >> 3 in bits 17-22, M >> 4 in bits 24-28).
+__host__ __device__ constexpr uint32_t idesc_f16_f32(uint32_t m, uint32_t n) {
+    return (1u << 4) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -125,6 +126,10 @@ __device__ __forceinline__ void tmem_ld32_raw(uint32_t taddr, uint32_t (&r)[32])
 __device__ __forceinline__ void tmem_wait_ld2(uint32_t (&r0)[32], uint32_t (&r1)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r0[0]), "+r"(r0[1]), "+r"(r0[2]), "+r"(r0[3]), "+r"(r0[4]), "+r"(r0[5]), "+r"(r0[6]), "+r"(r0[7]), "+r"(r0[8]), "+r"(r0[9]), "+r"(r0[10]), "+r"(r0[11]), "+r"(r0[12]), "+r"(r0[13]), "+r"(r0[14]), "+r"(r0[15]), "+r"(r0[16]), "+r"(r0[17]), "+r"(r0[18]), "+r"(r0[19]), "+r"(r0[20]), "+r"(r0[21]), "+r"(r0[22]), "+r"(r0[23]), "+r"(r0[24]), "+r"(r0[25]), "+r"(r0[26]), "+r"(r0[27]), "+r"(r0[28]), "+r"(r0[29]), "+r"(r0[30]), "+r"(r0[31])::"memory");
     asm volatile("" : "+r"(r1[0]), "+r"(r1[1]), "+r"(r1[2]), "+r"(r1[3]), "+r"(r1[4]), "+r"(r1[5]), "+r"(r1[6]), "+r"(r1[7]), "+r"(r1[8]), "+r"(r1[9]), "+r"(r1[10]), "+r"(r1[11]), "+r"(r1[12]), "+r"(r1[13]), "+r"(r1[14]), "+r"(r1[15]), "+r"(r1[16]), "+r"(r1[17]), "+r"(r1[18]), "+r"(r1[19]), "+r"(r1[20]), "+r"(r1[21]), "+r"(r1[22]), "+r"(r1[23]), "+r"(r1[24]), "+r"(r1[25]), "+r"(r1[26]), "+r"(r1[27]), "+r"(r1[28]), "+r"(r1[29]), "+r"(r1[30]), "+r"(r1[31]));
+}
+
+__device__ __forceinline__ void tmem_wait_ld1(uint32_t (&r)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])::"memory");
 }
 
 // Load and wait in one statement.

@@ -329,3 +329,33 @@ def test_tc_stress_vs_oracle(cuda, native, oracle, kind, d, m, n, N):
     topo = oracle.topography(m, n, 'square')
     o = oracle.compute_errors_raw(w, topo, x, None, 2.0, 'numba')
     np.testing.assert_allclose(som.compute_errors(x), o[:2] / o[2], rtol=ERR_RTOL)
+
+
+@pytest.mark.parametrize('algo', ALGOS)
+def test_near_tied_best_two_units(cuda, native, oracle, algo):
+    """Rows of the benchmark catalogue whose two nearest units are closer than float32 rounding (the third well
+    apart), against the benchmark's initial map. The BMU must be the reference's in both the BMU-only pass and the
+    pass that also produces the error sums (which ranks the best two), and the error sums must match."""
+    from decontamination_gb300 import synthetic
+    g = golden('near_ties')
+    x = np.ascontiguousarray(np.tile(g['x'], (64, 1)))
+    w = synthetic.uniform_weights(1024, 16, 2)
+    b = oracle.find_bmus(w, x, 'numba')
+    assert np.array_equal(b[:len(g['x'])], g['oracle_bmu'])
+    som = _som(32, 32, 16, w, topology='hexagonal', algo=algo)
+    assert np.array_equal(som.get_winners(x), b)
+    topo = oracle.topography(32, 32, 'hexagonal')
+    N, M, D = x.shape[0], 1024, 16
+    xd, wd, td = (torch.from_numpy(a).to(cuda) for a in (x, w, topo))
+    bmu = torch.empty(N, dtype=torch.int32, device=cuda)
+    err = torch.zeros(3, dtype=torch.float64, device=cuda)
+    A = native.ALGOS[algo]
+    nbytes = native.workspace_bytes(native.OP_FIND_BMUS, N, M, D, A)
+    ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=cuda)
+    wsp = ws.data_ptr() + (-ws.data_ptr()) % 256
+    native.call('somgb_train_bmu_pass', xd.data_ptr(), None, N, D, wd.data_ptr(), td.data_ptr(), M, 1.0, A,
+                bmu.data_ptr(), err.data_ptr(), wsp, nbytes, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(bmu.cpu().numpy(), b)
+    o = oracle.compute_errors_raw(w, topo, x, None, 1.0, 'numba')
+    np.testing.assert_allclose(err.cpu().numpy(), o, rtol=ERR_RTOL)
