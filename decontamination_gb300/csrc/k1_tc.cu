@@ -2,7 +2,8 @@
 //
 // Distances are expanded as |x - w_j|^2 = |x'|^2 + s_j with s_j = |w'_j|^2 - 2 x'.w'_j, where x' = (x - c) S and
 // w' = (w - c) S are centred on the mean unit c (the centring shrinks every error term below) and scaled by a power
-// of two S that puts the largest unit coordinate in [2^9, 2^10) (FP16 range; exact in float32). One GEMM per
+// of two S that puts the largest unit coordinate in [2^5, 2^6) (samples up to 512 times farther out stay in FP16
+// range; the scaling is exact in float32). One GEMM per
 // 128-sample row tile and 256-unit column tile produces s~_j in TMEM:
 //   A row (sample)  = [ x'_hi | x'_lo | x'_hi | 2^11 | 2^11 | 0 ... ]             (FP16, K padded to a multiple of 16)
 //   B row (unit j)  = [ -2w'_hi | -2w'_hi | -2w'_lo | q_hi | q_lo | 0 ... ] with q_hi + q_lo = 2^-11 |w'_j|^2
@@ -13,7 +14,7 @@
 // Error bound. With FP16 unit roundoff 2^-11, dropping x_lo w_lo and the two-term residuals costs at most
 // 3.01 * 2^-22 |x'_k||w'_k| per product; q's split and float32 evaluation cost 2.5 * 2^-22 |w'|^2 + (D+2) 2^-24 |w'|^2;
 // the FP32 accumulation of the K non-zero products is bounded by K * 2^-23 * sum|terms| (one rounding per product,
-// the worst case); FP16 subnormals add an absolute 2^-8 at most.
+// the worst case); FP16 subnormals add at most 2^-21 |x'|^2 plus an absolute 2^-8.
 // Using |w'_j|^2 <= 2|x'|^2 + 2 d'_j (d'_j = |x' - w'_j|^2) every term is bounded by
 //   |s~_j - s_j| <= alpha |x'|^2 + beta d'_j + gamma,
 // with alpha, beta computed on the host (tc_error_coefficients). A unit can beat the tile's best (or, for the
@@ -170,6 +171,8 @@ void tc_error_coefficients(int d, float* alpha, float* beta) {
     // centring rounding and the reference's own float32 rounding of each term
     a += std::ldexp(1.0, -21);
     b += std::ldexp(1.0, -21);
+    // FP16 subnormal split residuals (absolute 2^-25) times |x'_k| summed over k: below 2^-24 sqrt(D) (1 + |x'|^2) / 2
+    a += std::ldexp(1.0, -21);
     *alpha = (float)(1.25 * a);   // 25% safety margin
     *beta = (float)(1.25 * b);
 }
@@ -180,7 +183,7 @@ void tc_error_coefficients(int d, float* alpha, float* beta) {
 
 __global__ void tc_center_kernel(const float* __restrict__ w, int64_t m, int d, float* __restrict__ center) {
     // mean of the finite unit rows, per feature, in float64; then center[d] = the power-of-two scale S that puts the
-    // largest |w - c| coordinate of those rows in [2^9, 2^10)
+    // largest |w - c| coordinate of those rows in [2^5, 2^6)
     __shared__ double part[256];
     __shared__ unsigned long long cnt_s;
     __shared__ unsigned int maxbits_s;
@@ -216,7 +219,7 @@ __global__ void tc_center_kernel(const float* __restrict__ w, int64_t m, int d, 
         int e = 0;
         if (mx > 0.0f && isfinite(mx)) frexpf(mx, &e);   // mx < 2^e
         else e = 10;
-        center[d] = ldexpf(1.0f, min(max(10 - e, -100), 100));
+        center[d] = ldexpf(1.0f, min(max(6 - e, -100), 100));
     }
 }
 

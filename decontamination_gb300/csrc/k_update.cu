@@ -37,6 +37,26 @@ __device__ __forceinline__ void fx_add(int32_t* limbs, int64_t nb, int64_t bin, 
     atomicAdd(limbs + 2 * nb + bin, (int32_t)(q >> 32));
 }
 
+// Nearest integer of a float32 in [-2^22, 2^22], exactly, with full-rate float and integer ops: adding 1.5 * 2^23
+// rounds to an integer and puts it in the low mantissa bits.
+__device__ __forceinline__ int32_t fx_small_int(float v) {
+    return (int32_t)__float_as_uint(__fadd_rn(v, 12582912.0f)) - 0x4B400000;
+}
+
+// Adds q = rint(f) (|f| < 2^47) as three signed limbs, q = L2 * 2^32 + L1 * 2^16 + L0 with |L| <= 2^15, without a
+// 64-bit conversion: adding 1.5 * 2^55 rounds f to a multiple of 2^32 (f2), 1.5 * 2^39 rounds the exact remainder to
+// a multiple of 2^16 (f1), and 1.5 * 2^23 rounds the last remainder to an integer; every step is exact float32.
+// The limbs of 2^15 samples stay inside int32 and recombine as in the unsigned split.
+__device__ __forceinline__ void fx_add_float(int32_t* limbs, int64_t nb, int64_t bin, float f) {
+    const float f2 = __fsub_rn(__fadd_rn(f, 54043195528445952.0f), 54043195528445952.0f);   // 1.5 * 2^55
+    const float r = __fsub_rn(f, f2);                                                      // |r| <= 2^31
+    const float f1 = __fsub_rn(__fadd_rn(r, 824633720832.0f), 824633720832.0f);           // 1.5 * 2^39
+    const float r0 = __fsub_rn(r, f1);                                                     // |r0| <= 2^15
+    atomicAdd(limbs + bin, fx_small_int(r0));
+    atomicAdd(limbs + nb + bin, fx_small_int(__fmul_rn(f1, 1.52587890625e-05f)));          // f1 / 2^16
+    atomicAdd(limbs + 2 * nb + bin, fx_small_int(__fmul_rn(f2, 2.3283064365386963e-10f))); // f2 / 2^32
+}
+
 __global__ void __launch_bounds__(256) feature_bounds_kernel(const float* __restrict__ x, const double* __restrict__ rho,
                                                              int64_t n, int d, unsigned int* __restrict__ bounds) {
     extern __shared__ unsigned int smax[];   // d + 1
@@ -103,7 +123,7 @@ __global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restric
                 }
                 if (r == 1.0f) {
 #pragma unroll
-                    for (int k = 0; k < DT; ++k) fx_add(limbs, nb, bin + k, __float2ll_rn(xv[k] * scale_s[k]));
+                    for (int k = 0; k < DT; ++k) fx_add_float(limbs, nb, bin + k, xv[k] * scale_s[k]);
                 } else {
 #pragma unroll
                     for (int k = 0; k < DT; ++k) {
@@ -120,7 +140,7 @@ __global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restric
                     fx_add(limbs, nb, bin + k, __float2ll_rn(hi * scale_s[k]) + __float2ll_rn(lo_ * scale_s[k]));
                 }
             }
-            fx_add(limbs, nb, bin + d, __float2ll_rn(r * scale_s[d]));
+            fx_add_float(limbs, nb, bin + d, r * scale_s[d]);
         }
         __syncthreads();
         for (int64_t q = threadIdx.x; q < nb; q += blockDim.x) {
@@ -135,6 +155,105 @@ __global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restric
             const double val = ldexp((double)v, exp_s[k] - FX_BITS);
             if (k < d) atomicAdd(S + u * d + k, val);
             else atomicAdd(c + u, val);
+        }
+        __syncthreads();
+    }
+}
+
+// The same sums with the lanes of a warp spread over features: DP lanes (a power of two >= d) per sample, 32 / DP
+// samples per warp instruction. The DP lanes of a sample add d contiguous words of one unit's bins, so an atomic
+// instruction touches 32 / DP short runs of banks instead of 32 random banks. Unweighted samples add 1 to an
+// integer count per unit; weighted ones add their float32 weight in fixed point like a feature.
+template <int DP>
+__global__ void __launch_bounds__(1024) accumulate_lanes_kernel(const float* __restrict__ x, const double* __restrict__ rho,
+                                                                const int32_t* __restrict__ bmu, int64_t n, int d,
+                                                                int64_t units_per_range, int64_t m, int64_t chunk,
+                                                                const float* __restrict__ bounds, double* __restrict__ S,
+                                                                double* __restrict__ c) {
+    extern __shared__ int32_t lane_bins[];   // [3][cnt * d] feature limbs, then [cnt] counts or [3][cnt] weight limbs
+    __shared__ float scale_s[33];
+    __shared__ int exp_s[33];
+    constexpr int SPW = 32 / DP;
+    const int64_t lo = (int64_t)blockIdx.y * units_per_range;
+    const int64_t cnt = min64(units_per_range, m - lo);
+    const int64_t nbf = cnt * d;
+    int32_t* limbs = lane_bins;
+    int32_t* csum = lane_bins + 3 * nbf;
+    const int64_t nbc = rho ? 3 * cnt : cnt;
+    for (int64_t q = threadIdx.x; q < 3 * nbf + nbc; q += blockDim.x) lane_bins[q] = 0;
+    for (int k = threadIdx.x; k <= d; k += blockDim.x) {
+        const int e = fx_exponent(bounds[k]);
+        exp_s[k] = e;
+        scale_s[k] = ldexpf(1.0f, FX_BITS - e);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int slot = lane / DP, k = lane % DP;
+    const bool kval = k < d;
+    const float sk = kval ? scale_s[k] : 0.0f;
+    const int64_t s0 = (int64_t)blockIdx.x * chunk;
+    const int64_t s1 = min64(n, s0 + chunk);
+    for (int64_t w0 = s0; w0 < s1; w0 += FX_WINDOW) {
+        const int64_t w1 = min64(s1, w0 + FX_WINDOW);
+        // UNR sample groups per warp and step, all loaded before any is added (memory-level parallelism)
+        constexpr int UNR = 8;
+        for (int64_t base = w0 + (int64_t)warp * SPW * UNR; base < w1; base += (int64_t)nwarps * SPW * UNR) {
+            int32_t bb[UNR];
+            float xv[UNR];
+#pragma unroll
+            for (int t = 0; t < UNR; ++t) {
+                const int64_t i = base + t * SPW + slot;
+                bb[t] = i < w1 ? __ldg(bmu + i) : -1;
+                xv[t] = (i < w1 && kval) ? __ldg(x + i * d + k) : 0.0f;
+            }
+#pragma unroll
+            for (int t = 0; t < UNR; ++t) {
+                if (bb[t] < lo || bb[t] >= lo + cnt) continue;   // also skips b == -1
+                const int64_t u = bb[t] - lo;
+                if (!rho) {
+                    if (kval) fx_add_float(limbs, nbf, u * d + k, xv[t] * sk);
+                    if (k == 0) atomicAdd(csum + u, 1);
+                } else {
+                    const float r = (float)__ldg(rho + base + t * SPW + slot);   // float32 density (som_batch.py:312)
+                    if (kval) {
+                        const float hi = r * xv[t];
+                        const float lo_ = fmaf(r, xv[t], -hi);   // r * x exactly as hi + lo
+                        fx_add(limbs, nbf, u * d + k, __float2ll_rn(hi * sk) + __float2ll_rn(lo_ * sk));
+                    }
+                    if (k == 0) fx_add_float(csum, cnt, u, r * scale_s[d]);
+                }
+            }
+        }
+        __syncthreads();
+        for (int64_t q = threadIdx.x; q < nbf + cnt; q += blockDim.x) {
+            long long v;
+            int kk;
+            int64_t uu;
+            if (q < nbf) {
+                v = (long long)limbs[q] + ((long long)limbs[nbf + q] << 16) + ((long long)limbs[2 * nbf + q] << 32);
+                limbs[q] = 0;
+                limbs[nbf + q] = 0;
+                limbs[2 * nbf + q] = 0;
+                uu = q / d;
+                kk = (int)(q % d);
+            } else {
+                const int64_t qc = q - nbf;
+                if (!rho) {
+                    v = csum[qc];
+                    csum[qc] = 0;
+                } else {
+                    v = (long long)csum[qc] + ((long long)csum[cnt + qc] << 16) + ((long long)csum[2 * cnt + qc] << 32);
+                    csum[qc] = 0;
+                    csum[cnt + qc] = 0;
+                    csum[2 * cnt + qc] = 0;
+                }
+                uu = qc;
+                kk = d;
+            }
+            if (v == 0) continue;
+            const double val = (kk < d || rho) ? ldexp((double)v, exp_s[kk] - FX_BITS) : (double)v;
+            if (kk < d) atomicAdd(S + (lo + uu) * d + kk, val);
+            else atomicAdd(c + lo + uu, val);
         }
         __syncthreads();
     }
@@ -350,10 +469,11 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
         return SOMGB_OK;
     }
     if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "fixed-point segmented sums support D <= 64");
-    // three int32 limbs per bin; up to ~220 KB of bins per CTA, so that a 32x32 map with D = 16 (17 bins a unit) fits
-    // one CTA and every sample is read once
+    // three int32 limbs per bin; up to ~220 KB of bins per CTA, so that a 32x32 map with D = 16 fits one CTA and every
+    // sample is read once
     const size_t budget = 220 * 1024;
-    const int64_t per_unit = (int64_t)(d + 1) * 12;
+    const bool lanes = d <= 32;
+    const int64_t per_unit = lanes ? (int64_t)d * 12 + (rho ? 12 : 4) : (int64_t)(d + 1) * 12;
     int64_t upr = std::max<int64_t>(1, (int64_t)(budget / per_unit));
     upr = std::min(upr, m);
     const int64_t ranges = ceil_div(m, upr);
@@ -364,17 +484,22 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
     int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
     int64_t chunk = std::max<int64_t>(4096, ceil_div(n, chunks));
     chunks = ceil_div(n, chunk);
-    auto kern = accumulate_kernel<0>;
-    if (((uintptr_t)x) % 16 == 0) {
-        if (d == 4) kern = accumulate_kernel<4>;
-        else if (d == 8) kern = accumulate_kernel<8>;
-        else if (d == 16) kern = accumulate_kernel<16>;
-        else if (d == 32) kern = accumulate_kernel<32>;
+    const dim3 grid((unsigned)chunks, (unsigned)ranges);
+    if (lanes) {
+        auto kern = accumulate_lanes_kernel<32>;
+        if (d <= 4) kern = accumulate_lanes_kernel<4>;
+        else if (d <= 8) kern = accumulate_lanes_kernel<8>;
+        else if (d <= 16) kern = accumulate_lanes_kernel<16>;
+        if (smem > 48 * 1024)
+            SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid, 1024, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, bounds, S, c);
+        SOMGB_LAUNCH_CHECK();
+        return SOMGB_OK;
     }
+    auto kern = accumulate_kernel<0>;
     if (smem > 48 * 1024)
         SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<dim3((unsigned)chunks, (unsigned)ranges), 1024, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m,
-                                                                          chunk, bounds, S, c);
+    kern<<<grid, 1024, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, bounds, S, c);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
