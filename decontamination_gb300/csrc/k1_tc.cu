@@ -327,6 +327,20 @@ __device__ __forceinline__ void cand_dist32_multi(const float* __restrict__ w, c
     }
 }
 
+// Normalised float32 pairs (|lo| <= ulp(hi) / 2) in (value, unit) order; empty entries (unit < 0) last.
+__device__ __forceinline__ bool df_before(DFloat a, int32_t ja, DFloat b, int32_t jb) {
+    return ja >= 0 && (jb < 0 || a.hi < b.hi || (a.hi == b.hi && (a.lo < b.lo || (a.lo == b.lo && ja < jb))));
+}
+// b (unit jb; absent when jb < 0) exceeds a by more than 2^-36 of b. Each pair is the compensated float32 sum of
+// the D float32 squares: its low word carries at most (D-1)^2 2^-48 of the sum in rounding (2^-38 at D = 32), and the
+// reference's float64 sum of the same squares is within (D-1) 2^-53 of the exact one; so pairs that far apart stand
+// for float64 sums ordered the same way.
+__device__ __forceinline__ bool df_apart(DFloat a, DFloat b, int32_t jb) {
+    if (jb < 0) return true;
+    const float gap = __fadd_rn(__fsub_rn(b.hi, a.hi), __fsub_rn(b.lo, a.lo));
+    return gap > 1.4551915e-11f * b.hi;   // 2^-36
+}
+
 // (da, ja) ranks before (db, jb): lexicographic, empty entries (unit < 0) last
 __device__ __forceinline__ bool lex_before(float da, int32_t ja, float db, int32_t jb) {
     return ja >= 0 && (jb < 0 || da < db || (da == db && ja < jb));
@@ -768,19 +782,43 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     r2 = ERR ? j2 : -1;
                     if (ERR && j1 >= 0) rd1 = ref_dist_pair<DT>(a.w + (int64_t)j1 * DT, xr);
                 } else {
-                    // float64 reference sums of every contender, ranked in (distance, unit) order
-                    const float* xs = xg;
-                    Top2Lex tt;
-                    tt.init();
+                    // Contenders ranked by the compensated sum of the reference's float32 squares as a normalised
+                    // float32 pair; ranks whose pairs differ by more than 2^-36 of the larger are the reference's
+                    // ranks (df_apart). Closer ones (equal units, in practice) take the reference's float64 sums.
+                    DFloat p1{INFINITY, 0.0f}, p2{INFINITY, 0.0f}, p3{INFINITY, 0.0f};
+                    int32_t q1 = -1, q2 = -1, q3 = -1;
                     for (int k = 0; k < cnt; ++k) {
                         const int32_t j = list[k * TM];
                         if (!(cand_dist32v<DT>(a.w + (int64_t)j * DT, xr) <= climit)) continue;
-                        tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
+                        const DFloat t = ref_dist_pair<DT>(a.w + (int64_t)j * DT, xr);
+                        const DFloat v = two_sum(t.hi, t.lo);
+                        if (df_before(v, j, p3, q3)) {
+                            if (df_before(v, j, p2, q2)) {
+                                p3 = p2; q3 = q2;
+                                if (df_before(v, j, p1, q1)) { p2 = p1; q2 = q1; p1 = v; q1 = j; }
+                                else { p2 = v; q2 = j; }
+                            } else { p3 = v; q3 = j; }
+                        }
                     }
-                    r1 = tt.i1;
-                    r2 = ERR ? tt.i2 : -1;
-                    rd1.hi = (float)tt.d1;
-                    rd1.lo = (float)(tt.d1 - (double)rd1.hi);
+                    const bool sure = df_apart(p1, p2, q2) && (!ERR || df_apart(p2, p3, q3));
+                    if (sure) {
+                        r1 = q1;
+                        r2 = ERR ? q2 : -1;
+                        rd1 = p1;
+                    } else {
+                        const float* xs = xg;
+                        Top2Lex tt;
+                        tt.init();
+                        for (int k = 0; k < cnt; ++k) {
+                            const int32_t j = list[k * TM];
+                            if (!(cand_dist32v<DT>(a.w + (int64_t)j * DT, xr) <= climit)) continue;
+                            tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
+                        }
+                        r1 = tt.i1;
+                        r2 = ERR ? tt.i2 : -1;
+                        rd1.hi = (float)tt.d1;
+                        rd1.lo = (float)(tt.d1 - (double)rd1.hi);
+                    }
                     if (ERR && r1 >= 0 && r2 >= 0) {
                         tr1 = topo2[r1];
                         tr2 = topo2[r2];

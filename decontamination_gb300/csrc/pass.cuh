@@ -118,9 +118,11 @@ __device__ __forceinline__ void emit_sample32(const PassArgs& a, int64_t i, doub
     const int outs = a.outs;
     const long long bits = __double_as_longlong(r);
     const bool pos = bits > 0 && bits <= 0x7FF0000000000000LL;   // r > 0 (NaN excluded)
-    DFloat rho;
-    rho.hi = (float)r;
-    rho.lo = (float)(r - (double)rho.hi);
+    DFloat rho{1.0f, 0.0f};
+    if (a.rho) {   // no float64 work for unweighted samples
+        rho.hi = (float)r;
+        rho.lo = (float)(r - (double)rho.hi);
+    }
     if (outs & OUT_BMU) a.bmu_out[i] = i1 < 0 ? 0 : i1;
     if ((outs & OUT_HIST) && pos) atomicAdd(a.hist + (i1 < 0 ? 0 : i1), (double)rho.hi + (double)rho.lo);
     if (outs & OUT_TRAIN) a.train_bmu[i] = (rho.hi > 0.0f && i1 >= 0) ? i1 : -1;
