@@ -37,6 +37,10 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(name='hex 32x32 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=16, 20-epoch schedule',
                 m=32, n=32, d=16, N=12_582_912, topology='hexagonal', sigma0=16.0, schedule=20, seed=2)
 METRIC = 'SOM epoch Gsample·unit/s'
+# DRAM traffic (bytes read + written) of one tensor-core BMU pass per catalogue row, from an ncu capture of
+# tc_pass_kernel on the 4,194,304-row case of this workload (summary under profiles/). The pass streams every row
+# once (64 B of samples, 4 B of BMU, unit operand from L2), so the traffic of a full launch scales with N.
+K1_DRAM_BYTES_PER_ROW = 67.84
 UNIT = 'Gsample·unit/s'
 
 
@@ -336,16 +340,17 @@ def gpu_arm(args, ws, rank, local):
     achieved_tflops = flops / (k_ms * 1e-3) / 1e12
     peak = peaks.get('bf16_tflops_sustained', peaks.get('bf16_tflops'))
     roofline = {'bound': 'tensor', 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
-                'frac': achieved_tflops / peak, 'traffic': None,
-                'kernel': 'BMU pass (%s)' % ('tcgen05 split-BF16' if used_algo == 'tc' else 'FP32 CUDA cores'),
+                'frac': achieved_tflops / peak,
+                'traffic': K1_DRAM_BYTES_PER_ROW * N if used_algo == 'tc' else None,
+                'kernel': 'BMU pass (%s)' % ('tcgen05 split-FP16' if used_algo == 'tc' else 'FP32 CUDA cores'),
                 'kernel_ms': k_ms, 'kernel_share': k_ms * args.steps / total_ms,
-                'peak_source': f'{peak_kind} bf16_tflops_sustained',
+                'peak_source': f'{peak_kind} bf16_tflops_sustained (dense FP16 and BF16 share the rate)',
                 'hbm_bytes_algorithmic': N * D * 4 + N * 4,
                 'hbm_frac': (N * D * 4 + N * 4) / (k_ms * 1e-3) / 1e9 / peaks.get('hbm_gbs', 6800.0)}
     out = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'bf16x3-split/f32acc' if used_algo == 'tc' else 'f32',
+        'dtype': 'f16x3-split/f32acc' if used_algo == 'tc' else 'f32',
         'data': 'synthetic (seeded correlated log-normal, cond 100, 2% rows x10; weights U[-1,1])',
         'config': {'workload': w['name'], 'algo': used_algo, 'N_per_gpu': N, 'M': M, 'D': D,
                    'l2': 'catalogue 805 MB > 129 MB L2 per epoch; no flush', 'parallelism': f'replicas x{ws}'},
