@@ -35,10 +35,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Polls until phase `parity` of `bar` has completed; false after `limit` polls (about a second at the limit used).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 24)) {
+// The same with a suspend-time hint: a waiting thread sleeps until the phase completes or about `ns` nanoseconds
+// pass, instead of re-polling (which takes issue slots from the warps doing the work).
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+// Waits until phase `parity` of `bar` has completed; false after `limit` polls of at most ~1 us each (a second or
+// more at the default limit; shorter only if the hardware ignores the hint, still far above any legitimate wait).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 22)) {
+    if (mbar_try_wait(bar, parity)) return true;
     for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
     return false;
 }
 
