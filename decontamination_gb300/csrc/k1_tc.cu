@@ -7,7 +7,8 @@
 // 128-sample row tile and 256-unit column tile produces s~_j in TMEM:
 //   A row (sample)  = [ x'_hi | x'_lo | x'_hi | 2^11 | 2^11 | 0 ... ]             (FP16, K padded to a multiple of 16)
 //   B row (unit j)  = [ -2w'_hi | -2w'_hi | -2w'_lo | q_hi | q_lo | 0 ... ] with q_hi + q_lo = 2^-11 |w'_j|^2
-// so that sum_k A.B = -2 (x_hi w_hi + x_lo w_hi + x_hi w_lo) + |w'|^2 ~ s_j, accumulated in FP32. Invalid and padding
+// so that sum_k A.B = -2 (x_hi w_hi + x_lo w_hi + x_hi w_lo) + |w'|^2 ~ s_j, accumulated in FP32. (For D a multiple
+// of 16 the repeated blocks are stored once and the MMA K-steps point at them twice; see k_step_cols.) Invalid and padding
 // units carry q_hi = +inf (s~ = +inf); rows with a coordinate at or above 2^15 after scaling, or non-finite, go to
 // the exact recheck.
 //
@@ -29,7 +30,7 @@
 // CAPR candidates, non-finite features or overflowing distances go to an exact per-row recheck.
 //
 // Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
-//   warp 13     TMA producer: the unit operand B once (bulk copy), sample tiles (2-D tiled TMA, 3-stage ring);
+//   warp 13     TMA producer: the unit operand B once (bulk copy), sample tiles (2-D tiled TMA, 2-stage ring);
 //   warp 12     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
 //   warps 0-7   converters (FP32 tile -> centred split-BF16 A tile) and sweeps; warp e reads TMEM lanes
 //               32(e&3).. and column half e>>2, and writes the candidates of its rows into a double buffer;
@@ -80,7 +81,7 @@ constexpr int TN = 256;           // units per column tile (MMA N)
 constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
 constexpr int CAPR = 32;          // candidates a resolver keeps per row (unit indices as uint16)
 constexpr int MAX_U = 8;          // column tiles per row tile (the candidate summary is a 32-bit word per half)
-constexpr int XSTAGES = 3;
+constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
 constexpr int RES_WARPS = 4;
 constexpr int MMA_WARP = SWEEP_WARPS + RES_WARPS;
@@ -91,6 +92,30 @@ constexpr float Q_COLUMN = 2048.0f;   // A's value in the two q columns (B holds
 constexpr float GAMMA = 0.00390625f;  // 2^-8: absolute error bound of the FP16 subnormal range, in scaled units
 constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go to the exact recheck
 constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN);
+
+// K layout of the operands (elements per row, FP16). D a multiple of 16: A = [x_hi | x_lo | q columns],
+// B = [-2w_hi | -2w_lo | q_hi q_lo 0...], and the MMA K-steps pair the blocks (hi.hi, lo.hi, hi.lo, then q), so no
+// block is stored twice. Other D: A = [x_hi | x_lo | x_hi | 2^11 2^11 | 0...], B = [-2w_hi | -2w_hi | -2w_lo | q_hi
+// q_lo | 0...] padded to a multiple of 16, one K-step per 16 columns.
+__host__ __device__ constexpr bool k_dedup(int d) { return d % 16 == 0; }
+__host__ __device__ constexpr int k_width(int d) { return k_dedup(d) ? 2 * d + 16 : (3 * d + 2 + 15) / 16 * 16; }
+__host__ __device__ constexpr int k_steps(int d) { return k_dedup(d) ? 3 * (d / 16) + 1 : k_width(d) / 16; }
+__host__ __device__ constexpr int k_qcol(int d) { return k_dedup(d) ? 2 * d : 3 * d; }   // first q column
+// column offsets of K-step i in A and in B
+__device__ __forceinline__ void k_step_cols(int d, int i, int& ka, int& kb) {
+    if (!k_dedup(d)) {
+        ka = kb = 16 * i;
+        return;
+    }
+    const int nb = d / 16;
+    if (i == 3 * nb) {
+        ka = kb = 2 * d;
+        return;
+    }
+    const int blk = i % nb, kind = i / nb;   // kind 0: hi.hi, 1: lo.hi, 2: hi.lo
+    ka = (kind == 1 ? d : 0) + 16 * blk;
+    kb = (kind == 2 ? d : 0) + 16 * blk;
+}
 
 struct TcShape {
     int d = 0, kpad = 0, knz = 0;
@@ -105,7 +130,7 @@ TcShape tc_shape(int64_t m, int d) {
     TcShape s;
     s.d = d;
     s.knz = 3 * d + 2;
-    s.kpad = (int)align_up((size_t)s.knz, 16);
+    s.kpad = k_width(d);
     s.mpad = (int64_t)align_up((size_t)m, TN);
     s.utiles = (int)(s.mpad / TN);
     s.b_bytes = (size_t)s.mpad * s.kpad * 2;
@@ -245,22 +270,28 @@ __global__ void tc_prep_b_kernel(const float* __restrict__ w, int64_t m, int d, 
         if (!(q < 1.0e30f)) valid = false;
     }
     for (int k = 0; k < kpad; ++k) put(k, 0.0f);
+    const int qc = k_qcol(d);
     if (!valid) {
-        put(3 * d, INFINITY);   // never the minimum, never under a threshold: s~ = +inf
+        put(qc, INFINITY);   // never the minimum, never under a threshold: s~ = +inf
         return;
     }
+    const bool dedup = k_dedup(d);
     for (int k = 0; k < d; ++k) {
         const float t = (w[j * d + k] - center[k]) * scale;
         const __half hi = __float2half_rn(t);
         const __half lo = __float2half_rn(t - __half2float(hi));
         put(k, -2.0f * __half2float(hi));
-        put(d + k, -2.0f * __half2float(hi));
-        put(2 * d + k, -2.0f * __half2float(lo));
+        if (dedup) {
+            put(d + k, -2.0f * __half2float(lo));
+        } else {
+            put(d + k, -2.0f * __half2float(hi));
+            put(2 * d + k, -2.0f * __half2float(lo));
+        }
     }
     const float qs = q * (1.0f / Q_COLUMN);
     const __half qh = __float2half_rn(qs);
-    put(3 * d, __half2float(qh));
-    put(3 * d + 1, qs - __half2float(qh));
+    put(qc, __half2float(qh));
+    put(qc + 1, qs - __half2float(qh));
 }
 
 // ---------------------------------------------------------------------------------------------------------------------
@@ -393,7 +424,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     const PassArgs& a = P.a;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int d = DT;
-    constexpr int kpad = (3 * DT + 2 + 15) / 16 * 16;
+    constexpr int kpad = k_width(DT);
     const int U = P.utiles;
     const int64_t num_tiles = (a.n + TM - 1) / TM;
     const int64_t n_my = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
@@ -487,10 +518,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         ptx::tc_fence_after();
                         const uint32_t dt = tbase + (uint32_t)(buf * TN);
                         const uint32_t bu = b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
-                        for (int kb = 0; kb < kpad / 16; ++kb) {
-                            const uint64_t ad = ptx::smem_desc(a_addr + kb * 256, 128, sbo);
-                            const uint64_t bd = ptx::smem_desc(bu + kb * 256, 128, sbo);
-                            ptx::mma_f16(dt, ad, bd, IDESC, kb > 0);
+#pragma unroll
+                        for (int ks = 0; ks < k_steps(DT); ++ks) {
+                            int ka, kb;
+                            k_step_cols(DT, ks, ka, kb);
+                            const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
+                            const uint64_t bd = ptx::smem_desc(bu + (uint32_t)(kb / 8) * 128u, 128, sbo);
+                            ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
                         }
                         ptx::mma_commit(t_full + buf);
                     }
@@ -543,12 +577,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int k = kc * 8 + i;
+                        constexpr int nx = k_dedup(DT) ? 2 * DT : 3 * DT;   // x_hi | x_lo (| x_hi)
                         float val = 0.0f;
-                        if (k < 3 * DT) {
+                        if (k < nx) {
                             const float t = xp[k % DT];
                             const float hi = __half2float(__float2half_rn(t));
                             val = (k >= DT && k < 2 * DT) ? t - hi : hi;
-                        } else if (k == 3 * DT || k == 3 * DT + 1) {
+                        } else if (k == k_qcol(DT) || k == k_qcol(DT) + 1) {
                             val = Q_COLUMN;
                         }
                         v[i] = __float2half_rn(finite ? val : 0.0f);
