@@ -79,7 +79,8 @@ namespace {
 constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
 constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
-constexpr int CAPR = 32;          // candidates a resolver keeps per row (unit indices as uint16)
+constexpr int CAPR = 24;          // candidates a resolver keeps per row (unit indices as uint16)
+constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
 constexpr int MAX_U = 8;          // column tiles per row tile (the candidate summary is a 32-bit word per half)
 constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
@@ -123,7 +124,7 @@ struct TcShape {
     int utiles = 0;
     size_t b_bytes = 0, a_bytes = 0, x_bytes = 0;
     size_t off_a = 0, off_x = 0, off_mask = 0, off_sum = 0, off_flag = 0, off_rlist = 0, off_part = 0, off_center = 0,
-           off_bar = 0, smem = 0;
+           off_bar = 0, off_w = 0, smem = 0;
 };
 
 TcShape tc_shape(int64_t m, int d) {
@@ -150,12 +151,19 @@ TcShape tc_shape(int64_t m, int d) {
     s.off_rlist = off;
     off += (size_t)(CAPR + 1) * TM * 2;
     s.off_part = off;
-    off += (size_t)2 * HALVES * TM * 8;
+    off += (size_t)HALVES * TM * 8;
     s.off_center = off;
     off += align_up((size_t)(d + 1) * 4, 16);
     s.off_bar = align_up(off, 8);
     off = s.off_bar + 32 * 8;
-    s.smem = off + 1024;   // slack for aligning the dynamic base to 1024
+    // the float32 unit rows, for the resolvers' candidate distances, when they fit (otherwise read from L2)
+    const size_t w_bytes = (size_t)m * d * 4;
+    const size_t off_w = align_up(off, 16);
+    if (off_w + w_bytes + 128 <= SMEM_LIMIT) {
+        s.off_w = off_w;
+        off = off_w + w_bytes;
+    }
+    s.smem = off + 128;   // slack for aligning the dynamic base to 128 bytes (TMA tile destinations)
     return s;
 }
 
@@ -307,7 +315,7 @@ struct TcArgs {
     int kpad;
     int utiles;
     float alpha, beta;
-    size_t off_a, off_x, off_mask, off_sum, off_flag, off_rlist, off_part, off_center, off_bar, a_stride, x_stride;
+    size_t off_a, off_x, off_mask, off_sum, off_flag, off_rlist, off_part, off_center, off_bar, off_w, a_stride, x_stride;
     uint32_t b_bytes;
 };
 
@@ -318,7 +326,7 @@ __device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, cons
     const float4* w4 = (const float4*)wr;
 #pragma unroll
     for (int k4 = 0; k4 < DT / 4; ++k4) {
-        const float4 w = __ldg(w4 + k4);
+        const float4 w = w4[k4];
         float t = w.x - xr[4 * k4]; acc = fmaf(t, t, acc);
         t = w.y - xr[4 * k4 + 1]; acc = fmaf(t, t, acc);
         t = w.z - xr[4 * k4 + 2]; acc = fmaf(t, t, acc);
@@ -343,7 +351,7 @@ __device__ __forceinline__ void cand_dist32_multi(const float* __restrict__ w, c
 #pragma unroll
     for (int i = 0; i < NQ; ++i)
 #pragma unroll
-        for (int k4 = 0; k4 < DT / 4; ++k4) r[i][k4] = __ldg((const float4*)(w + (int64_t)jj[i] * DT) + k4);
+        for (int k4 = 0; k4 < DT / 4; ++k4) r[i][k4] = ((const float4*)(w + (int64_t)jj[i] * DT))[k4];
 #pragma unroll
     for (int i = 0; i < NQ; ++i) {
         float acc = 0.0f;
@@ -384,7 +392,7 @@ __device__ __forceinline__ DFloat ref_dist_pair(const float* __restrict__ wr, co
     const float4* w4 = (const float4*)wr;
 #pragma unroll
     for (int k4 = 0; k4 < DT / 4; ++k4) {
-        const float4 w = __ldg(w4 + k4);
+        const float4 w = w4[k4];
         const float t0 = __fsub_rn(w.x, xr[4 * k4]), t1 = __fsub_rn(w.y, xr[4 * k4 + 1]);
         const float t2 = __fsub_rn(w.z, xr[4 * k4 + 2]), t3 = __fsub_rn(w.w, xr[4 * k4 + 3]);
         acc.add(__fmul_rn(t0, t0));
@@ -398,14 +406,14 @@ __device__ __forceinline__ DFloat ref_dist_pair(const float* __restrict__ wr, co
 template <bool ERR, int DT>
 __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs P) {
     extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
     uint32_t* sMask = (uint32_t*)(smem + P.off_mask);   // [half][u][4][TM]: bit 31-i of word w: column 32w+i is a candidate
     uint32_t* sSum = (uint32_t*)(smem + P.off_sum);     // [half][TM]: bit 4u+w set when mask word (u, w) is non-zero
     uint8_t* sFlag = smem + P.off_flag;                 // [TM]: the row goes to the exact recheck
     uint16_t* sList = (uint16_t*)(smem + P.off_rlist);  // [CAPR + 1][TM]: the resolvers' candidate lists (+ scratch)
-    float2* sPart = (float2*)(smem + P.off_part);       // [buf][half][TM]: (m1, m2) of the half
+    float2* sPart = (float2*)(smem + P.off_part);       // [half][TM]: (m1, m2) of the half
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
     uint64_t* x_full = bars + 1;    // [XSTAGES]
@@ -449,6 +457,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         abort_s = 0;
     }
     for (int k = tid; k <= d; k += NUM_THREADS) sCenter[k] = P.center[k];   // centre and scale
+    if (P.off_w) {   // unit rows for the resolvers (16-byte aligned: checked on the host)
+        const float4* src = (const float4*)a.w;
+        float4* dst = (float4*)(smem + P.off_w);
+        for (int64_t i = tid; i < a.m * DT / 4; i += NUM_THREADS) dst[i] = __ldg(src + i);
+    }
     if (warp == MMA_WARP) {
         ptx::tmem_alloc(&tmem_base_s, 512);
         ptx::tmem_relinquish();
@@ -669,7 +682,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 TC_T(1);
             }
             if (!ok) break;
-            sPart[(cb * HALVES + h) * TM + row] =
+            sPart[h * TM + row] =
                 make_float2(fminf(a1, b1), fminf(fmaxf(a1, b1), fminf(a2, b2)));
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(p_full + cb * 4 + q);
@@ -677,7 +690,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             float M1 = INFINITY, M2 = INFINITY;
 #pragma unroll
             for (int t = 0; t < HALVES; ++t) {
-                const float2 p = sPart[(cb * HALVES + t) * TM + row];
+                const float2 p = sPart[t * TM + row];
                 M2 = fminf(fminf(M2, p.y), fmaxf(M1, p.x));
                 M1 = fminf(M1, p.x);
             }
@@ -725,6 +738,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         const float fac = 1.0f + 8.0f * g32;
         DFAcc e0, e1, e2;
         uint16_t* list = sList + row;
+        const float* wrows = P.off_w ? (const float*)(smem + P.off_w) : a.w;   // unit rows: shared memory or L2
         for (int64_t it = 0; it < n_my && !*abort_v; ++it) {
             TC_T0();
             if (!ptx::mbar_wait(m_full, (uint32_t)(it & 1))) { fail(1024u); break; }
@@ -735,6 +749,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             // the sample row from global memory (just read by the tile load, so in L2): the shared-memory stage is
             // released by the converters, which decouples the resolvers from the sample-tile ring
             const float* xg = a.x + (live ? grow : 0) * DT;
+            float xr[DT];   // loads issued before the candidate extraction, whose latency they overlap
+#pragma unroll
+            for (int k4 = 0; k4 < DT / 4; ++k4) {
+                const float4 t = __ldg((const float4*)xg + k4);
+                xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
+            }
             // candidate list of the row from the two halves' masks: one candidate per lane and iteration, the next
             // non-zero mask word (from the summary bits) fetched in the same iteration; no divergent branches
             const bool flagged = sFlag[row] != 0;
@@ -765,24 +785,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                 P.rows[slotq] = (int32_t)grow;
             } else if (live) {
-                float xr[DT];
-#pragma unroll
-                for (int k4 = 0; k4 < DT / 4; ++k4) {
-                    const float4 t = __ldg((const float4*)xg + k4);
-                    xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
-                }
-                // float32 top-3 of the candidates in (distance, unit) order, NQ candidates' loads in flight at once
-                // (with their topographic coordinates, which the error sums need for the best two)
+                // float32 top-3 of the candidates in (distance, unit) order, NQ candidates' rows read at once
                 float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
                 int32_t j1 = -1, j2 = -1, j3 = -1;
-                float2 t1 = make_float2(0.0f, 0.0f), t2 = t1, t3 = t1;
-                auto push = [&](float df, int32_t j, float2 tj) {
+                auto push = [&](float df, int32_t j) {
                     if (!lex_before(df, j, f3, j3)) return;
                     if (lex_before(df, j, f2, j2)) {
-                        f3 = f2; j3 = j2; t3 = t2;
-                        if (lex_before(df, j, f1, j1)) { f2 = f1; j2 = j1; t2 = t1; f1 = df; j1 = j; t1 = tj; }
-                        else { f2 = df; j2 = j; t2 = tj; }
-                    } else { f3 = df; j3 = j; t3 = tj; }
+                        f3 = f2; j3 = j2;
+                        if (lex_before(df, j, f1, j1)) { f2 = f1; j2 = j1; f1 = df; j1 = j; }
+                        else { f2 = df; j2 = j; }
+                    } else { f3 = df; j3 = j; }
                 };
                 constexpr int NQ = DT <= 16 ? 4 : 2;
                 const float2* topo2 = (const float2*)a.topo;
@@ -790,14 +802,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     int32_t jj[NQ];
 #pragma unroll
                     for (int i = 0; i < NQ; ++i) jj[i] = list[(k + i < cnt ? k + i : k) * TM];
-                    float2 tt[NQ];
-#pragma unroll
-                    for (int i = 0; i < NQ; ++i) tt[i] = ERR ? __ldg(topo2 + jj[i]) : make_float2(0.0f, 0.0f);
                     float dd[NQ];
-                    cand_dist32_multi<DT, NQ>(a.w, jj, xr, dd);
+                    cand_dist32_multi<DT, NQ>(wrows, jj, xr, dd);
 #pragma unroll
                     for (int i = 0; i < NQ; ++i)
-                        if (k + i < cnt) push(dd[i], jj[i], tt[i]);
+                        if (k + i < cnt) push(dd[i], jj[i]);
                 }
                 TC_T(8);
                 // The float32 ranking decides when every rank that matters is separated by more than the float32
@@ -810,12 +819,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const bool separated = ERR ? (gap12 && (j3 < 0 || !(f3 <= c2lim))) : gap12;
                 const float climit = ERR ? c2lim : c1lim;
                 int32_t r1, r2;
-                float2 tr1 = t1, tr2 = t2;
+                float2 tr1 = make_float2(0.0f, 0.0f), tr2 = tr1;
                 DFloat rd1{0.0f, 0.0f};
                 if (separated) {
                     r1 = j1;
                     r2 = ERR ? j2 : -1;
-                    if (ERR && j1 >= 0) rd1 = ref_dist_pair<DT>(a.w + (int64_t)j1 * DT, xr);
+                    // the error sums' topographic coordinates of the best two, loaded while rd1 is computed
+                    if (ERR && j1 >= 0 && j2 >= 0) {
+                        tr1 = __ldg(topo2 + j1);
+                        tr2 = __ldg(topo2 + j2);
+                    }
+                    if (ERR && j1 >= 0) rd1 = ref_dist_pair<DT>(wrows + (int64_t)j1 * DT, xr);
                 } else {
                     // Contenders ranked by the compensated sum of the reference's float32 squares as a normalised
                     // float32 pair; ranks whose pairs differ by more than 2^-36 of the larger are the reference's
@@ -824,8 +838,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     int32_t q1 = -1, q2 = -1, q3 = -1;
                     for (int k = 0; k < cnt; ++k) {
                         const int32_t j = list[k * TM];
-                        if (!(cand_dist32v<DT>(a.w + (int64_t)j * DT, xr) <= climit)) continue;
-                        const DFloat t = ref_dist_pair<DT>(a.w + (int64_t)j * DT, xr);
+                        if (!(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr) <= climit)) continue;
+                        const DFloat t = ref_dist_pair<DT>(wrows + (int64_t)j * DT, xr);
                         const DFloat v = two_sum(t.hi, t.lo);
                         if (df_before(v, j, p3, q3)) {
                             if (df_before(v, j, p2, q2)) {
@@ -846,7 +860,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         tt.init();
                         for (int k = 0; k < cnt; ++k) {
                             const int32_t j = list[k * TM];
-                            if (!(cand_dist32v<DT>(a.w + (int64_t)j * DT, xr) <= climit)) continue;
+                            if (!(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr) <= climit)) continue;
                             tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
                         }
                         r1 = tt.i1;
@@ -942,7 +956,7 @@ size_t max_smem_optin() {
 bool tc_shape_ok(int64_t m, int d) {
     if (d != 4 && d != 8 && d != 16 && d != 32) return false;
     if (m <= 0 || m > (int64_t)MAX_U * TN) return false;   // the per-half candidate summary covers MAX_U column tiles
-    return tc_shape(m, d).smem <= 227 * 1024;
+    return tc_shape(m, d).smem <= SMEM_LIMIT;
 }
 
 bool tc_device_ok(int64_t m, int d) {
@@ -1024,6 +1038,7 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     P.off_flag = s.off_flag;
     P.off_rlist = s.off_rlist;
     P.off_part = s.off_part;
+    P.off_w = s.off_w;
     P.off_center = s.off_center;
     P.off_bar = s.off_bar;
     P.a_stride = align_up(s.a_bytes, 1024);
