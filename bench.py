@@ -56,6 +56,10 @@ def parse():
     ap.add_argument('--skip-e2e', action='store_true')
     ap.add_argument('--skip-fp32', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--serve', action='store_true',
+                    help='BMU-serving latency instead of the epoch: 64x64x16 map, Poisson arrivals, mixed sizes')
+    ap.add_argument('--serve-seconds', type=float, default=5.0, help='arrival window of the serving run')
+    ap.add_argument('--serve-rate', type=float, default=200.0, help='mean request arrivals per second')
     return ap.parse_args()
 
 
@@ -402,9 +406,85 @@ def gpu_arm(args, ws, rank, local):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------------------------------------------------
+# BMU serving: requests of mixed sizes on a resident 64x64 map
+# ----------------------------------------------------------------------------------------------------------------------
+
+SERVE = dict(name='BMU serving: square 64x64 map (M = 4096), D = 16, Poisson arrivals, request sizes log-uniform '
+                  'in [1e3, 1e7] rows', m=64, n=64, d=16, seed=4, pool=10_000_000, lo=1_000, hi=10_000_000)
+
+
+def serve_arm(args):
+    """Requests arrive as a Poisson process and are submitted to SomServer as slices of a pinned host catalogue;
+    latency is submit to result on the host. The map is trained once (3 epochs on 500k rows) before the clock runs."""
+    import threading
+    import torch
+    import decontamination_gb300 as dg
+    from decontamination_gb300 import synthetic, _native, build as gbuild
+    from decontamination_gb300.serve import SomServer
+    gbuild.build()
+    s = SERVE
+    M, D = s['m'] * s['n'], s['d']
+    pool = torch.from_numpy(synthetic.gaussian_mixture(s['pool'], D, s['seed'])).pin_memory()
+    som = dg.SOM_Batch(s['m'], s['n'], D, topology='square')
+    som.init_rand(seed=s['seed'])
+    som.bmu_algo = args.algo
+    som.train(pool[:500_000].numpy(), n_epochs=3)
+    algo_used = 'tc' if _native.lib().somgb_algo_supported(_native.ALGO_TC, s['pool'], M, D) and \
+        args.algo != 'fp32' else 'fp32'
+    rng = np.random.default_rng(s['seed'])
+    n_req = max(1, int(rng.poisson(args.serve_rate * args.serve_seconds)))
+    arrivals = np.sort(rng.uniform(0.0, args.serve_seconds, n_req))
+    sizes = np.exp(rng.uniform(np.log(s['lo']), np.log(s['hi']), n_req)).astype(np.int64)
+    starts = rng.integers(0, s['pool'] - sizes + 1)
+    with SomServer(max_batch_rows=1 << 20) as srv:
+        mid = srv.add_map(som)
+        # warm-up: every request shape class once (library state, pinned staging buffers)
+        for n in (1_000, 100_000, 2_000_000):
+            srv.submit_bmu(mid, pool[:n]).result()
+        futs = [None] * n_req
+        t0 = time.perf_counter()
+
+        def feeder():
+            for i in range(n_req):
+                delay = t0 + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                futs[i] = srv.submit_bmu(mid, pool[starts[i]:starts[i] + sizes[i]])
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        for f in futs:
+            f.result()
+        t_end = time.perf_counter()
+    # latencies of the timed requests only (the warm-up requests completed first)
+    lat = np.asarray(srv.latencies('bmu')[3:]) * 1e3
+    rows = int(sizes.sum())
+    wall = t_end - t0
+    out = {
+        'metric': 'BMU-serve latency p99', 'value': float(np.percentile(lat, 99)), 'unit': 'ms',
+        'higher_is_better': False, 'n_gpus': 1, 'p50_ms': float(np.percentile(lat, 50)),
+        'p99_ms': float(np.percentile(lat, 99)), 'mean_ms': float(lat.mean()), 'requests': n_req,
+        'rows': rows, 'wall_s': wall,
+        'throughput': {'value': rows * M / wall / 1e9, 'unit': UNIT},
+        'offered': {'requests_per_s': args.serve_rate, 'sample_units_per_s': rows * M / args.serve_seconds / 1e9,
+                    'unit': UNIT},
+        'passes': len(srv.batch_sizes()), 'dtype': 'f16x3-split/f32acc' if algo_used == 'tc' else 'f32',
+        'data': 'synthetic (seeded 5-component Gaussian mixture, D = 16); requests are slices of a pinned 1e7-row '
+                'catalogue', 'config': {'workload': s['name'], 'algo': algo_used, 'rate': args.serve_rate,
+                                         'window_s': args.serve_seconds, 'max_batch_rows': 1 << 20},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
+    if args.serve:
+        if rank == 0:
+            serve_arm(args)
+        return
     if args.impl == 'reference':
         reference_arm(args, ws, rank)
     else:

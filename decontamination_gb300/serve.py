@@ -1,0 +1,336 @@
+"""Serving loop: BMU-assignment, activation-map, error and training requests on one GPU.
+
+The reference has no server; its callers (``Decontamination_SOM``, ``HypParamFinder_SOM``) call ``get_winners``,
+``get_activation_map``, ``compute_errors`` and ``SOM_Batch.train`` one after another. ``SomServer`` takes the same
+requests as they arrive, from any thread, and returns futures:
+
+* maps are registered once (``add_map``) and stay resident on the device;
+* requests are admitted in arrival order when their device-memory footprint (catalogue, outputs, workspace) fits the
+  budget; a request that can never fit is rejected with ``MemoryError``;
+* consecutive small BMU-assignment requests on the same map are packed into one pinned host buffer and served by one
+  upload, one BMU pass and one download;
+* activation-map and error requests run one at a time on the serving stream; training requests run on their own
+  thread and stream, so that a long training does not hold up assignments;
+* a request whose computation raises fails alone: its future carries the exception and the loop goes on;
+* latency (submit to result on the host) is recorded per kind; ``stats()`` gives count, p50 and p99.
+"""
+
+import collections
+import concurrent.futures
+import threading
+import time
+
+import numpy as np
+
+__all__ = ['SomServer', 'GpuExecutor']
+
+KINDS = ('bmu', 'activation', 'errors', 'train')
+
+
+class _Request:
+    __slots__ = ('kind', 'map_id', 'x', 'rho', 'n', 'footprint', 'future', 't_submit', 'kwargs')
+
+    def __init__(self, kind, map_id, x, rho, n, footprint, kwargs=None):
+        self.kind, self.map_id, self.x, self.rho, self.n = kind, map_id, x, rho, n
+        self.footprint = int(footprint)
+        self.future = concurrent.futures.Future()
+        self.t_submit = time.perf_counter()
+        self.kwargs = kwargs or {}
+
+
+def _rows(x):
+    return int(x.shape[0])
+
+
+class GpuExecutor:
+    """Runs the requests through libsomgb on a CUDA device (float32 maps)."""
+
+    def __init__(self, device=None):
+        import torch
+        from . import _device, _native
+        self._torch, self._dev_mod, self._nat = torch, _device, _native
+        self.device = device if device is not None else _device.require_cuda()
+        self.stream = torch.cuda.Stream(device=self.device)
+        self.train_stream = torch.cuda.Stream(device=self.device)
+        self._stage = None      # pinned host staging buffer for packed requests
+        self._out = None        # pinned host buffer for packed results
+
+    def free_bytes(self):
+        free, _ = self._torch.cuda.mem_get_info(self.device)
+        return int(free)
+
+    # --- resident maps -------------------------------------------------------------------------------------------------
+    def load(self, som):
+        """Resident copy of `som`: its weights on the device and a private map object (own workspace), so that later
+        changes to `som`, or calls on it from other threads, do not touch what the server uses."""
+        from .som_abstract import SOM_Abstract
+        if som.dtype != np.float32:
+            raise TypeError('the serving loop holds float32 maps')
+        own = SOM_Abstract(som.m, som.n, som.dim, som.dtype, som.topology)
+        own._weights[...] = som._weights
+        own.bmu_algo = som.bmu_algo
+        torch = self._torch
+        with torch.cuda.stream(self.stream):
+            w = torch.from_numpy(np.ascontiguousarray(own.weights.reshape(-1, own.dim))).to(self.device)
+        self.stream.synchronize()
+        return {'som': own, 'w': w, 'M': own.m * own.n, 'D': own.dim, 'algo': own._algo,
+                'ws': self._dev_mod.Workspace()}
+
+    def footprint(self, entry, kind, n, weighted):
+        nat = self._nat
+        M, D = entry['M'], entry['D']
+        op = {'bmu': nat.OP_FIND_BMUS, 'activation': nat.OP_COUNT_BMUS, 'errors': nat.OP_ERRORS}[kind]
+        b = n * D * 4 + n * 4 + (n * 8 if weighted else 0)
+        return b + nat.workspace_bytes(op, max(n, 1), M, D, entry['algo'])
+
+    # --- requests ------------------------------------------------------------------------------------------------------
+    def _pinned(self, attr, nbytes):
+        torch = self._torch
+        buf = getattr(self, attr)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8).pin_memory()
+            setattr(self, attr, buf)
+        return buf
+
+    def run_bmu(self, entry, xs):
+        """BMUs of every request in `xs` (host arrays or device tensors), packed into one pass."""
+        torch, nat = self._torch, self._nat
+        M, D = entry['M'], entry['D']
+        counts = [_rows(x) for x in xs]
+        n = sum(counts)
+        with torch.cuda.stream(self.stream):
+            one = xs[0] if len(xs) == 1 and isinstance(xs[0], torch.Tensor) else None
+            if one is not None and (one.is_cuda or one.is_pinned()):
+                # device tensor, or pinned host memory: no staging copy
+                xd = one.to(device=self.device, dtype=torch.float32, non_blocking=True).contiguous()
+            else:
+                stage = self._pinned('_stage', n * D * 4)
+                host = stage[:n * D * 4].view(torch.float32).view(n, D)
+                hv = host.numpy()
+                r = 0
+                for x, c in zip(xs, counts):
+                    hv[r:r + c] = x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x, dtype=np.float32)
+                    r += c
+                xd = host.to(self.device, non_blocking=True)
+            out = torch.empty(n, dtype=torch.int32, device=self.device)
+            if n:
+                wsp, wsb = entry['ws'].for_op(nat.OP_FIND_BMUS, n, M, D, entry['algo'], self.device)
+                nat.call('somgb_find_bmus', xd.data_ptr(), n, D, entry['w'].data_ptr(), M, entry['algo'],
+                         out.data_ptr(), wsp, wsb, self.stream.cuda_stream)
+            ob = self._pinned('_out', n * 4)
+            oh = ob[:n * 4].view(torch.int32)
+            oh.copy_(out, non_blocking=True)
+        self.stream.synchronize()
+        res = oh.numpy().copy()
+        parts, r = [], 0
+        for c in counts:
+            parts.append(res[r:r + c])
+            r += c
+        return parts
+
+    def run_activation(self, entry, x, rho):
+        with self._torch.cuda.stream(self.stream):
+            return entry['som'].get_activation_map(x, rho)
+
+    def run_errors(self, entry, x, rho):
+        with self._torch.cuda.stream(self.stream):
+            return entry['som'].compute_errors(x, rho)
+
+    def run_train(self, som, dataset, rho, kwargs):
+        with self._torch.cuda.stream(self.train_stream):
+            som.train(dataset, rho, **kwargs)
+        return som
+
+
+class SomServer:
+    """Request loop over resident maps (see the module docstring).
+
+    executor: the object that runs requests (default: ``GpuExecutor`` on the current CUDA device).
+    hbm_budget: device bytes that admitted requests may hold at once (default: 80 % of the free memory at start).
+    max_batch_rows: BMU requests with at most this many rows are packed together, up to this many rows per pass.
+    """
+
+    def __init__(self, executor=None, hbm_budget=None, max_batch_rows=1 << 20):
+        self._ex = executor if executor is not None else GpuExecutor()
+        self.hbm_budget = int(hbm_budget if hbm_budget is not None else 0.8 * self._ex.free_bytes())
+        self.max_batch_rows = int(max_batch_rows)
+        self._maps = {}
+        self._queue = collections.deque()
+        self._train_queue = collections.deque()
+        self._cv = threading.Condition()
+        self._in_flight = 0
+        self._closing = False
+        self._lat = {k: [] for k in KINDS}
+        self._batches = []
+        self._threads = [threading.Thread(target=self._serve_loop, name='somgb-serve', daemon=True),
+                         threading.Thread(target=self._train_loop, name='somgb-train', daemon=True)]
+        for t in self._threads:
+            t.start()
+
+    # --- public API ----------------------------------------------------------------------------------------------------
+    def add_map(self, som):
+        """Registers `som` (its current weights) as a resident map; returns its id."""
+        entry = self._ex.load(som)
+        with self._cv:
+            mid = len(self._maps)
+            self._maps[mid] = entry
+        return mid
+
+    def submit_bmu(self, map_id, x):
+        """Future of the int32 BMU of every row of `x` (``get_winners``)."""
+        return self._submit('bmu', map_id, x, None)
+
+    def submit_activation(self, map_id, x, rho=None):
+        """Future of the activation map of `x` (``get_activation_map``)."""
+        return self._submit('activation', map_id, x, rho)
+
+    def submit_errors(self, map_id, x, rho=None):
+        """Future of (QE, TE) of `x` (``compute_errors``)."""
+        return self._submit('errors', map_id, x, rho)
+
+    def submit_train(self, som, dataset, dataset_weights=None, **train_kwargs):
+        """Future of `som` after ``som.train(dataset, dataset_weights, **train_kwargs)`` (runs on its own stream)."""
+        n = _rows(dataset) if hasattr(dataset, 'shape') else 0
+        fp = n * som.dim * 4 * 2 + som.m * som.n * som.dim * 8 * 4
+        req = _Request('train', None, dataset, dataset_weights, n, fp, train_kwargs)
+        req.x = (som, dataset)
+        with self._cv:
+            self._check_open()
+            if req.footprint > self.hbm_budget:
+                req.future.set_exception(MemoryError(f'training request needs {req.footprint} device bytes, '
+                                                     f'over the {self.hbm_budget}-byte budget'))
+                return req.future
+            self._train_queue.append(req)
+            self._cv.notify_all()
+        return req.future
+
+    def stats(self):
+        """Per kind: number of completed requests and their p50 / p99 latency in milliseconds."""
+        with self._cv:
+            out = {}
+            for k, v in self._lat.items():
+                if v:
+                    a = np.asarray(v) * 1e3
+                    out[k] = {'count': len(v), 'p50_ms': float(np.percentile(a, 50)),
+                              'p99_ms': float(np.percentile(a, 99))}
+            return out
+
+    def latencies(self, kind):
+        """Latencies (seconds, completion order) of the completed requests of `kind`."""
+        with self._cv:
+            return list(self._lat[kind])
+
+    def batch_sizes(self):
+        """Requests packed into each BMU pass so far."""
+        with self._cv:
+            return list(self._batches)
+
+    def close(self, wait=True):
+        """Stops accepting requests; with `wait`, serves what is queued and joins the loops."""
+        with self._cv:
+            self._closing = True
+            self._cv.notify_all()
+        if wait:
+            for t in self._threads:
+                t.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # --- internals -----------------------------------------------------------------------------------------------------
+    def _check_open(self):
+        if self._closing:
+            raise RuntimeError('the server is closed')
+
+    def _submit(self, kind, map_id, x, rho):
+        n = _rows(x)
+        with self._cv:
+            self._check_open()
+            if map_id not in self._maps:
+                raise KeyError(f'unknown map {map_id}')
+            entry = self._maps[map_id]
+        req = _Request(kind, map_id, x, rho, n, self._ex.footprint(entry, kind, n, rho is not None))
+        with self._cv:
+            if req.footprint > self.hbm_budget:
+                req.future.set_exception(MemoryError(f'request needs {req.footprint} device bytes, over the '
+                                                     f'{self.hbm_budget}-byte budget'))
+                return req.future
+            self._queue.append(req)
+            self._cv.notify_all()
+        return req.future
+
+    def _admit(self, q):
+        """Pops the next batch from `q` once its footprint fits the budget (lock held); None when closing and empty."""
+        while True:
+            if q:
+                head = q[0]
+                if self._in_flight + head.footprint <= self.hbm_budget:
+                    batch = [q.popleft()]
+                    total_rows, total_fp = head.n, head.footprint
+                    if head.kind == 'bmu' and head.n <= self.max_batch_rows:
+                        while q and q[0].kind == 'bmu' and q[0].map_id == head.map_id and \
+                                total_rows + q[0].n <= self.max_batch_rows and \
+                                self._in_flight + total_fp + q[0].footprint <= self.hbm_budget:
+                            nxt = q.popleft()
+                            batch.append(nxt)
+                            total_rows += nxt.n
+                            total_fp += nxt.footprint
+                    self._in_flight += total_fp
+                    return batch, total_fp
+            elif self._closing:
+                return None, 0
+            self._cv.wait(0.05)
+
+    def _finish(self, batch, fp, results=None, exc=None):
+        t = time.perf_counter()
+        for i, req in enumerate(batch):
+            if exc is not None:
+                req.future.set_exception(exc)
+            else:
+                req.future.set_result(results[i])
+        with self._cv:
+            self._in_flight -= fp
+            if exc is None:
+                for req in batch:
+                    self._lat[req.kind].append(t - req.t_submit)
+            self._cv.notify_all()
+
+    def _serve_loop(self):
+        while True:
+            with self._cv:
+                batch, fp = self._admit(self._queue)
+            if batch is None:
+                return
+            head = batch[0]
+            try:
+                entry = self._maps[head.map_id]
+                if head.kind == 'bmu':
+                    res = self._ex.run_bmu(entry, [r.x for r in batch])
+                    with self._cv:
+                        self._batches.append(len(batch))
+                elif head.kind == 'activation':
+                    res = [self._ex.run_activation(entry, head.x, head.rho)]
+                else:
+                    res = [self._ex.run_errors(entry, head.x, head.rho)]
+            except Exception as e:   # the request fails alone
+                self._finish(batch, fp, exc=e)
+                continue
+            self._finish(batch, fp, results=res)
+
+    def _train_loop(self):
+        while True:
+            with self._cv:
+                batch, fp = self._admit(self._train_queue)
+            if batch is None:
+                return
+            req = batch[0]
+            som, dataset = req.x
+            try:
+                res = self._ex.run_train(som, dataset, req.rho, req.kwargs)
+            except Exception as e:
+                self._finish(batch, fp, exc=e)
+                continue
+            self._finish(batch, fp, results=[res])

@@ -1,0 +1,197 @@
+"""The serving loop: queueing, packing, admission and failure isolation on CPU with a fake executor; results against
+the direct API calls on the GPU."""
+
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from decontamination_gb300.serve import SomServer
+
+
+class FakeExecutor:
+    """Records the batches it is given; BMU i of a request is its first value; a row of NaN makes a pass raise."""
+
+    def __init__(self, free=10 ** 9, block_first=False):
+        self.free = free
+        self.release = threading.Event()
+        if not block_first:
+            self.release.set()
+        self.bmu_batches = []
+        self.trained = []
+
+    def free_bytes(self):
+        return self.free
+
+    def load(self, som):
+        return {'M': 4, 'D': 2, 'name': som}
+
+    def footprint(self, entry, kind, n, weighted):
+        return 100 * n + (50 if weighted else 0)
+
+    def run_bmu(self, entry, xs):
+        self.release.wait(5)
+        self.bmu_batches.append([len(x) for x in xs])
+        for x in xs:
+            if np.isnan(np.asarray(x)).any():
+                raise ValueError('poisoned request')
+        return [np.full(len(x), int(np.asarray(x)[0, 0]), dtype=np.int32) for x in xs]
+
+    def run_activation(self, entry, x, rho):
+        return ('activation', entry['name'], len(x))
+
+    def run_errors(self, entry, x, rho):
+        return (0.5, 0.25)
+
+    def run_train(self, som, dataset, rho, kwargs):
+        time.sleep(0.05)
+        self.trained.append((som, len(dataset), kwargs))
+        return som
+
+
+def _req(v, n=10):
+    return np.full((n, 2), float(v), dtype=np.float32)
+
+
+def test_small_requests_on_one_map_are_packed():
+    ex = FakeExecutor(block_first=True)
+    srv = SomServer(ex, max_batch_rows=1000)
+    m0, m1 = srv.add_map('a'), srv.add_map('b')
+    first = srv.submit_bmu(m0, _req(0))
+    time.sleep(0.1)   # the loop now holds the first request inside the executor
+    futs = [srv.submit_bmu(m0, _req(i)) for i in range(1, 6)] + [srv.submit_bmu(m1, _req(9))] + \
+           [srv.submit_bmu(m0, _req(7))]
+    ex.release.set()
+    assert first.result(5)[0] == 0
+    got = [f.result(5) for f in futs]
+    assert [g[0] for g in got] == [1, 2, 3, 4, 5, 9, 7]
+    srv.close()
+    # the five queued requests on map 0 share a pass; the map-1 request breaks the run
+    assert ex.bmu_batches == [[10], [10] * 5, [10], [10]]
+    assert srv.batch_sizes() == [1, 5, 1, 1]
+
+
+def test_row_cap_splits_packs():
+    ex = FakeExecutor(block_first=True)
+    srv = SomServer(ex, max_batch_rows=100)
+    m = srv.add_map('a')
+    f0 = srv.submit_bmu(m, _req(0, 40))
+    time.sleep(0.1)
+    futs = [srv.submit_bmu(m, _req(i, 40)) for i in range(5)]
+    ex.release.set()
+    f0.result(5)
+    for f in futs:
+        assert len(f.result(5)) == 40
+    srv.close()
+    assert ex.bmu_batches == [[40], [40, 40], [40, 40], [40]]
+    # a request above the cap is served alone
+    ex2 = FakeExecutor()
+    with SomServer(ex2, max_batch_rows=100) as srv2:
+        assert len(srv2.submit_bmu(srv2.add_map('a'), _req(3, 150)).result(5)) == 150
+    assert ex2.bmu_batches == [[150]]
+
+
+def test_admission_rejects_what_can_never_fit_and_serves_the_rest():
+    ex = FakeExecutor()
+    with SomServer(ex, hbm_budget=5000) as srv:
+        m = srv.add_map('a')
+        big = srv.submit_bmu(m, _req(1, 60))       # 6000 bytes > budget
+        small = srv.submit_bmu(m, _req(2, 10))
+        with pytest.raises(MemoryError):
+            big.result(5)
+        assert small.result(5)[0] == 2
+
+
+def test_a_failing_request_fails_alone():
+    ex = FakeExecutor(block_first=True)
+    srv = SomServer(ex, max_batch_rows=10)
+    m = srv.add_map('a')
+    f0 = srv.submit_bmu(m, _req(0))
+    time.sleep(0.1)
+    bad = np.full((10, 2), np.nan, dtype=np.float32)
+    fb = srv.submit_bmu(m, bad)
+    f1 = srv.submit_bmu(m, _req(1))
+    ex.release.set()
+    assert f0.result(5)[0] == 0
+    with pytest.raises(ValueError):
+        fb.result(5)
+    assert f1.result(5)[0] == 1
+    srv.close()
+    assert 'bmu' in srv.stats() and srv.stats()['bmu']['count'] == 2
+
+
+def test_other_kinds_training_and_stats():
+    ex = FakeExecutor()
+    with SomServer(ex) as srv:
+        m = srv.add_map('a')
+        fa = srv.submit_activation(m, _req(0, 7))
+        fe = srv.submit_errors(m, _req(0, 7), rho=np.ones(7))
+        assert fa.result(5) == ('activation', 'a', 7)
+        assert fe.result(5) == (0.5, 0.25)
+    st = srv.stats()
+    assert st['activation']['count'] == 1 and st['errors']['count'] == 1
+    assert st['errors']['p99_ms'] >= st['errors']['p50_ms'] >= 0.0
+    with pytest.raises(RuntimeError):
+        srv.submit_bmu(m, _req(0))
+
+
+class _Som:
+    dim, m, n = 2, 2, 2
+
+
+def test_training_runs_on_its_own_loop_while_assignments_continue():
+    ex = FakeExecutor()
+    with SomServer(ex) as srv:
+        m = srv.add_map('a')
+        ft = srv.submit_train(_Som(), _req(0, 12), n_epochs=3)
+        fb = srv.submit_bmu(m, _req(4))
+        assert fb.result(5)[0] == 4
+        assert isinstance(ft.result(5), _Som)
+    assert ex.trained[0][1:] == (12, {'n_epochs': 3})
+    assert srv.stats()['train']['count'] == 1
+
+
+def test_close_serves_what_is_queued():
+    ex = FakeExecutor(block_first=True)
+    srv = SomServer(ex)
+    m = srv.add_map('a')
+    futs = [srv.submit_bmu(m, _req(i)) for i in range(4)]
+    t = threading.Thread(target=srv.close)
+    t.start()
+    time.sleep(0.05)
+    ex.release.set()
+    t.join(5)
+    assert [f.result(0)[0] for f in futs] == [0, 1, 2, 3]
+
+
+@pytest.mark.gpu
+def test_served_results_match_the_direct_calls(cuda):
+    import decontamination_gb300 as dg
+    from decontamination_gb300 import synthetic
+    x = synthetic.gaussian_mixture(300_000, 16, 4)
+    som = dg.SOM_Batch(16, 16, 16, topology='hexagonal')
+    som._weights[...] = x[np.random.default_rng(1).integers(0, len(x), 256)].reshape(som._weights.shape)
+    rho = np.random.default_rng(2).random(len(x))
+    sizes = [1000, 37, 250_000, 5000, 20_000, 1]
+    parts, r = [], 0
+    for s in sizes:
+        parts.append(np.ascontiguousarray(x[r:r + s]))
+        r += s
+    with SomServer(max_batch_rows=1 << 16) as srv:
+        mid = srv.add_map(som)
+        fb = [srv.submit_bmu(mid, p) for p in parts]
+        fa = srv.submit_activation(mid, x, rho)
+        fe = srv.submit_errors(mid, x)
+        for p, f in zip(parts, fb):
+            assert np.array_equal(f.result(120), som.get_winners(p))
+        assert np.array_equal(fa.result(120), som.get_activation_map(x, rho))
+        np.testing.assert_allclose(fe.result(120), som.compute_errors(x), rtol=1e-12)
+        # a training request gives the same map as training directly
+        a = dg.SOM_Batch(8, 8, 16, topology='square')
+        b = dg.SOM_Batch(8, 8, 16, topology='square')
+        a.init_rand(seed=3)
+        b.init_rand(seed=3)
+        ft = srv.submit_train(a, x[:50_000], n_epochs=3)
+        b.train(x[:50_000], n_epochs=3)
+        assert np.array_equal(ft.result(120).weights, b.weights)
