@@ -42,7 +42,6 @@
 
 #include <algorithm>
 #include <mutex>
-#include <type_traits>
 
 #include "tc.cuh"
 #include "tc_ptx.cuh"
@@ -81,7 +80,8 @@ constexpr int TN = 256;           // units per column tile (MMA N)
 constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
 constexpr int CAPR = 24;          // candidates a resolver keeps per row (unit indices as uint16)
 constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
-constexpr int MAX_U = 8;          // column tiles per row tile (the candidate summary is a 32-bit word per half)
+constexpr int MAX_U = 16;         // column tiles per row tile (candidate summaries: 32-bit words of 8 tiles per half)
+constexpr int NBARS = 40;         // mbarrier slots
 constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
 constexpr int RES_WARPS = 4;
@@ -122,10 +122,34 @@ struct TcShape {
     int d = 0, kpad = 0, knz = 0;
     int64_t mpad = 0;
     int utiles = 0;
-    size_t b_bytes = 0, a_bytes = 0, x_bytes = 0;
+    int bstages = 0;   // 0: the whole unit operand resident in shared memory; else a ring of this many column tiles
+    size_t b_bytes = 0, b_tile = 0, a_bytes = 0, x_bytes = 0;
     size_t off_a = 0, off_x = 0, off_mask = 0, off_sum = 0, off_flag = 0, off_rlist = 0, off_part = 0, off_center = 0,
            off_bar = 0, off_w = 0, smem = 0;
 };
+
+// Layout after a unit-operand region of `bregion` bytes; returns the end offset (before the unit rows).
+size_t tc_layout(TcShape& s, size_t bregion) {
+    size_t off = align_up(bregion, 1024);
+    s.off_a = off;
+    off += 2 * align_up(s.a_bytes, 1024);
+    s.off_x = off;
+    off += XSTAGES * s.x_bytes;
+    s.off_mask = off;
+    off += (size_t)HALVES * s.utiles * 4 * TM * 4;
+    s.off_sum = off;
+    off += (size_t)2 * HALVES * TM * 4;
+    s.off_flag = off;
+    off += TM;
+    s.off_rlist = off;
+    off += (size_t)(CAPR + 1) * TM * 2;
+    s.off_part = off;
+    off += (size_t)HALVES * TM * 8;
+    s.off_center = off;
+    off += align_up((size_t)(s.d + 1) * 4, 16);
+    s.off_bar = align_up(off, 8);
+    return s.off_bar + NBARS * 8;
+}
 
 TcShape tc_shape(int64_t m, int d) {
     TcShape s;
@@ -135,27 +159,18 @@ TcShape tc_shape(int64_t m, int d) {
     s.mpad = (int64_t)align_up((size_t)m, TN);
     s.utiles = (int)(s.mpad / TN);
     s.b_bytes = (size_t)s.mpad * s.kpad * 2;
+    s.b_tile = (size_t)TN * s.kpad * 2;
     s.a_bytes = (size_t)TM * s.kpad * 2;
     s.x_bytes = align_up((size_t)TM * d * 4, 128);
-    size_t off = align_up(s.b_bytes, 1024);
-    s.off_a = off;
-    off += 2 * align_up(s.a_bytes, 1024);
-    s.off_x = off;
-    off += XSTAGES * s.x_bytes;
-    s.off_mask = off;
-    off += (size_t)HALVES * s.utiles * 4 * TM * 4;
-    s.off_sum = off;
-    off += (size_t)HALVES * TM * 4;
-    s.off_flag = off;
-    off += TM;
-    s.off_rlist = off;
-    off += (size_t)(CAPR + 1) * TM * 2;
-    s.off_part = off;
-    off += (size_t)HALVES * TM * 8;
-    s.off_center = off;
-    off += align_up((size_t)(d + 1) * 4, 16);
-    s.off_bar = align_up(off, 8);
-    off = s.off_bar + 32 * 8;
+    // the whole unit operand when it fits, else a ring of 3 (or 2) column tiles streamed from L2 by the TMA warp
+    size_t off = tc_layout(s, s.b_bytes);
+    if (off + 128 > SMEM_LIMIT) {
+        for (int st = 3; st >= 2; --st) {
+            s.bstages = st;
+            off = tc_layout(s, (size_t)st * align_up(s.b_tile, 1024));
+            if (off + 128 <= SMEM_LIMIT) break;
+        }
+    }
     // the float32 unit rows, for the resolvers' candidate distances, when they fit (otherwise read from L2)
     const size_t w_bytes = (size_t)m * d * 4;
     const size_t off_w = align_up(off, 16);
@@ -317,6 +332,8 @@ struct TcArgs {
     float alpha, beta;
     size_t off_a, off_x, off_mask, off_sum, off_flag, off_rlist, off_part, off_center, off_bar, off_w, a_stride, x_stride;
     uint32_t b_bytes;
+    uint32_t b_tile;         // bytes of one column tile of the unit operand
+    int bstages;             // 0: resident unit operand; else the ring depth
 };
 
 // float32 distance over the reference's float32 differences (FMA chain): |df - d_ref| <= (D+2) 2^-24 d_ref
@@ -403,14 +420,17 @@ __device__ __forceinline__ DFloat ref_dist_pair(const float* __restrict__ wr, co
     return DFloat{acc.hi, acc.lo};
 }
 
-template <bool ERR, int DT>
+// LARGE: the unit operand streams through a ring (more than fits in shared memory) or the map has more than 8 column
+// tiles; the other instantiations (resident operand, at most 8 column tiles) carry none of that logic.
+template <bool ERR, int DT, bool LARGE>
 __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs P) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
     uint32_t* sMask = (uint32_t*)(smem + P.off_mask);   // [half][u][4][TM]: bit 31-i of word w: column 32w+i is a candidate
-    uint32_t* sSum = (uint32_t*)(smem + P.off_sum);     // [half][TM]: bit 4u+w set when mask word (u, w) is non-zero
+    uint32_t* sSum = (uint32_t*)(smem + P.off_sum);     // [u / 8][half][TM]: bit 4(u%8)+w set when mask word (u, w) is
+                                                        // non-zero (the second pair only for more than 8 column tiles)
     uint8_t* sFlag = smem + P.off_flag;                 // [TM]: the row goes to the exact recheck
     uint16_t* sList = (uint16_t*)(smem + P.off_rlist);  // [CAPR + 1][TM]: the resolvers' candidate lists (+ scratch)
     float2* sPart = (float2*)(smem + P.off_part);       // [half][TM]: (m1, m2) of the half
@@ -426,6 +446,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint64_t* m_empty = bars + 16;  // the resolvers have read them
     uint64_t* drain = bars + 19;
     uint64_t* p_full = bars + 20;   // [2][4]: both halves of a lane quarter have published (m1, m2)
+    uint64_t* bs_full = bars + 28;  // [3]: a column tile of the unit operand has landed (streamed operand)
+    uint64_t* bs_empty = bars + 31; // [3]: the MMAs reading it have completed
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_s;
 
@@ -439,6 +461,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
     if (tid == 0) {
         ptx::mbar_init(b_full, 1);
+        for (int s = 0; s < 3; ++s) {
+            ptx::mbar_init(bs_full + s, 1);
+            ptx::mbar_init(bs_empty + s, 1);
+        }
         for (int s = 0; s < XSTAGES; ++s) {
             ptx::mbar_init(x_full + s, 1);
             ptx::mbar_init(x_empty + s, SWEEP_WARPS);
@@ -484,37 +510,73 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     if (warp == TMA_WARP) {
         if (lane == 0 && n_my > 0) {
             ptx::prefetch_tensormap(&tmap);
-            ptx::mbar_arrive_expect_tx(b_full, P.b_bytes);
-            for (uint32_t off = 0; off < P.b_bytes; off += 32768u) {
-                const uint32_t len = P.b_bytes - off < 32768u ? P.b_bytes - off : 32768u;
-                ptx::bulk_g2s(sB + off, P.b + off, len, b_full);
+            const int BST = LARGE ? P.bstages : 0;
+            if (BST == 0) {
+                ptx::mbar_arrive_expect_tx(b_full, P.b_bytes);
+                for (uint32_t off = 0; off < P.b_bytes; off += 32768u) {
+                    const uint32_t len = P.b_bytes - off < 32768u ? P.b_bytes - off : 32768u;
+                    ptx::bulk_g2s(sB + off, P.b + off, len, b_full);
+                }
             }
-            int64_t issued = 0;
-            for (int64_t it = 0; it < n_my && !*abort_v; ++it) {
+            const uint32_t b_stride = (P.b_tile + 1023u) & ~1023u;
+            int64_t issued = 0, kb = 0;
+            bool ok = true;
+            auto issue_x = [&](int64_t it) -> bool {
                 const int s = (int)(it % XSTAGES);
                 if (it >= XSTAGES && !ptx::mbar_wait(x_empty + s, (uint32_t)((it / XSTAGES - 1) & 1))) {
                     fail(1u);
-                    break;
+                    return false;
                 }
                 const int64_t t = blockIdx.x + it * gridDim.x;
                 ptx::mbar_arrive_expect_tx(x_full + s, (uint32_t)(TM * d * 4));
                 ptx::tma_load_2d(smem + P.off_x + s * P.x_stride, &tmap, 0, (int32_t)(t * TM), x_full + s);
                 issued = it + 1;
+                return true;
+            };
+            if (BST == 0) {
+                for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) ok = issue_x(it);
+            } else {
+                // sample tiles one row tile ahead of the unit-operand tiles, which go in the MMAs' order
+                for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
+                    while (ok && issued < n_my && issued <= it + 1) ok = issue_x(issued);
+                    for (int sweep = 0; ok && sweep < 2; ++sweep) {
+                        for (int u = 0; u < U && !*abort_v; ++u, ++kb) {
+                            const int st = (int)(kb % BST);
+                            if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BST - 1) & 1))) {
+                                fail(4096u);
+                                ok = false;
+                                break;
+                            }
+                            ptx::mbar_arrive_expect_tx(bs_full + st, P.b_tile);
+                            const uint8_t* src = P.b + (size_t)u * P.b_tile;
+                            for (uint32_t off = 0; off < P.b_tile; off += 32768u) {
+                                const uint32_t len = P.b_tile - off < 32768u ? P.b_tile - off : 32768u;
+                                ptx::bulk_g2s(sB + (size_t)st * b_stride + off, src + off, len, bs_full + st);
+                            }
+                        }
+                    }
+                }
             }
-            if (*abort_v) {
+            if (*abort_v || !ok) {
                 // let the copies still in flight land before the CTA releases its shared memory
-                ptx::mbar_wait(b_full, 0);
+                if (BST == 0) ptx::mbar_wait(b_full, 0);
                 for (int64_t k = issued > XSTAGES ? issued - XSTAGES : 0; k < issued; ++k)
                     ptx::mbar_wait(x_full + (int)(k % XSTAGES), (uint32_t)((k / XSTAGES) & 1));
+                for (int64_t k = kb > BST ? kb - BST : 0; BST > 0 && k < kb; ++k)
+                    ptx::mbar_wait(bs_full + (int)(k % BST), (uint32_t)((k / BST) & 1));
             }
         }
     } else if (warp == MMA_WARP) {
         if (lane == 0 && n_my > 0) {
-            bool ok = ptx::mbar_wait(b_full, 0);
+            const int BST = LARGE ? P.bstages : 0;
+            bool ok = BST > 0 || ptx::mbar_wait(b_full, 0);
             if (!ok) fail(2u);
             const uint32_t sbo = (uint32_t)(kpad / 8) * 128u;
             const uint32_t b_addr = ptx::smem_u32(sB);
+            const uint32_t b_stride = (P.b_tile + 1023u) & ~1023u;
             int64_t g = 0;
+            int bst = 0;              // ring stage of the next streamed column tile, and the parity of its use
+            uint32_t bpar = 0;
             for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
                 const int s = (int)(it & 1);
                 if (!ptx::mbar_wait(a_full + s, (uint32_t)((it >> 1) & 1))) { fail(4u); break; }
@@ -528,9 +590,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                             ok = false;
                             break;
                         }
+                        if (LARGE && BST > 0 && !ptx::mbar_wait(bs_full + bst, bpar)) {
+                            fail(8192u);
+                            ok = false;
+                            break;
+                        }
                         ptx::tc_fence_after();
                         const uint32_t dt = tbase + (uint32_t)(buf * TN);
-                        const uint32_t bu = b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
+                        const uint32_t bu = (LARGE && BST > 0) ? b_addr + (uint32_t)bst * b_stride
+                                                               : b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
 #pragma unroll
                         for (int ks = 0; ks < k_steps(DT); ++ks) {
                             int ka, kb;
@@ -540,6 +608,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                             ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
                         }
                         ptx::mma_commit(t_full + buf);
+                        if (LARGE && BST > 0) {
+                            ptx::mma_commit(bs_empty + bst);   // the stage is free once these MMAs have completed
+                            if (++bst == BST) {
+                                bst = 0;
+                                bpar ^= 1u;
+                            }
+                        }
                     }
                 }
                 ptx::mma_commit(a_empty + s);
@@ -709,7 +784,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
             // floats never rounds to zero), so each value costs one subtraction and one shift-or of its sign bit.
             const float thr_up = nextafterf(thr, INFINITY);
-            uint32_t summary = 0;
+            uint32_t summary = 0, summary_hi = 0;   // column tiles 0-7 and 8-15
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
@@ -719,12 +794,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
                     const uint32_t mw = sign_mask32(r, thr_up);
                     mrow[c * TM] = mw;
-                    summary |= (mw != 0u ? 1u : 0u) << (u * 4 + c);
+                    if (LARGE) {
+                        const uint32_t bit = (mw != 0u ? 1u : 0u) << ((u & 7) * 4 + c);
+                        if (u < 8) summary |= bit;
+                        else summary_hi |= bit;
+                    } else {
+                        summary |= (mw != 0u ? 1u : 0u) << (u * 4 + c);
+                    }
                 });
                 TC_T(3);
             }
             if (!ok) break;
             sSum[h * TM + row] = flagged ? 0u : summary;
+            if (LARGE && U > 8) sSum[(HALVES + h) * TM + row] = flagged ? 0u : summary_hi;
             if (h == 0) sFlag[row] = flagged ? 1 : 0;
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(m_full);
@@ -758,25 +840,31 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             // candidate list of the row from the two halves' masks: one candidate per lane and iteration, the next
             // non-zero mask word (from the summary bits) fetched in the same iteration; no divergent branches
             const bool flagged = sFlag[row] != 0;
-            uint64_t S = flagged ? 0ull : ((uint64_t)sSum[row] | ((uint64_t)sSum[TM + row] << 32));
-            uint32_t word = 0;
-            int jtop = 0, cnt = 0;
-            bool more = S != 0ull;
-            while (__any_sync(0xffffffffu, more)) {
-                const bool need = word == 0u;
-                const int b = __ffsll((long long)S) - 1;
-                const int bb = b < 0 ? 0 : b;
-                const int hh = bb >> 5, ub = (bb & 31) >> 2, wb = bb & 3;
-                const uint32_t nw = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
-                word = need ? (b >= 0 ? nw : 0u) : word;
-                jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
-                S = need ? (S & (S - 1ull)) : S;
-                const int j = jtop - (__ffs(word) - 1);
-                const bool take = word != 0u && j < (int)a.m;
-                word &= word - 1u;
-                list[(take && cnt < CAPR ? cnt : CAPR) * TM] = (uint16_t)j;
-                cnt += take ? 1 : 0;
-                more = word != 0u || S != 0ull;
+            int cnt = 0;
+            // column tiles 0-7, then (for more than 8) 8-15: each part's two halves fit one 64-bit word
+            const int parts = LARGE ? (U + 7) / 8 : 1;
+            for (int part = 0; part < parts; ++part) {
+                const uint32_t* ss = sSum + part * HALVES * TM;
+                uint64_t S = flagged ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
+                uint32_t word = 0;
+                int jtop = 0;
+                bool more = S != 0ull;
+                while (__any_sync(0xffffffffu, more)) {
+                    const bool need = word == 0u;
+                    const int b = __ffsll((long long)S) - 1;
+                    const int bb = b < 0 ? 0 : b;
+                    const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
+                    const uint32_t nw = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
+                    word = need ? (b >= 0 ? nw : 0u) : word;
+                    jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
+                    S = need ? (S & (S - 1ull)) : S;
+                    const int j = jtop - (__ffs(word) - 1);
+                    const bool take = word != 0u && j < (int)a.m;
+                    word &= word - 1u;
+                    list[(take && cnt < CAPR ? cnt : CAPR) * TM] = (uint16_t)j;
+                    cnt += take ? 1 : 0;
+                    more = word != 0u || S != 0ull;
+                }
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(m_empty);
@@ -908,9 +996,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
 template <bool ERR, int DT>
 int launch_main(const CUtensorMap& tmap, const TcArgs& P, unsigned grid, size_t smem, cudaStream_t stream) {
-    SOMGB_CUDA_TRY(cudaFuncSetAttribute(tc_pass_kernel<ERR, DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = (P.bstages > 0 || P.utiles > 8) ? tc_pass_kernel<ERR, DT, true> : tc_pass_kernel<ERR, DT, false>;
+    SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     timer_begin(stream);
-    tc_pass_kernel<ERR, DT><<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
+    kern<<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
     timer_end(stream);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
@@ -1044,6 +1133,8 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     P.a_stride = align_up(s.a_bytes, 1024);
     P.x_stride = s.x_bytes;
     P.b_bytes = (uint32_t)s.b_bytes;
+    P.b_tile = (uint32_t)s.b_tile;
+    P.bstages = s.bstages;
 
     const int64_t tiles = ceil_div(a.n, TM);
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());

@@ -291,6 +291,12 @@ TC_STRESS = [
     ('far-offset', 4, 20, 20, 100_000),
     ('uniform', 32, 8, 16, 60_000),
     ('duplicates', 8, 10, 10, 50_000),
+    # maps whose unit operand streams through shared memory (64x64 at D = 16 and 32), more than 8 column tiles with
+    # a resident operand (64x64 at D = 4), and 9 column tiles (48x48)
+    ('large-streamed', 16, 64, 64, 30_000),
+    ('large-streamed', 32, 64, 64, 20_000),
+    ('large-streamed', 4, 64, 64, 30_000),
+    ('large-streamed', 16, 48, 48, 30_000),
 ]
 
 
@@ -314,6 +320,9 @@ def test_tc_stress_vs_oracle(cuda, native, oracle, kind, d, m, n, N):
     elif kind == 'far-offset':
         x = (1.0e4 + rng.standard_normal((N, d))).astype(np.float32)
         w = (1.0e4 + 0.7 * rng.standard_normal((M, d))).astype(np.float32)
+    elif kind == 'large-streamed':
+        x = synthetic.correlated_lognormal(N, d, 11)
+        w = x[rng.integers(0, N, M)] * (1 + 0.02 * rng.standard_normal((M, d))).astype(np.float32)
     elif kind == 'uniform':
         x = rng.random((N, d), dtype=np.float32)
         w = rng.random((M, d), dtype=np.float32)
