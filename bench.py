@@ -36,6 +36,12 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name='hex 32x32 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=16, 20-epoch schedule',
                 m=32, n=32, d=16, N=12_582_912, topology='hexagonal', sigma0=16.0, schedule=20, seed=2)
+# the larger training configuration (square 64x64 map, D = 32, N = 50,331,648 = HEALPix nside 2048), measured with
+# --workload sq64
+WORKLOADS = {'hex32': WORKLOAD,
+             'sq64': dict(name='square 64x64 SOM, D=32, N=50331648 (HEALPix nside=2048 pixel count), sigma0=32, '
+                               '20-epoch schedule', m=64, n=64, d=32, N=50_331_648, topology='square', sigma0=32.0,
+                          schedule=20, seed=3)}
 METRIC = 'SOM epoch Gsample·unit/s'
 # DRAM traffic (bytes read + written) of one tensor-core BMU pass per catalogue row, from an ncu capture of
 # tc_pass_kernel on the 4,194,304-row case of this workload (summary under profiles/). The pass streams every row
@@ -51,7 +57,9 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--algo', default='auto', choices=['auto', 'tc', 'fp32'])
-    ap.add_argument('--n', type=int, default=WORKLOAD['N'], help='catalogue rows (default: the full workload)')
+    ap.add_argument('--workload', default='hex32', choices=sorted(WORKLOADS),
+                    help='hex32: the headline epoch (default); sq64: the 64x64, D = 32 training configuration')
+    ap.add_argument('--n', type=int, default=None, help='catalogue rows (default: the full workload)')
     ap.add_argument('--skip-cpu', action='store_true')
     ap.add_argument('--skip-e2e', action='store_true')
     ap.add_argument('--skip-fp32', action='store_true')
@@ -181,10 +189,10 @@ def cpu_epoch_rate(x, w0, w, seconds, threads=0):
 
 
 def reference_arm(args, ws, rank):
-    w = WORKLOAD
+    w = WORKLOADS[args.workload]
     if rank != 0:
         return
-    x, w0 = make_data(min(args.n, 400_000), w)
+    x, w0 = make_data(min(args.n or w['N'], 400_000), w)
     rates = []
     info = None
     for step in range(args.warmup + args.steps):
@@ -304,9 +312,9 @@ def gpu_arm(args, ws, rank, local):
     device = torch.device('cuda', local)
     if ws > 1:
         dist.init_process_group('nccl', device_id=device)
-    w = WORKLOAD
+    w = WORKLOADS[args.workload]
     M, D = w['m'] * w['n'], w['d']
-    x, w0 = make_data(args.n, w)
+    x, w0 = make_data(args.n or w['N'], w)
     N = x.shape[0]
     topo_np = dg.SOM_Batch(w['m'], w['n'], D, topology=w['topology'])._topography
     xh = torch.from_numpy(x).pin_memory()
@@ -357,7 +365,8 @@ def gpu_arm(args, ws, rank, local):
         'dtype': 'f16x3-split/f32acc' if used_algo == 'tc' else 'f32',
         'data': 'synthetic (seeded correlated log-normal, cond 100, 2% rows x10; weights U[-1,1])',
         'config': {'workload': w['name'], 'algo': used_algo, 'N_per_gpu': N, 'M': M, 'D': D,
-                   'l2': 'catalogue 805 MB > 129 MB L2 per epoch; no flush', 'parallelism': f'replicas x{ws}'},
+                   'l2': f'catalogue {N * D * 4 / 1e6:.0f} MB > 129 MB L2 per epoch; no flush',
+                   'parallelism': f'replicas x{ws}'},
         'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clocks, 'phases': phases,
         'recheck_last_epoch': int(rechecks[0]),
         'qe_last': float(errs[-1][0] / errs[-1][2]) if errs[-1][2] > 0 else None,

@@ -120,23 +120,51 @@ __device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live
     }
 
     double e0 = 0.0, e1 = 0.0, e2 = 0.0;
-    if (live) {
-        const float g = (float)(d + 2) * 5.9604645e-8f;
-        const float fac = 1.0f + 8.0f * g;
-        bool ok = m1 < 1.0e37f && m2 < 1.0e37f && m2 > fmaf(m1, fac, 1.0e-37f);
-        if (TOP3) ok = ok && m3 < 1.0e37f && m3 > fmaf(m2, fac, 1.0e-37f);
-        SampleResult r;
-        if (ok) {
-            r.i1 = u1;
-            r.i2 = TOP3 ? u2 : -1;
-            r.d1 = (a.outs & OUT_ERR) ? ref_sqdist(a.w + (int64_t)u1 * d, xg, d) : 0.0;
-        } else {
-            if (a.recheck_count) atomicAdd(a.recheck_count, 1ull);
-            const float thr = m2 < 1.0e37f ? fmaf(m2, fac, 1.0e-37f) : INFINITY;
-            r = exact_top2(a, xg, thr);
-        }
-        emit_sample(a, i, r, e0, e1, e2);
+    const float g = (float)(d + 2) * 5.9604645e-8f;
+    const float fac = 1.0f + 8.0f * g;
+    bool ok = m1 < 1.0e37f && m2 < 1.0e37f && m2 > fmaf(m1, fac, 1.0e-37f);
+    if (TOP3) ok = ok && m3 < 1.0e37f && m3 > fmaf(m2, fac, 1.0e-37f);
+    const bool exact = live && !ok;
+    SampleResult r;
+    if (live && ok) {
+        r.i1 = u1;
+        r.i2 = TOP3 ? u2 : -1;
+        r.d1 = (a.outs & OUT_ERR) ? ref_sqdist(a.w + (int64_t)u1 * d, xg, d) : 0.0;
     }
+    if (exact && a.recheck_count) atomicAdd(a.recheck_count, 1ull);
+    const float thr = m2 < 1.0e37f ? fmaf(m2, fac, 1.0e-37f) : INFINITY;
+    if constexpr (DMAX > 0) {
+        // exact path: a second pass over the same shared-memory unit tiles, for the rows of the block that need it;
+        // the reference's float64 sum for every unit the float32 screen cannot exclude
+        if (__syncthreads_or(exact)) {
+            Top2 t;
+            t.init();
+            for (int64_t j0 = 0; j0 < a.m; j0 += K0_TILE) {
+                const int tu = (int)min64(K0_TILE, a.m - j0);
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < K0_TILE * DMAX; idx += K0_THREADS) {
+                    int jj = idx / DMAX, k = idx - jj * DMAX;
+                    wsh[idx] = (jj < tu && k < d) ? a.w[(j0 + jj) * d + k] : 0.0f;
+                }
+                __syncthreads();
+                if (exact) {
+                    for (int jj = 0; jj < tu; ++jj) {
+                        const float df = fp32_dist<DMAX>(wsh + jj * DMAX, xr, d);
+                        if (!(df <= thr)) continue;   // also drops NaN, whose reference distance is NaN as well
+                        t.push(ref_sqdist(wsh + jj * DMAX, xg, d), (int32_t)(j0 + jj));
+                    }
+                }
+            }
+            if (exact) {
+                r.i1 = t.i1;
+                r.i2 = t.i2;
+                r.d1 = t.d1;
+            }
+        }
+    } else {
+        if (exact) r = exact_top2(a, xg, thr);
+    }
+    if (live) emit_sample(a, i, r, e0, e1, e2);
     if (a.outs & OUT_ERR) block_add3(e0, e1, e2, a.err3);
     __syncthreads();   // the shared tile and reduction buffers are reused by the next row block
 }
@@ -193,9 +221,11 @@ __device__ __forceinline__ float row_dist32(const float* __restrict__ wr, const 
 
 template <int DMAX, bool TOP3>
 __global__ void __launch_bounds__(KR_THREADS) k0_rows_kernel(PassArgs a, const int32_t* __restrict__ rows,
-                                                             const unsigned long long* __restrict__ count) {
+                                                             const unsigned long long* __restrict__ count,
+                                                             long long max_rows) {
     const int lane = threadIdx.x & 31;
     const int64_t total = (int64_t)*count;
+    if (total > max_rows) return;   // a long list: k0_rows_block_kernel takes it
     const int64_t nwarps = (int64_t)gridDim.x * (KR_THREADS / 32);
     const int d = a.d;
     const float g = (float)(d + 2) * 5.9604645e-8f;
@@ -286,13 +316,33 @@ __global__ void __launch_bounds__(KR_THREADS) k0_rows_kernel(PassArgs a, const i
     if (a.outs & OUT_ERR) block_add3(e0, e1, e2, a.err3);
 }
 
+// A long list: thread t of block b takes listed row 128 i + t for the blocks' turns i; the unit tiles are shared
+// through shared memory by the block's 128 rows (k0_block), instead of each row reading the whole map.
+template <int DMAX, bool TOP3>
+__global__ void __launch_bounds__(K0_THREADS) k0_rows_block_kernel(PassArgs a, const int32_t* __restrict__ rows,
+                                                                   const unsigned long long* __restrict__ count,
+                                                                   long long min_rows) {
+    const int64_t total = (int64_t)*count;
+    if (total < min_rows) return;   // a short list: k0_rows_kernel takes it
+    for (int64_t base = (int64_t)blockIdx.x * K0_THREADS; base < total; base += (int64_t)gridDim.x * K0_THREADS) {
+        const int64_t e = base + threadIdx.x;
+        const bool live = e < total;
+        k0_block<DMAX, TOP3>(a, live ? (int64_t)rows[e] : 0, live);
+    }
+}
+
 template <int DMAX>
 int launch_rows(const PassArgs& a, const int32_t* rows, const unsigned long long* count, cudaStream_t stream) {
-    const dim3 grid((unsigned)(4 * num_sms()));
-    if (a.outs & OUT_ERR)
-        k0_rows_kernel<DMAX, true><<<grid, KR_THREADS, 0, stream>>>(a, rows, count);
-    else
-        k0_rows_kernel<DMAX, false><<<grid, KR_THREADS, 0, stream>>>(a, rows, count);
+    // the list length is known on the device only: both kernels launch and the one whose range it is in runs
+    const long long split = (long long)num_sms() * K0_THREADS;   // one 128-row turn per SM
+    const dim3 grid((unsigned)(4 * num_sms())), bgrid((unsigned)(2 * num_sms()));
+    if (a.outs & OUT_ERR) {
+        k0_rows_kernel<DMAX, true><<<grid, KR_THREADS, 0, stream>>>(a, rows, count, split - 1);
+        k0_rows_block_kernel<DMAX, true><<<bgrid, K0_THREADS, 0, stream>>>(a, rows, count, split);
+    } else {
+        k0_rows_kernel<DMAX, false><<<grid, KR_THREADS, 0, stream>>>(a, rows, count, split - 1);
+        k0_rows_block_kernel<DMAX, false><<<bgrid, K0_THREADS, 0, stream>>>(a, rows, count, split);
+    }
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }
