@@ -56,6 +56,21 @@ __device__ SampleResult exact_top2(const PassArgs& a, const float* __restrict__ 
 template <int DMAX, bool TOP3>
 __device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live);
 
+// Units j0 .. j0 + K0_TILE - 1 into the block's shared tile (rows padded to DMAX with zeros, past the map too);
+// returns how many are real. Every thread of the block calls it.
+template <int DMAX>
+__device__ __forceinline__ int k0_load_tile(const PassArgs& a, float* wsh, int64_t j0) {
+    const int tu = (int)min64(K0_TILE, a.m - j0);
+    const int d = a.d;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < K0_TILE * DMAX; idx += K0_THREADS) {
+        int jj = idx / DMAX, k = idx - jj * DMAX;
+        wsh[idx] = (jj < tu && k < d) ? a.w[(j0 + jj) * d + k] : 0.0f;
+    }
+    __syncthreads();
+    return tu;
+}
+
 // Thread t of block b handles sample b*128 + t.
 template <int DMAX, bool TOP3>
 __global__ void __launch_bounds__(K0_THREADS) k0_pass_kernel(PassArgs a) {
@@ -81,14 +96,7 @@ __device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live
     int32_t u1 = -1, u2 = -1, u3 = -1;
     for (int64_t j0 = 0; j0 < a.m; j0 += K0_TILE) {
         const int tu = (int)min64(K0_TILE, a.m - j0);
-        if constexpr (DMAX > 0) {
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < K0_TILE * DMAX; idx += K0_THREADS) {
-                int jj = idx / DMAX, k = idx - jj * DMAX;
-                wsh[idx] = (jj < tu && k < d) ? a.w[(j0 + jj) * d + k] : 0.0f;
-            }
-            __syncthreads();
-        }
+        if constexpr (DMAX > 0) k0_load_tile<DMAX>(a, wsh, j0);
         for (int jj = 0; jj < tu; ++jj) {
             float df;
             if constexpr (DMAX > 0) {
@@ -134,28 +142,62 @@ __device__ __forceinline__ void k0_block(const PassArgs& a, int64_t i, bool live
     if (exact && a.recheck_count) atomicAdd(a.recheck_count, 1ull);
     const float thr = m2 < 1.0e37f ? fmaf(m2, fac, 1.0e-37f) : INFINITY;
     if constexpr (DMAX > 0) {
-        // exact path: a second pass over the same shared-memory unit tiles, for the rows of the block that need it;
-        // the reference's float64 sum for every unit the float32 screen cannot exclude
-        if (__syncthreads_or(exact)) {
+        // Exact path: more passes over the same shared-memory unit tiles, for the rows of the block that need them.
+        // First the units the float32 screen cannot exclude are ranked by compensated float32 sums of the reference's
+        // squares; ranks that pass df_apart are the reference's (D <= 32). Rows left undecided (equal units,
+        // non-finite sums) take the reference's float64 sums in a last pass.
+        bool fp64 = exact && !(DMAX <= 32 && thr < 1.0e37f);
+        if (__syncthreads_or(exact && !fp64)) {
+            DFloat p1{INFINITY, 0.0f}, p2{INFINITY, 0.0f}, p3{INFINITY, 0.0f};
+            int32_t q1 = -1, q2 = -1, q3 = -1;
+            for (int64_t j0 = 0; j0 < a.m; j0 += K0_TILE) {
+                const int tu = k0_load_tile<DMAX>(a, wsh, j0);
+                if (exact && !fp64) {
+                    for (int jj = 0; jj < tu; ++jj) {
+                        if (!(fp32_dist<DMAX>(wsh + jj * DMAX, xr, d) <= thr)) continue;
+                        const DFloat t = ref_dist_pair<DMAX>(wsh + jj * DMAX, xr);
+                        const DFloat v = two_sum(t.hi, t.lo);
+                        const int32_t j = (int32_t)(j0 + jj);
+                        if (TOP3) {
+                            if (df_before(v, j, p3, q3)) {
+                                if (df_before(v, j, p2, q2)) {
+                                    p3 = p2; q3 = q2;
+                                    if (df_before(v, j, p1, q1)) { p2 = p1; q2 = q1; p1 = v; q1 = j; }
+                                    else { p2 = v; q2 = j; }
+                                } else { p3 = v; q3 = j; }
+                            }
+                        } else if (df_before(v, j, p2, q2)) {
+                            if (df_before(v, j, p1, q1)) { p2 = p1; q2 = q1; p1 = v; q1 = j; }
+                            else { p2 = v; q2 = j; }
+                        }
+                    }
+                }
+            }
+            if (exact && !fp64) {
+                const bool finite = q1 >= 0 && p1.hi < 1.0e37f && (q2 < 0 || p2.hi < 1.0e37f) &&
+                                    (!TOP3 || q3 < 0 || p3.hi < 1.0e37f);
+                if (finite && df_apart(p1, p2, q2) && (!TOP3 || df_apart(p2, p3, q3))) {
+                    r.i1 = q1;
+                    r.i2 = q2;
+                    r.d1 = (a.outs & OUT_ERR) ? ref_sqdist(a.w + (int64_t)q1 * d, xg, d) : 0.0;
+                } else {
+                    fp64 = true;
+                }
+            }
+        }
+        if (__syncthreads_or(fp64)) {
             Top2 t;
             t.init();
             for (int64_t j0 = 0; j0 < a.m; j0 += K0_TILE) {
-                const int tu = (int)min64(K0_TILE, a.m - j0);
-                __syncthreads();
-                for (int idx = threadIdx.x; idx < K0_TILE * DMAX; idx += K0_THREADS) {
-                    int jj = idx / DMAX, k = idx - jj * DMAX;
-                    wsh[idx] = (jj < tu && k < d) ? a.w[(j0 + jj) * d + k] : 0.0f;
-                }
-                __syncthreads();
-                if (exact) {
+                const int tu = k0_load_tile<DMAX>(a, wsh, j0);
+                if (fp64) {
                     for (int jj = 0; jj < tu; ++jj) {
-                        const float df = fp32_dist<DMAX>(wsh + jj * DMAX, xr, d);
-                        if (!(df <= thr)) continue;   // also drops NaN, whose reference distance is NaN as well
+                        if (!(fp32_dist<DMAX>(wsh + jj * DMAX, xr, d) <= thr)) continue;   // drops NaN, as the reference
                         t.push(ref_sqdist(wsh + jj * DMAX, xg, d), (int32_t)(j0 + jj));
                     }
                 }
             }
-            if (exact) {
+            if (fp64) {
                 r.i1 = t.i1;
                 r.i2 = t.i2;
                 r.d1 = t.d1;

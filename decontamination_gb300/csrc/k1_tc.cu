@@ -95,15 +95,16 @@ constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go
 constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN);
 
 // K layout of the operands (elements per row, FP16). D a multiple of 16: A = [x_hi | x_lo | q columns],
-// B = [-2w_hi | -2w_lo | q_hi q_lo 0...], and the MMA K-steps pair the blocks (hi.hi, lo.hi, hi.lo, then q), so no
-// block is stored twice. Other D: A = [x_hi | x_lo | x_hi | 2^11 2^11 | 0...], B = [-2w_hi | -2w_hi | -2w_lo | q_hi
-// q_lo | 0...] padded to a multiple of 16, one K-step per 16 columns.
+// B = [-2w_hi | -2w_lo | q_hi q_lo 0...], and the MMA K-steps pair the blocks (lo.hi, hi.lo, hi.hi, then q), so no
+// block is stored twice. Other D: A = [x_lo | x_hi | x_hi | 2^11 2^11 | 0...], B = [-2w_hi | -2w_lo | -2w_hi | q_hi
+// q_lo | 0...] padded to a multiple of 16, one K-step per 16 columns. Either way the small (lo) products enter the
+// FP32 accumulator first, while it is small, so their roundings are small too (tc_error_coefficients).
 __host__ __device__ constexpr bool k_dedup(int d) { return d % 16 == 0; }
 __host__ __device__ constexpr int k_width(int d) { return k_dedup(d) ? 2 * d + 16 : (3 * d + 2 + 15) / 16 * 16; }
 __host__ __device__ constexpr int k_steps(int d) { return k_dedup(d) ? 3 * (d / 16) + 1 : k_width(d) / 16; }
 __host__ __device__ constexpr int k_qcol(int d) { return k_dedup(d) ? 2 * d : 3 * d; }   // first q column
 // column offsets of K-step i in A and in B
-__device__ __forceinline__ void k_step_cols(int d, int i, int& ka, int& kb) {
+__host__ __device__ __forceinline__ void k_step_cols(int d, int i, int& ka, int& kb) {
     if (!k_dedup(d)) {
         ka = kb = 16 * i;
         return;
@@ -113,13 +114,13 @@ __device__ __forceinline__ void k_step_cols(int d, int i, int& ka, int& kb) {
         ka = kb = 2 * d;
         return;
     }
-    const int blk = i % nb, kind = i / nb;   // kind 0: hi.hi, 1: lo.hi, 2: hi.lo
-    ka = (kind == 1 ? d : 0) + 16 * blk;
-    kb = (kind == 2 ? d : 0) + 16 * blk;
+    const int blk = i % nb, kind = i / nb;   // kind 0: lo.hi, 1: hi.lo, 2: hi.hi
+    ka = (kind == 0 ? d : 0) + 16 * blk;
+    kb = (kind == 1 ? d : 0) + 16 * blk;
 }
 
 struct TcShape {
-    int d = 0, kpad = 0, knz = 0;
+    int d = 0, kpad = 0;
     int64_t mpad = 0;
     int utiles = 0;
     int bstages = 0;   // 0: the whole unit operand resident in shared memory; else a ring of this many column tiles
@@ -154,7 +155,6 @@ size_t tc_layout(TcShape& s, size_t bregion) {
 TcShape tc_shape(int64_t m, int d) {
     TcShape s;
     s.d = d;
-    s.knz = 3 * d + 2;
     s.kpad = k_width(d);
     s.mpad = (int64_t)align_up((size_t)m, TN);
     s.utiles = (int)(s.mpad / TN);
@@ -207,21 +207,63 @@ size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
     return off;
 }
 
+// Operand classes of the K columns (tc_error_coefficients walks the layout with them).
+enum KCol { KC_ZERO = 0, KC_HI, KC_LO, KC_Q, KC_QL };
+inline int k_col_a(int d, int k) {
+    if (k_dedup(d)) return k < d ? KC_HI : k < 2 * d ? KC_LO : (k == 2 * d || k == 2 * d + 1) ? KC_Q : KC_ZERO;
+    return k < d ? KC_LO : k < 3 * d ? KC_HI : (k == 3 * d || k == 3 * d + 1) ? KC_Q : KC_ZERO;
+}
+inline int k_col_b(int d, int k) {
+    const int qc = k_qcol(d);
+    if (k == qc) return KC_Q;
+    if (k == qc + 1) return KC_QL;
+    if (k_dedup(d)) return k < d ? KC_HI : k < 2 * d ? KC_LO : KC_ZERO;
+    return k < d ? KC_HI : k < 2 * d ? KC_LO : k < 3 * d ? KC_HI : KC_ZERO;
+}
+
+// |s~_j - s_j| <= alpha |x'|^2 + beta d'_j + gamma. With P = |x'|^2 + |w'|^2 <= 3|x'|^2 + 2d' and
+// Q = |w'|^2 <= 2|x'|^2 + 2d':
+//  * representation: dropping x_lo w_lo and the two-term residuals costs 3.01 * 2^-22 |x'_k||w'_k| per product, so
+//    3.01 * 2^-22 P over the row; q's split (computed in float64) 2.5 * 2^-22 Q;
+//  * accumulation: each non-zero product is one FP32 rounding of the running sum (2^-23 of it, a worst case that also
+//    covers truncation). The MMA K-steps run in order and the running sum after step s is bounded by the magnitudes of
+//    the product classes seen so far: hi.hi products sum to at most 1.0011 P, each lo class (lo.hi, hi.lo) to
+//    2^-11 * 1.0011 P, the q pair to (1 + 2^-10) Q. The bound is summed step by step over the actual layout, so the
+//    small products placed first cost almost nothing;
+//  * centring rounding and the reference's own float32 rounding of each term: 2^-21 (|x'|^2 + d');
+//  * FP16 subnormal split residuals (absolute 2^-25) times |x'_k| summed over k: below 2^-24 sqrt(D) (1 + |x'|^2) / 2,
+//    a further 2^-21 |x'|^2 and an absolute part inside gamma.
+// 25% is added to alpha and beta as a safety margin.
 void tc_error_coefficients(int d, float* alpha, float* beta) {
-    const double u22 = std::ldexp(1.0, -22);
-    const double knz = 3.0 * d + 2.0;
-    const double acc = knz * std::ldexp(1.0, -23);       // one rounding per product, worst case
-    // representation: 3.01*2^-22 (|x'|^2 + |w'|^2) from -2 x'.w'; 2.5*2^-22 |w'|^2 from q's split and (D+2) 2^-24 |w'|^2
-    // from its float32 evaluation; |w'|^2 <= 2|x'|^2 + 2d'
-    const double qe = 2.5 * u22 + (d + 2.0) * std::ldexp(1.0, -24);
-    double a = 3.01 * u22 * 3.0 + qe * 2.0 + acc * 5.05;
-    double b = 3.01 * u22 * 2.0 + qe * 2.0 + acc * 4.04;
-    // centring rounding and the reference's own float32 rounding of each term
-    a += std::ldexp(1.0, -21);
+    const double u22 = std::ldexp(1.0, -22), u23 = std::ldexp(1.0, -23), u11 = std::ldexp(1.0, -11);
+    double cp = 0.0, cq = 0.0;   // accumulated rounding bound, in units of 2^-23 P and 2^-23 Q
+    bool seen_hi = false, seen_lo_a = false, seen_lo_b = false, seen_q = false;
+    for (int st = 0; st < k_steps(d); ++st) {
+        int ka = 0, kb = 0;
+        k_step_cols(d, st, ka, kb);
+        int nz = 0;
+        for (int i = 0; i < 16; ++i) {
+            const int ca = k_col_a(d, ka + i), cb = k_col_b(d, kb + i);
+            if (ca == KC_ZERO || cb == KC_ZERO) continue;
+            ++nz;
+            if (ca == KC_HI && cb == KC_HI) seen_hi = true;
+            else if (ca == KC_LO && cb == KC_HI) seen_lo_a = true;
+            else if (ca == KC_HI && cb == KC_LO) seen_lo_b = true;
+            else if (ca == KC_Q) seen_q = true;
+            else seen_hi = seen_lo_a = seen_lo_b = seen_q = true;   // not produced by the layouts; counted in full
+        }
+        const double run_p = (seen_hi ? 1.0011 : 0.0) + (seen_lo_a ? u11 * 1.0011 : 0.0) + (seen_lo_b ? u11 * 1.0011 : 0.0);
+        const double run_q = seen_q ? 1.0 + 2.0 * u11 : 0.0;
+        cp += nz * run_p;
+        cq += nz * run_q;
+    }
+    const double rep_p = 3.01 * u22, rep_q = 2.5 * u22;
+    const double kp = rep_p + cp * u23, kq = rep_q + cq * u23;   // error <= kp P + kq Q
+    double a = 3.0 * kp + 2.0 * kq, b = 2.0 * kp + 2.0 * kq;
+    a += std::ldexp(1.0, -21);   // centring and the reference's float32 terms
     b += std::ldexp(1.0, -21);
-    // FP16 subnormal split residuals (absolute 2^-25) times |x'_k| summed over k: below 2^-24 sqrt(D) (1 + |x'|^2) / 2
-    a += std::ldexp(1.0, -21);
-    *alpha = (float)(1.25 * a);   // 25% safety margin
+    a += std::ldexp(1.0, -21);   // FP16 subnormal residuals
+    *alpha = (float)(1.25 * a);
     *beta = (float)(1.25 * b);
 }
 
@@ -282,15 +324,15 @@ __global__ void tc_prep_b_kernel(const float* __restrict__ w, int64_t m, int d, 
     auto put = [&](int k, float v) { *(__half*)(b + canon_off(j, k, kpad)) = __float2half_rn(v); };
     const float scale = center[d];
     bool valid = j < m;
-    float q = 0.0f;
+    double q = 0.0;   // |w'|^2 of the float32 coordinates, to float64 rounding (once per unit and pass)
     if (valid) {
         for (int k = 0; k < d; ++k) {
             const float v = w[j * d + k];
             if (!isfinite(v)) valid = false;
             const float t = (v - center[k]) * scale;
-            q = fmaf(t, t, q);
+            q = fma((double)t, (double)t, q);
         }
-        if (!(q < 1.0e30f)) valid = false;
+        if (!(q < 1.0e30)) valid = false;
     }
     for (int k = 0; k < kpad; ++k) put(k, 0.0f);
     const int qc = k_qcol(d);
@@ -304,17 +346,14 @@ __global__ void tc_prep_b_kernel(const float* __restrict__ w, int64_t m, int d, 
         const __half hi = __float2half_rn(t);
         const __half lo = __float2half_rn(t - __half2float(hi));
         put(k, -2.0f * __half2float(hi));
-        if (dedup) {
-            put(d + k, -2.0f * __half2float(lo));
-        } else {
-            put(d + k, -2.0f * __half2float(hi));
-            put(2 * d + k, -2.0f * __half2float(lo));
-        }
+        put(d + k, -2.0f * __half2float(lo));
+        if (!dedup) put(2 * d + k, -2.0f * __half2float(hi));
     }
-    const float qs = q * (1.0f / Q_COLUMN);
-    const __half qh = __float2half_rn(qs);
+    // q_hi + q_lo = 2^-11 |w'|^2 to 2^-22 relative
+    const double qs = q * (1.0 / Q_COLUMN);
+    const __half qh = __float2half_rn((float)qs);
     put(qc, __half2float(qh));
-    put(qc + 1, qs - __half2float(qh));
+    put(qc + 1, (float)(qs - (double)__half2float(qh)));
 }
 
 // ---------------------------------------------------------------------------------------------------------------------
@@ -383,42 +422,11 @@ __device__ __forceinline__ void cand_dist32_multi(const float* __restrict__ w, c
     }
 }
 
-// Normalised float32 pairs (|lo| <= ulp(hi) / 2) in (value, unit) order; empty entries (unit < 0) last.
-__device__ __forceinline__ bool df_before(DFloat a, int32_t ja, DFloat b, int32_t jb) {
-    return ja >= 0 && (jb < 0 || a.hi < b.hi || (a.hi == b.hi && (a.lo < b.lo || (a.lo == b.lo && ja < jb))));
-}
-// b (unit jb; absent when jb < 0) exceeds a by more than 2^-36 of b. Each pair is the compensated float32 sum of
-// the D float32 squares: its low word carries at most (D-1)^2 2^-48 of the sum in rounding (2^-38 at D = 32), and the
-// reference's float64 sum of the same squares is within (D-1) 2^-53 of the exact one; so pairs that far apart stand
-// for float64 sums ordered the same way.
-__device__ __forceinline__ bool df_apart(DFloat a, DFloat b, int32_t jb) {
-    if (jb < 0) return true;
-    const float gap = __fadd_rn(__fsub_rn(b.hi, a.hi), __fsub_rn(b.lo, a.lo));
-    return gap > 1.4551915e-11f * b.hi;   // 2^-36
-}
-
 // (da, ja) ranks before (db, jb): lexicographic, empty entries (unit < 0) last
 __device__ __forceinline__ bool lex_before(float da, int32_t ja, float db, int32_t jb) {
     return ja >= 0 && (jb < 0 || da < db || (da == db && ja < jb));
 }
 
-// Reference distance (float64 sum of float32 squares) as an exact float32 pair; used for d1 of QE.
-template <int DT>
-__device__ __forceinline__ DFloat ref_dist_pair(const float* __restrict__ wr, const float (&xr)[DT]) {
-    DFAcc acc;
-    const float4* w4 = (const float4*)wr;
-#pragma unroll
-    for (int k4 = 0; k4 < DT / 4; ++k4) {
-        const float4 w = w4[k4];
-        const float t0 = __fsub_rn(w.x, xr[4 * k4]), t1 = __fsub_rn(w.y, xr[4 * k4 + 1]);
-        const float t2 = __fsub_rn(w.z, xr[4 * k4 + 2]), t3 = __fsub_rn(w.w, xr[4 * k4 + 3]);
-        acc.add(__fmul_rn(t0, t0));
-        acc.add(__fmul_rn(t1, t1));
-        acc.add(__fmul_rn(t2, t2));
-        acc.add(__fmul_rn(t3, t3));
-    }
-    return DFloat{acc.hi, acc.lo};
-}
 
 // LARGE: the unit operand streams through a ring (more than fits in shared memory) or the map has more than 8 column
 // tiles; the other instantiations (resident operand, at most 8 column tiles) carry none of that logic.
@@ -665,12 +673,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int k = kc * 8 + i;
-                        constexpr int nx = k_dedup(DT) ? 2 * DT : 3 * DT;   // x_hi | x_lo (| x_hi)
+                        constexpr int nx = k_dedup(DT) ? 2 * DT : 3 * DT;   // x_hi | x_lo, or x_lo | x_hi | x_hi
+                        constexpr int klo = k_dedup(DT) ? DT : 0;              // first x_lo column
                         float val = 0.0f;
                         if (k < nx) {
                             const float t = xp[k % DT];
                             const float hi = __half2float(__float2half_rn(t));
-                            val = (k >= DT && k < 2 * DT) ? t - hi : hi;
+                            val = (k >= klo && k < klo + DT) ? t - hi : hi;
                         } else if (k == k_qcol(DT) || k == k_qcol(DT) + 1) {
                             val = Q_COLUMN;
                         }

@@ -101,6 +101,39 @@ __device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
     return DFloat{p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e))};
 }
 
+// Normalised float32 pairs (|lo| <= ulp(hi) / 2) in (value, unit) order; empty entries (unit < 0) last.
+__device__ __forceinline__ bool df_before(DFloat a, int32_t ja, DFloat b, int32_t jb) {
+    return ja >= 0 && (jb < 0 || a.hi < b.hi || (a.hi == b.hi && (a.lo < b.lo || (a.lo == b.lo && ja < jb))));
+}
+// b (unit jb; absent when jb < 0) exceeds a by more than 2^-36 of b. Each pair is the compensated float32 sum of
+// the D float32 squares: its low word carries at most (D-1)^2 2^-48 of the sum in rounding (2^-38 at D = 32), and the
+// reference's float64 sum of the same squares is within (D-1) 2^-53 of the exact one; so pairs that far apart stand
+// for float64 sums ordered the same way.
+__device__ __forceinline__ bool df_apart(DFloat a, DFloat b, int32_t jb) {
+    if (jb < 0) return true;
+    const float gap = __fadd_rn(__fsub_rn(b.hi, a.hi), __fsub_rn(b.lo, a.lo));
+    return gap > 1.4551915e-11f * b.hi;   // 2^-36
+}
+
+// The reference distance (float64 sum of the float32 squares in feature order) as a compensated float32 pair, within
+// (D-1)^2 2^-48 of the sum; unnormalised (two_sum(hi, lo) normalises). wr: 16-byte aligned, DT a multiple of 4.
+template <int DT>
+__device__ __forceinline__ DFloat ref_dist_pair(const float* __restrict__ wr, const float (&xr)[DT]) {
+    DFAcc acc;
+    const float4* w4 = (const float4*)wr;
+#pragma unroll
+    for (int k4 = 0; k4 < DT / 4; ++k4) {
+        const float4 w = w4[k4];
+        const float t0 = __fsub_rn(w.x, xr[4 * k4]), t1 = __fsub_rn(w.y, xr[4 * k4 + 1]);
+        const float t2 = __fsub_rn(w.z, xr[4 * k4 + 2]), t3 = __fsub_rn(w.w, xr[4 * k4 + 3]);
+        acc.add(__fmul_rn(t0, t0));
+        acc.add(__fmul_rn(t1, t1));
+        acc.add(__fmul_rn(t2, t2));
+        acc.add(__fmul_rn(t3, t3));
+    }
+    return DFloat{acc.hi, acc.lo};
+}
+
 // Is the reference's float64 sum of the float32 squares of the float32 topographic differences above `penalty`
 // (exactly representable)? The two squares are summed exactly in float32 pairs. ta, tb: the two units' coordinates.
 __device__ __forceinline__ bool topo_far32(float2 ta, float2 tb, float penalty) {

@@ -43,7 +43,7 @@ typedef struct CUstream_st* somgb_stream_t; /* == cudaStream_t; NULL = legacy de
 
 /* distance-search algorithms */
 #define SOMGB_ALGO_FP32 0       /* CUDA cores: float32 direct differences, margin-gated float64 recheck */
-#define SOMGB_ALGO_TC 1         /* tcgen05 split-BF16 distance GEMM, margin-gated recheck */
+#define SOMGB_ALGO_TC 1         /* tcgen05 split-FP16 distance GEMM, margin-gated recheck */
 #define SOMGB_ALGO_AUTO 2       /* TC where its shape limits allow, FP32 otherwise */
 
 /* workspace query operations */
