@@ -164,67 +164,111 @@ __global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restric
 // samples per warp instruction. The DP lanes of a sample add d contiguous words of one unit's bins, so an atomic
 // instruction touches 32 / DP short runs of banks instead of 32 random banks. Unweighted samples add 1 to an
 // integer count per unit; weighted ones add their float32 weight in fixed point like a feature.
+// A warp takes 128 samples at a time: each lane loads four BMUs (one 16-byte load), and the samples whose BMU lies in
+// this CTA's unit range are listed in shared memory (ballot prefix sums) as (offset << 16 | unit - lo). The list is
+// then processed UNR groups at a time, every group's feature loads issued before any is added. With several unit
+// ranges only the CTA of a sample's range reads its features, and scanning the other ranges' samples costs a few
+// instructions per 128. The bins are flushed to the float64 sums once the samples added since the last flush could
+// reach FX_WINDOW (the limbs' headroom): each sample adds to one unit's bins, so no bin has more adds than that.
+constexpr int ACC_BATCH = 128;    // samples a warp scans at once (four per lane)
+constexpr int ACC_THREADS = 1024;
+
 template <int DP>
-__global__ void __launch_bounds__(1024) accumulate_lanes_kernel(const float* __restrict__ x, const double* __restrict__ rho,
-                                                                const int32_t* __restrict__ bmu, int64_t n, int d,
-                                                                int64_t units_per_range, int64_t m, int64_t chunk,
-                                                                const float* __restrict__ bounds, double* __restrict__ S,
-                                                                double* __restrict__ c) {
-    extern __shared__ int32_t lane_bins[];   // [3][cnt * d] feature limbs, then [cnt] counts or [3][cnt] weight limbs
+__global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const float* __restrict__ x,
+                                                                       const double* __restrict__ rho,
+                                                                       const int32_t* __restrict__ bmu, int64_t n,
+                                                                       int d, int64_t units_per_range, int64_t m,
+                                                                       int64_t chunk, const float* __restrict__ bounds,
+                                                                       double* __restrict__ S, double* __restrict__ c) {
+    // [3][cnt * d] feature limbs, [cnt] counts or [3][cnt] weight limbs, then the warps' sample lists [32][128]
+    extern __shared__ int32_t lane_bins[];
     __shared__ float scale_s[33];
     __shared__ int exp_s[33];
+    __shared__ int added_s;   // samples added to the bins since the last flush
     constexpr int SPW = 32 / DP;
+    constexpr int UNR = 8;
+    constexpr int64_t SCAN = FX_WINDOW / 4;   // samples scanned between flush decisions
     const int64_t lo = (int64_t)blockIdx.y * units_per_range;
     const int64_t cnt = min64(units_per_range, m - lo);
     const int64_t nbf = cnt * d;
     int32_t* limbs = lane_bins;
     int32_t* csum = lane_bins + 3 * nbf;
     const int64_t nbc = rho ? 3 * cnt : cnt;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    uint32_t* list = (uint32_t*)(lane_bins + 3 * nbf + nbc) + warp * ACC_BATCH;
     for (int64_t q = threadIdx.x; q < 3 * nbf + nbc; q += blockDim.x) lane_bins[q] = 0;
     for (int k = threadIdx.x; k <= d; k += blockDim.x) {
         const int e = fx_exponent(bounds[k]);
         exp_s[k] = e;
         scale_s[k] = ldexpf(1.0f, FX_BITS - e);
     }
+    if (threadIdx.x == 0) added_s = 0;
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int slot = lane / DP, k = lane % DP;
     const bool kval = k < d;
     const float sk = kval ? scale_s[k] : 0.0f;
+    const bool vec = ((uintptr_t)bmu & 15u) == 0u;   // chunk starts are multiples of ACC_BATCH samples
+    const uint32_t lt_mask = (1u << lane) - 1u;
     const int64_t s0 = (int64_t)blockIdx.x * chunk;
     const int64_t s1 = min64(n, s0 + chunk);
-    for (int64_t w0 = s0; w0 < s1; w0 += FX_WINDOW) {
-        const int64_t w1 = min64(s1, w0 + FX_WINDOW);
-        // UNR sample groups per warp and step, all loaded before any is added (memory-level parallelism)
-        constexpr int UNR = 8;
-        for (int64_t base = w0 + (int64_t)warp * SPW * UNR; base < w1; base += (int64_t)nwarps * SPW * UNR) {
-            int32_t bb[UNR];
-            float xv[UNR];
+    for (int64_t w0 = s0; w0 < s1; w0 += SCAN) {
+        const int64_t w1 = min64(s1, w0 + SCAN);
+        for (int64_t base = w0 + (int64_t)warp * ACC_BATCH; base < w1; base += (int64_t)nwarps * ACC_BATCH) {
+            const int64_t i0 = base + 4 * lane;
+            int32_t b[4];
+            if (vec && i0 + 3 < w1) {
+                const int4 v = __ldg((const int4*)(bmu + i0));
+                b[0] = v.x; b[1] = v.y; b[2] = v.z; b[3] = v.w;
+            } else {
 #pragma unroll
-            for (int t = 0; t < UNR; ++t) {
-                const int64_t i = base + t * SPW + slot;
-                bb[t] = i < w1 ? __ldg(bmu + i) : -1;
-                xv[t] = (i < w1 && kval) ? __ldg(x + i * d + k) : 0.0f;
+                for (int j = 0; j < 4; ++j) b[j] = i0 + j < w1 ? __ldg(bmu + i0 + j) : -1;
             }
+            int total = 0;
 #pragma unroll
-            for (int t = 0; t < UNR; ++t) {
-                if (bb[t] < lo || bb[t] >= lo + cnt) continue;   // also skips b == -1
-                const int64_t u = bb[t] - lo;
-                if (!rho) {
-                    if (kval) fx_add_float(limbs, nbf, u * d + k, xv[t] * sk);
-                    if (k == 0) atomicAdd(csum + u, 1);
-                } else {
-                    const float r = (float)__ldg(rho + base + t * SPW + slot);   // float32 density (som_batch.py:312)
-                    if (kval) {
-                        const float hi = r * xv[t];
-                        const float lo_ = fmaf(r, xv[t], -hi);   // r * x exactly as hi + lo
-                        fx_add(limbs, nbf, u * d + k, __float2ll_rn(hi * sk) + __float2ll_rn(lo_ * sk));
+            for (int j = 0; j < 4; ++j) {
+                const bool in = b[j] >= lo && b[j] < lo + cnt;   // never for b == -1
+                const uint32_t mk = __ballot_sync(0xffffffffu, in);
+                if (in) list[total + __popc(mk & lt_mask)] = ((uint32_t)(4 * lane + j) << 16) | (uint32_t)(b[j] - lo);
+                total += __popc(mk);
+            }
+            __syncwarp();
+            for (int p0 = 0; p0 < total; p0 += SPW * UNR) {
+                uint32_t e[UNR];
+                float xv[UNR];
+#pragma unroll
+                for (int t = 0; t < UNR; ++t) {
+                    const int p = p0 + t * SPW + slot;
+                    e[t] = p < total ? list[p] : 0xFFFFFFFFu;
+                }
+#pragma unroll
+                for (int t = 0; t < UNR; ++t)
+                    xv[t] = (e[t] != 0xFFFFFFFFu && kval) ? __ldg(x + (base + (e[t] >> 16)) * d + k) : 0.0f;
+#pragma unroll
+                for (int t = 0; t < UNR; ++t) {
+                    if (e[t] == 0xFFFFFFFFu) continue;
+                    const int64_t u = e[t] & 0xFFFFu;
+                    if (!rho) {
+                        if (kval) fx_add_float(limbs, nbf, u * d + k, xv[t] * sk);
+                        if (k == 0) atomicAdd(csum + u, 1);
+                    } else {
+                        const float r = (float)__ldg(rho + base + (e[t] >> 16));   // float32 density (som_batch.py:312)
+                        if (kval) {
+                            const float hi = r * xv[t];
+                            const float lo_ = fmaf(r, xv[t], -hi);   // r * x exactly as hi + lo
+                            fx_add(limbs, nbf, u * d + k, __float2ll_rn(hi * sk) + __float2ll_rn(lo_ * sk));
+                        }
+                        if (k == 0) fx_add_float(csum, cnt, u, r * scale_s[d]);
                     }
-                    if (k == 0) fx_add_float(csum, cnt, u, r * scale_s[d]);
                 }
             }
+            if (lane == 0 && total) atomicAdd(&added_s, total);
+            __syncwarp();   // the list is rewritten by the next batch
         }
         __syncthreads();
+        const bool flush = w1 == s1 || added_s + SCAN > FX_WINDOW;
+        __syncthreads();   // every thread has read added_s
+        if (!flush) continue;
+        if (threadIdx.x == 0) added_s = 0;
         for (int64_t q = threadIdx.x; q < nbf + cnt; q += blockDim.x) {
             long long v;
             int kk;
@@ -469,20 +513,22 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
         return SOMGB_OK;
     }
     if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "fixed-point segmented sums support D <= 64");
-    // three int32 limbs per bin; up to ~220 KB of bins per CTA, so that a 32x32 map with D = 16 fits one CTA and every
-    // sample is read once
-    const size_t budget = 220 * 1024;
+    // three int32 limbs per bin; up to ~204 KB of bins per CTA (beside the warps' sample lists), so that a 32x32 map
+    // with D = 16 fits one CTA and every sample is read once
     const bool lanes = d <= 32;
+    const size_t lists = lanes ? (size_t)(ACC_THREADS / 32) * ACC_BATCH * 4 : 0;
+    const size_t budget = 220 * 1024 - lists;
     const int64_t per_unit = lanes ? (int64_t)d * 12 + (rho ? 12 : 4) : (int64_t)(d + 1) * 12;
     int64_t upr = std::max<int64_t>(1, (int64_t)(budget / per_unit));
     upr = std::min(upr, m);
     const int64_t ranges = ceil_div(m, upr);
     upr = ceil_div(m, ranges);
-    const size_t smem = (size_t)(upr * per_unit);
+    const size_t smem = (size_t)(upr * per_unit) + lists;
     const int64_t ctas_per_sm = smem <= 100 * 1024 ? 2 : 1;
     const int64_t ctas_wanted = ctas_per_sm * (int64_t)num_sms();
     int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
     int64_t chunk = std::max<int64_t>(4096, ceil_div(n, chunks));
+    chunk = ceil_div(chunk, ACC_BATCH) * ACC_BATCH;
     chunks = ceil_div(n, chunk);
     const dim3 grid((unsigned)chunks, (unsigned)ranges);
     if (lanes) {
@@ -492,7 +538,7 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
         else if (d <= 16) kern = accumulate_lanes_kernel<16>;
         if (smem > 48 * 1024)
             SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<grid, 1024, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, bounds, S, c);
+        kern<<<grid, ACC_THREADS, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, bounds, S, c);
         SOMGB_LAUNCH_CHECK();
         return SOMGB_OK;
     }

@@ -270,6 +270,61 @@ def test_c_abi_epoch_pass_accumulators(cuda, native, oracle):
     assert ei.value.status == native.SOMGB_ERR_WORKSPACE
 
 
+ACCUMULATE_CASES = [
+    # (M, D, N, weighted, bmu pattern): one unit range; several (64x64 at D = 32: 8 ranges; 48x48 at D = 24); every
+    # sample on one unit (more than the limbs' 2^15-add headroom per flush decision); BMUs of -1; a BMU array that
+    # is not 16-byte aligned (scalar loads)
+    (1024, 16, 300_000, False, 'uniform'),
+    (4096, 32, 400_000, False, 'uniform'),
+    (2304, 24, 200_000, True, 'uniform'),
+    (4096, 32, 200_000, True, 'clustered'),
+    (64, 3, 500_000, False, 'one-unit'),
+    (300, 7, 100_000, True, 'with-negatives'),
+    (4096, 32, 150_001, False, 'unaligned'),
+]
+
+
+@pytest.mark.parametrize('M,D,N,weighted,pattern', ACCUMULATE_CASES)
+def test_accumulate_segmented_sums(cuda, native, M, D, N, weighted, pattern):
+    rng = np.random.default_rng(M + D + N)
+    x = _rand(rng, N, D, 'lognormal')
+    if pattern == 'one-unit':
+        b = np.full(N, 17 % M, dtype=np.int32)
+    elif pattern == 'clustered':
+        b = np.minimum(rng.geometric(0.01, N) - 1, M - 1).astype(np.int32)
+    else:
+        b = rng.integers(0, M, N).astype(np.int32)
+    if pattern == 'with-negatives':
+        b[rng.random(N) < 0.2] = -1
+    rho = rng.random(N) * 3.0 if weighted else None
+    xd = torch.from_numpy(x).to(cuda)
+    if pattern == 'unaligned':
+        bd_full = torch.from_numpy(np.concatenate([[0], b]).astype(np.int32)).to(cuda)
+        bd = bd_full[1:]
+        assert bd.data_ptr() % 16 != 0
+    else:
+        bd = torch.from_numpy(b).to(cuda)
+    rd = torch.from_numpy(rho).to(cuda) if weighted else None
+    bounds = torch.zeros(D + 1, dtype=torch.float32, device=cuda)
+    S = torch.zeros((M, D), dtype=torch.float64, device=cuda)
+    c = torch.zeros(M, dtype=torch.float64, device=cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    native.call('somgb_feature_bounds', xd.data_ptr(), rd.data_ptr() if weighted else None, N, D, bounds.data_ptr(), s)
+    native.call('somgb_accumulate', xd.data_ptr(), rd.data_ptr() if weighted else None, bd.data_ptr(), N, D, M,
+                bounds.data_ptr(), S.data_ptr(), c.data_ptr(), s)
+    torch.cuda.synchronize()
+    keep = b >= 0
+    r32 = rho.astype(np.float32).astype(np.float64) if weighted else np.ones(N)
+    S_ref = np.zeros((M, D))
+    np.add.at(S_ref, b[keep], x[keep].astype(np.float64) * r32[keep, None])
+    c_ref = np.bincount(b[keep], weights=r32[keep], minlength=M)
+    np.testing.assert_allclose(S.cpu().numpy(), S_ref, rtol=1e-12, atol=1e-9)
+    if weighted:
+        np.testing.assert_allclose(c.cpu().numpy(), c_ref, rtol=1e-12)
+    else:
+        assert np.array_equal(c.cpu().numpy(), c_ref)
+
+
 def test_edge_cases_tc_padded(cuda, native):
     """The golden edge cases through the tensor-core pass: two zero features pad D=6 to 8 without changing any
     distance, so every output must equal the reference's."""
