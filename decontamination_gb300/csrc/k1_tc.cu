@@ -846,18 +846,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const float4 t = __ldg((const float4*)xg + k4);
                 xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
             }
-            // candidate list of the row from the two halves' masks: one candidate per lane and iteration, the next
-            // non-zero mask word (from the summary bits) fetched in the same iteration; no divergent branches
+            // Candidates of the row from the two halves' masks, one per lane and iteration (the next non-zero mask word,
+            // from the summary bits, fetched in the same iteration), each one's float32 distance computed and ranked
+            // (float32 top-3 in (distance, unit) order) as it is found; the list is kept for the rare slower paths.
+            // A row with more than CAPR candidates stops there and goes to the exact recheck.
             const bool flagged = sFlag[row] != 0;
             int cnt = 0;
+            float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
+            int32_t j1 = -1, j2 = -1, j3 = -1;
+            auto push = [&](float df, int32_t j) {
+                if (!lex_before(df, j, f3, j3)) return;
+                if (lex_before(df, j, f2, j2)) {
+                    f3 = f2; j3 = j2;
+                    if (lex_before(df, j, f1, j1)) { f2 = f1; j2 = j1; f1 = df; j1 = j; }
+                    else { f2 = df; j2 = j; }
+                } else { f3 = df; j3 = j; }
+            };
             // column tiles 0-7, then (for more than 8) 8-15: each part's two halves fit one 64-bit word
             const int parts = LARGE ? (U + 7) / 8 : 1;
             for (int part = 0; part < parts; ++part) {
                 const uint32_t* ss = sSum + part * HALVES * TM;
-                uint64_t S = flagged ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
+                uint64_t S = (flagged || !live) ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
                 uint32_t word = 0;
                 int jtop = 0;
-                bool more = S != 0ull;
+                bool more = S != 0ull && cnt <= CAPR;
                 while (__any_sync(0xffffffffu, more)) {
                     const bool need = word == 0u;
                     const int b = __ffsll((long long)S) - 1;
@@ -868,11 +880,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
                     S = need ? (S & (S - 1ull)) : S;
                     const int j = jtop - (__ffs(word) - 1);
-                    const bool take = word != 0u && j < (int)a.m;
+                    const bool take = more && word != 0u && j < (int)a.m;
                     word &= word - 1u;
-                    list[(take && cnt < CAPR ? cnt : CAPR) * TM] = (uint16_t)j;
-                    cnt += take ? 1 : 0;
-                    more = word != 0u || S != 0ull;
+                    if (take) {
+                        list[(cnt < CAPR ? cnt : CAPR) * TM] = (uint16_t)j;
+                        ++cnt;
+                        push(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr), j);
+                    }
+                    more = (word != 0u || S != 0ull) && cnt <= CAPR;
                 }
             }
             __syncwarp();
@@ -882,29 +897,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                 P.rows[slotq] = (int32_t)grow;
             } else if (live) {
-                // float32 top-3 of the candidates in (distance, unit) order, NQ candidates' rows read at once
-                float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
-                int32_t j1 = -1, j2 = -1, j3 = -1;
-                auto push = [&](float df, int32_t j) {
-                    if (!lex_before(df, j, f3, j3)) return;
-                    if (lex_before(df, j, f2, j2)) {
-                        f3 = f2; j3 = j2;
-                        if (lex_before(df, j, f1, j1)) { f2 = f1; j2 = j1; f1 = df; j1 = j; }
-                        else { f2 = df; j2 = j; }
-                    } else { f3 = df; j3 = j; }
-                };
-                constexpr int NQ = DT <= 16 ? 4 : 2;
                 const float2* topo2 = (const float2*)a.topo;
-                for (int k = 0; k < cnt; k += NQ) {
-                    int32_t jj[NQ];
-#pragma unroll
-                    for (int i = 0; i < NQ; ++i) jj[i] = list[(k + i < cnt ? k + i : k) * TM];
-                    float dd[NQ];
-                    cand_dist32_multi<DT, NQ>(wrows, jj, xr, dd);
-#pragma unroll
-                    for (int i = 0; i < NQ; ++i)
-                        if (k + i < cnt) push(dd[i], jj[i]);
-                }
                 TC_T(8);
                 // The float32 ranking decides when every rank that matters is separated by more than the float32
                 // rounding bound: best vs second (both modes) and, for the error sums, second vs third. Otherwise the
