@@ -392,11 +392,22 @@ __device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, cons
 }
 
 // Bit 31-i set when v[i] - thr_up < 0, i.e. v[i] < thr_up (false for NaN): a subtraction and a shift-or per value.
+// Two independent 16-bit chains (columns 0-15 in the high half), so the shift-ors do not form one 32-long dependency.
 __device__ __forceinline__ uint32_t sign_mask32(const uint32_t (&v)[32], float thr_up) {
-    uint32_t m = 0;
+    uint32_t m0 = 0u, m1 = 0u;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) m = (m << 1) | (__float_as_uint(__fsub_rn(__uint_as_float(v[i]), thr_up)) >> 31);
-    return m;
+    for (int i = 0; i < 16; ++i) {
+        m0 = (m0 << 1) | (__float_as_uint(__fsub_rn(__uint_as_float(v[i]), thr_up)) >> 31);
+        m1 = (m1 << 1) | (__float_as_uint(__fsub_rn(__uint_as_float(v[16 + i]), thr_up)) >> 31);
+    }
+    return (m0 << 16) | m1;
+}
+
+// min(a, b, c) in one instruction (three-input form of min.f32, sm_100 and later); NaN inputs are ignored as by fminf
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 // NQ candidates at once (every row's loads issued before any chain): the same chain as cand_dist32v.
@@ -749,11 +760,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
 #pragma unroll
                     for (int g8 = 0; g8 < 32; g8 += 8) {
-                        const float g = fminf(
-                            fminf(fminf(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1])),
-                                  fminf(__uint_as_float(r[g8 + 2]), __uint_as_float(r[g8 + 3]))),
-                            fminf(fminf(__uint_as_float(r[g8 + 4]), __uint_as_float(r[g8 + 5])),
-                                  fminf(__uint_as_float(r[g8 + 6]), __uint_as_float(r[g8 + 7]))));
+                        const float g = fmin3(fmin3(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1]),
+                                                    __uint_as_float(r[g8 + 2])),
+                                              fmin3(__uint_as_float(r[g8 + 3]), __uint_as_float(r[g8 + 4]),
+                                                    __uint_as_float(r[g8 + 5])),
+                                              fminf(__uint_as_float(r[g8 + 6]), __uint_as_float(r[g8 + 7])));
                         if (c & 1) {
                             if (ERR) b2 = fminf(b2, fmaxf(b1, g));
                             b1 = fminf(b1, g);
