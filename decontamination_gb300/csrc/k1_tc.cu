@@ -78,7 +78,8 @@ namespace {
 constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
 constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
-constexpr int CAPR = 24;          // candidates a resolver keeps per row (unit indices as uint16)
+constexpr int CAPR = 24;          // candidates a resolver ranks per row
+constexpr int KW = 8;             // non-zero candidate-mask words a resolver copies per row
 constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
 constexpr int MAX_U = 16;         // column tiles per row tile (candidate summaries: 32-bit words of 8 tiles per half)
 constexpr int NBARS = 40;         // mbarrier slots
@@ -143,7 +144,7 @@ size_t tc_layout(TcShape& s, size_t bregion) {
     s.off_flag = off;
     off += TM;
     s.off_rlist = off;
-    off += (size_t)(CAPR + 1) * TM * 2;
+    off += (size_t)KW * TM * 6;
     s.off_part = off;
     off += (size_t)HALVES * TM * 8;
     s.off_center = off;
@@ -451,7 +452,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint32_t* sSum = (uint32_t*)(smem + P.off_sum);     // [u / 8][half][TM]: bit 4(u%8)+w set when mask word (u, w) is
                                                         // non-zero (the second pair only for more than 8 column tiles)
     uint8_t* sFlag = smem + P.off_flag;                 // [TM]: the row goes to the exact recheck
-    uint16_t* sList = (uint16_t*)(smem + P.off_rlist);  // [CAPR + 1][TM]: the resolvers' candidate lists (+ scratch)
+    uint32_t* sWords = (uint32_t*)(smem + P.off_rlist);  // [KW][TM]: the resolvers' copies of the non-zero mask words
+    uint16_t* sWtop = (uint16_t*)(sWords + KW * TM);      // [KW][TM]: the unit of bit 0 of each, plus 31
     float2* sPart = (float2*)(smem + P.off_part);       // [half][TM]: (m1, m2) of the half
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
@@ -839,7 +841,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         const float g32 = (float)(d + 2) * 5.9604645e-8f;
         const float fac = 1.0f + 8.0f * g32;
         DFAcc e0, e1, e2;
-        uint16_t* list = sList + row;
+        uint32_t* pw = sWords + row;
+        uint16_t* pt = sWtop + row;
         const float* wrows = P.off_w ? (const float*)(smem + P.off_w) : a.w;   // unit rows: shared memory or L2
         for (int64_t it = 0; it < n_my && !*abort_v; ++it) {
             TC_T0();
@@ -857,11 +860,36 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const float4 t = __ldg((const float4*)xg + k4);
                 xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
             }
-            // Candidates of the row from the two halves' masks, one per lane and iteration (the next non-zero mask word,
-            // from the summary bits, fetched in the same iteration), each one's float32 distance computed and ranked
-            // (float32 top-3 in (distance, unit) order) as it is found; the list is kept for the rare slower paths.
-            // A row with more than CAPR candidates stops there and goes to the exact recheck.
+            // The row's non-zero candidate-mask words (from the summary bits) are first copied to the resolver's own
+            // buffer, which hands the masks back to the sweeps early; more than KW of them send the row to the exact
+            // recheck.
             const bool flagged = sFlag[row] != 0;
+            int nw = 0;
+            // column tiles 0-7, then (for more than 8) 8-15: each part's two halves fit one 64-bit word
+            const int parts = LARGE ? (U + 7) / 8 : 1;
+            for (int part = 0; part < parts; ++part) {
+                const uint32_t* ss = sSum + part * HALVES * TM;
+                uint64_t S = (flagged || !live) ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
+                while (__any_sync(0xffffffffu, S != 0ull)) {
+                    const int b = __ffsll((long long)S) - 1;
+                    const int bb = b < 0 ? 0 : b;
+                    const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
+                    const uint32_t word = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
+                    if (b >= 0) {
+                        if (nw < KW) {
+                            pw[nw * TM] = word;
+                            pt[nw * TM] = (uint16_t)(ub * TN + hh * 128 + wb * 32 + 31);
+                        }
+                        ++nw;
+                        S &= S - 1ull;
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(m_empty);
+            // Then the candidates, one per lane and iteration (the next copied word fetched in the same iteration),
+            // each one's float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found.
+            // A row with more than CAPR candidates stops there and goes to the exact recheck.
             int cnt = 0;
             float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
             int32_t j1 = -1, j2 = -1, j3 = -1;
@@ -873,38 +901,42 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     else { f2 = df; j2 = j; }
                 } else { f3 = df; j3 = j; }
             };
-            // column tiles 0-7, then (for more than 8) 8-15: each part's two halves fit one 64-bit word
-            const int parts = LARGE ? (U + 7) / 8 : 1;
-            for (int part = 0; part < parts; ++part) {
-                const uint32_t* ss = sSum + part * HALVES * TM;
-                uint64_t S = (flagged || !live) ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
-                uint32_t word = 0;
-                int jtop = 0;
-                bool more = S != 0ull && cnt <= CAPR;
+            {
+                const int nwc = nw <= KW ? nw : 0;
+                int wi = 0, jtop = 0;
+                uint32_t word = 0u;
+                bool more = nwc > 0;
                 while (__any_sync(0xffffffffu, more)) {
                     const bool need = word == 0u;
-                    const int b = __ffsll((long long)S) - 1;
-                    const int bb = b < 0 ? 0 : b;
-                    const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
-                    const uint32_t nw = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
-                    word = need ? (b >= 0 ? nw : 0u) : word;
-                    jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
-                    S = need ? (S & (S - 1ull)) : S;
+                    const uint32_t nwd = pw[(wi < KW ? wi : KW - 1) * TM];
+                    const int ntop = pt[(wi < KW ? wi : KW - 1) * TM];
+                    word = need ? (wi < nwc ? nwd : 0u) : word;
+                    jtop = need ? ntop : jtop;
+                    wi += need ? 1 : 0;
                     const int j = jtop - (__ffs(word) - 1);
                     const bool take = more && word != 0u && j < (int)a.m;
                     word &= word - 1u;
                     if (take) {
-                        list[(cnt < CAPR ? cnt : CAPR) * TM] = (uint16_t)j;
                         ++cnt;
                         push(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr), j);
                     }
-                    more = (word != 0u || S != 0ull) && cnt <= CAPR;
+                    more = (word != 0u || wi < nwc) && cnt <= CAPR;
                 }
             }
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(m_empty);
+            // every candidate of the row again (the rare slower paths)
+            auto for_each_cand = [&](auto&& f) {
+                for (int w = 0; w < nw; ++w) {
+                    uint32_t word = pw[w * TM];
+                    const int jt = pt[w * TM];
+                    while (word) {
+                        const int j = jt - (__ffs(word) - 1);
+                        word &= word - 1u;
+                        if (j < (int)a.m) f(j);
+                    }
+                }
+            };
             TC_T(9);
-            if (live && (flagged || cnt == 0 || cnt > CAPR)) {
+            if (live && (flagged || nw > KW || cnt == 0 || cnt > CAPR)) {
                 const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                 P.rows[slotq] = (int32_t)grow;
             } else if (live) {
@@ -937,9 +969,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     // ranks (df_apart). Closer ones (equal units, in practice) take the reference's float64 sums.
                     DFloat p1{INFINITY, 0.0f}, p2{INFINITY, 0.0f}, p3{INFINITY, 0.0f};
                     int32_t q1 = -1, q2 = -1, q3 = -1;
-                    for (int k = 0; k < cnt; ++k) {
-                        const int32_t j = list[k * TM];
-                        if (!(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr) <= climit)) continue;
+                    for_each_cand([&](int32_t j) {
+                        if (!(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr) <= climit)) return;
                         const DFloat t = ref_dist_pair<DT>(wrows + (int64_t)j * DT, xr);
                         const DFloat v = two_sum(t.hi, t.lo);
                         if (df_before(v, j, p3, q3)) {
@@ -949,7 +980,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                                 else { p2 = v; q2 = j; }
                             } else { p3 = v; q3 = j; }
                         }
-                    }
+                    });
                     const bool sure = df_apart(p1, p2, q2) && (!ERR || df_apart(p2, p3, q3));
                     if (sure) {
                         r1 = q1;
@@ -959,11 +990,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         const float* xs = xg;
                         Top2Lex tt;
                         tt.init();
-                        for (int k = 0; k < cnt; ++k) {
-                            const int32_t j = list[k * TM];
-                            if (!(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr) <= climit)) continue;
+                        for_each_cand([&](int32_t j) {
+                            if (!(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr) <= climit)) return;
                             tt.push(ref_sqdist(a.w + (int64_t)j * d, xs, d), j);
-                        }
+                        });
                         r1 = tt.i1;
                         r2 = ERR ? tt.i2 : -1;
                         rd1.hi = (float)tt.d1;
