@@ -376,20 +376,21 @@ struct TcArgs {
     int bstages;             // 0: resident unit operand; else the ring depth
 };
 
-// float32 distance over the reference's float32 differences (FMA chain): |df - d_ref| <= (D+2) 2^-24 d_ref
+// float32 distance over the reference's float32 differences: four FMA chains (features k mod 4) summed at the end,
+// so the dependent chain is D/4 + 2 long; any summation order keeps |df - d_ref| <= (D+2) 2^-24 d_ref
 template <int DT>
 __device__ __forceinline__ float cand_dist32v(const float* __restrict__ wr, const float (&xr)[DT]) {
-    float acc = 0.0f;
+    float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
     const float4* w4 = (const float4*)wr;
 #pragma unroll
     for (int k4 = 0; k4 < DT / 4; ++k4) {
         const float4 w = w4[k4];
-        float t = w.x - xr[4 * k4]; acc = fmaf(t, t, acc);
-        t = w.y - xr[4 * k4 + 1]; acc = fmaf(t, t, acc);
-        t = w.z - xr[4 * k4 + 2]; acc = fmaf(t, t, acc);
-        t = w.w - xr[4 * k4 + 3]; acc = fmaf(t, t, acc);
+        float t = w.x - xr[4 * k4]; c0 = fmaf(t, t, c0);
+        t = w.y - xr[4 * k4 + 1]; c1 = fmaf(t, t, c1);
+        t = w.z - xr[4 * k4 + 2]; c2 = fmaf(t, t, c2);
+        t = w.w - xr[4 * k4 + 3]; c3 = fmaf(t, t, c3);
     }
-    return acc;
+    return (c0 + c1) + (c2 + c3);
 }
 
 // Bit 31-i set when v[i] - thr_up < 0, i.e. v[i] < thr_up (false for NaN): a subtraction and a shift-or per value.
