@@ -81,6 +81,56 @@ __global__ void __launch_bounds__(256) feature_bounds_kernel(const float* __rest
         if (smax[k]) atomicMax(bounds + k, smax[k]);
 }
 
+// The same bounds with the lanes of a warp over features (DP lanes per sample, DP a power of two >= d): the loads of a
+// warp are 32 consecutive floats, each lane keeps the running maximum of its feature in a register, and shared
+// memory sees one atomic per feature and warp at the end. A sample counts when all its features are finite
+// (a vote over its DP lanes) and its float32 weight is positive. UNR groups are loaded before any is used.
+template <int DP>
+__global__ void __launch_bounds__(256) feature_bounds_lanes_kernel(const float* __restrict__ x,
+                                                                   const double* __restrict__ rho, int64_t n, int d,
+                                                                   unsigned int* __restrict__ bounds) {
+    __shared__ unsigned int smax[33];
+    for (int k = threadIdx.x; k <= d; k += blockDim.x) smax[k] = 0u;
+    __syncthreads();
+    constexpr int SPW = 32 / DP;
+    constexpr int UNR = 4;
+    const int lane = threadIdx.x & 31, slot = lane / DP, k = lane % DP;
+    const bool kval = k < d;
+    const uint32_t slot_mask = DP == 32 ? 0xffffffffu : (((1u << DP) - 1u) << (slot * DP));
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned int mx = 0u, mr = 0u;
+    for (int64_t base = gw * SPW * UNR; base < n; base += nw * SPW * UNR) {
+        float v[UNR], r[UNR];
+#pragma unroll
+        for (int t = 0; t < UNR; ++t) {
+            const int64_t i = base + t * SPW + slot;
+            v[t] = (i < n && kval) ? __ldg(x + i * d + k) : 0.0f;
+            r[t] = i < n ? (rho ? (float)__ldg(rho + i) : 1.0f) : 0.0f;
+        }
+#pragma unroll
+        for (int t = 0; t < UNR; ++t) {
+            const bool bad = __ballot_sync(0xffffffffu, !isfinite(v[t])) & slot_mask;
+            if (!bad && r[t] > 0.0f) {
+                const float av = fabsf(r[t] * v[t]);
+                // the float product may round down: one ulp up keeps the bound above the exact product
+                mx = max(mx, __float_as_uint(av) + (av > 0.0f ? 1u : 0u));
+                mr = max(mr, __float_as_uint(r[t]));
+            }
+        }
+    }
+#pragma unroll
+    for (int o = DP; o < 32; o <<= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    }
+    if (lane < DP && kval && mx) atomicMax(smax + k, mx);
+    if (lane == 0 && mr) atomicMax(smax + d, mr);
+    __syncthreads();
+    for (int q = threadIdx.x; q <= d; q += blockDim.x)
+        if (smax[q]) atomicMax(bounds + q, smax[q]);
+}
+
 // DT > 0: the feature count known at compile time (rows loaded as float4); DT == 0: any d.
 template <int DT>
 __global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restrict__ x, const double* __restrict__ rho,
@@ -497,6 +547,18 @@ __global__ void divide_kernel(const double* __restrict__ num, const double* __re
 
 int launch_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, cudaStream_t stream) {
     if (n == 0) return SOMGB_OK;
+    if (d <= 32) {
+        auto kern = feature_bounds_lanes_kernel<32>;
+        if (d <= 4) kern = feature_bounds_lanes_kernel<4>;
+        else if (d <= 8) kern = feature_bounds_lanes_kernel<8>;
+        else if (d <= 16) kern = feature_bounds_lanes_kernel<16>;
+        const int dp = d <= 4 ? 4 : d <= 8 ? 8 : d <= 16 ? 16 : 32;
+        const int64_t per_block = (int64_t)(256 / 32) * (32 / dp) * 4;   // samples per block and step
+        const int64_t blocks = std::min<int64_t>(ceil_div(n, per_block), 8 * (int64_t)num_sms());
+        kern<<<(unsigned)blocks, 256, 0, stream>>>(x, rho, n, d, (unsigned int*)bounds);
+        SOMGB_LAUNCH_CHECK();
+        return SOMGB_OK;
+    }
     const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), 4 * (int64_t)num_sms());
     feature_bounds_kernel<<<(unsigned)blocks, 256, (size_t)(d + 1) * 4, stream>>>(x, rho, n, d, (unsigned int*)bounds);
     SOMGB_LAUNCH_CHECK();

@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _device, _native
-from ._dataset import dataset_to_generator_builder, iterate_chunks
+from ._dataset import dataset_to_generator_builder, device_pieces, iterate_chunks, iterate_pieces
 
 ALGO_DEFAULT = 'auto'
 
@@ -196,7 +196,8 @@ class SOM_Abstract(object):
 
     @property
     def last_recheck_count(self) -> int:
-        """Samples the last projection call sent to the exact float64 recheck (diagnostic)."""
+        """Samples the last get_winners call sent to the exact recheck (diagnostic; for a host catalogue copied in
+        pieces, those of its last piece)."""
         return self._last_recheck_count
 
     # -- device helpers ---------------------------------------------------------------------------------------------------
@@ -246,7 +247,7 @@ class SOM_Abstract(object):
         w = self._device_weights()
         topo = self._device_topography()
         M, D = self._m * self._n, self._dim
-        for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device):
+        for xc, rc in iterate_pieces(dataset, dataset_weights, self._dtype, device):
             n = _device.rows(xc)
             if self._is_f64:
                 _native.call('somgb_compute_errors_f64', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
@@ -267,7 +268,7 @@ class SOM_Abstract(object):
         M, D = self._m * self._n, self._dim
         hist = torch.zeros(M, dtype=torch.float64, device=device)
         w = self._device_weights()
-        for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device):
+        for xc, rc in iterate_pieces(dataset, dataset_weights, self._dtype, device):
             n = _device.rows(xc)
             if self._is_f64:
                 _native.call('somgb_count_bmus_f64', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), M,
@@ -285,17 +286,19 @@ class SOM_Abstract(object):
         """Best matching unit index of every row of `dataset`, int32 (algo/som_abstract.py:670-695)."""
         device = _device.require_cuda()
         M, D = self._m * self._n, self._dim
-        x = _device.to_device(dataset, self._dtype, device)
-        n = _device.rows(x)
-        out = torch.empty(n, dtype=torch.int32, device=device)
+        x, _, pieces = device_pieces(dataset, None, self._dtype, device)
+        out = torch.empty(_device.rows(x), dtype=torch.int32, device=device)
         w = self._device_weights()
-        if self._is_f64:
-            _native.call('somgb_find_bmus_f64', x.data_ptr(), n, D, w.data_ptr(), M, out.data_ptr(),
-                         _device.stream())
-        else:
-            wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, n, M, D, self._algo, device)
-            _native.call('somgb_find_bmus', x.data_ptr(), n, D, w.data_ptr(), M, self._algo, out.data_ptr(), wsp, wsb,
-                         _device.stream())
+        for a, b in pieces:
+            xp, op = x[a:b], out[a:b]
+            if self._is_f64:
+                _native.call('somgb_find_bmus_f64', xp.data_ptr(), b - a, D, w.data_ptr(), M, op.data_ptr(),
+                             _device.stream())
+            else:
+                wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, b - a, M, D, self._algo, device)
+                _native.call('somgb_find_bmus', xp.data_ptr(), b - a, D, w.data_ptr(), M, self._algo, op.data_ptr(),
+                             wsp, wsb, _device.stream())
+        if not self._is_f64:
             self._record_recheck()
         res = out.cpu().numpy()
         self._check_device()

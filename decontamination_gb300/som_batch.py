@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from . import _device, _native
-from ._dataset import is_array, iterate_chunks
+from ._dataset import device_pieces, is_array, iterate_chunks, raw_chunks
 from .som_abstract import SOM_Abstract
 
 FLOAT_EPS = 1.0e-12   # algo/som_batch.py:24
@@ -85,12 +85,22 @@ class SOM_Batch(SOM_Abstract):
         return xc, rc, bounds
 
     def _chunk_source(self, dataset, dataset_weights, device):
-        """Chunks for the epoch loop: arrays are uploaded once (with their bounds) and reused by every epoch."""
+        """Chunks for the epoch loop, as (x, rho, bounds, pieces). Arrays are uploaded once and reused by every epoch:
+        the first epoch gets them with the row pieces of their upload (its passes overlap the copy, and the bounds
+        are accumulated piece by piece), later epochs whole (pieces None, bounds complete). Generator datasets are
+        uploaded every epoch, as the reference does."""
         if (dataset is None or is_array(dataset)) and (dataset_weights is None or is_array(dataset_weights)):
-            chunks = [self._with_bounds(xc, rc, device)
-                      for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device)]
-            return lambda: iter(chunks)
-        return lambda: (self._with_bounds(xc, rc, device)
+            resident = []
+
+            def first():
+                for xr, rr in raw_chunks(dataset, dataset_weights):
+                    xd, rd, pieces = device_pieces(xr, rr, self._dtype, device)
+                    bounds = None if self._is_f64 else torch.zeros(self._dim + 1, dtype=torch.float32, device=device)
+                    resident.append((xd, rd, bounds, None))
+                    yield xd, rd, bounds, pieces
+
+            return lambda: first() if not resident else iter(resident)
+        return lambda: ((*self._with_bounds(xc, rc, device), None)
                         for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device))
 
     def _bmu_buffer(self, n, device):
@@ -99,22 +109,45 @@ class SOM_Batch(SOM_Abstract):
             buf = self._bmu_buf = torch.empty(max(n, 1), dtype=torch.int32, device=device)
         return buf
 
-    def _epoch_pass(self, xc, rc, bounds, w, topo, S, c, err, device):
-        n = _device.rows(xc)
+    def _piece_pass(self, xd, rd, a, b, last, with_errors, w, topo, err, e, device):
+        """Rows a..b of a resident chunk: the training pass (BMUs; error sums of the previous epoch's map when e > 0)
+        or, after the last epoch, the error pass. Float64 maps train in one call per chunk (_accumulate)."""
+        M, D = self._m * self._n, self._dim
+        xc, rc = xd[a:b], (None if rd is None else rd[a:b])
+        n = b - a
+        if last:
+            if not with_errors:
+                return
+            if self._is_f64:
+                _native.call('somgb_compute_errors_f64', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
+                             topo.data_ptr(), M, self._penalty, err.data_ptr(), _device.stream())
+            else:
+                wsp, wsb = self._ws.for_op(_native.OP_ERRORS, n, M, D, self._algo, device)
+                _native.call('somgb_compute_errors', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
+                             topo.data_ptr(), M, self._penalty, self._algo, err.data_ptr(), wsp, wsb,
+                             _device.stream())
+            return
+        if self._is_f64:
+            return
+        bmu = self._bmu_buffer(_device.rows(xd), device)[a:b]
+        wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, n, M, D, self._algo, device)
+        _native.call('somgb_train_bmu_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(), M,
+                     self._penalty, self._algo, bmu.data_ptr(), _device.ptr(err if e > 0 else None), wsp, wsb,
+                     _device.stream())
+
+    def _accumulate(self, xd, rd, bounds, S, c, w, topo, err):
+        """The per-BMU sums of a whole chunk after its BMU passes (float64 maps: the fused float64 epoch pass, with
+        the error sums `err` of the previous epoch's map)."""
+        n = _device.rows(xd)
         M, D = self._m * self._n, self._dim
         if self._is_f64:
-            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, n, M, D, _native.ALGO_FP32, device)
-            _native.call('somgb_train_epoch_pass_f64', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
+            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, n, M, D, _native.ALGO_FP32, xd.device)
+            _native.call('somgb_train_epoch_pass_f64', xd.data_ptr(), _device.ptr(rd), n, D, w.data_ptr(),
                          topo.data_ptr(), M, self._penalty, S.data_ptr(), c.data_ptr(), _device.ptr(err), wsp, wsb,
                          _device.stream())
-        else:
-            bmu = self._bmu_buffer(n, device)
-            wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, n, M, D, self._algo, device)
-            _native.call('somgb_train_bmu_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
-                         topo.data_ptr(), M, self._penalty, self._algo, bmu.data_ptr(), _device.ptr(err), wsp, wsb,
-                         _device.stream())
-            _native.call('somgb_accumulate', xc.data_ptr(), _device.ptr(rc), bmu.data_ptr(), n, D, M,
-                         bounds.data_ptr(), S.data_ptr(), c.data_ptr(), _device.stream())
+            return
+        _native.call('somgb_accumulate', xd.data_ptr(), _device.ptr(rd), self._bmu_buffer(n, xd.device).data_ptr(),
+                     n, D, M, bounds.data_ptr(), S.data_ptr(), c.data_ptr(), _device.stream())
 
     def _update(self, S, c, topo, sigma, w_out):
         M, D = self._m * self._n, self._dim
@@ -172,20 +205,22 @@ class SOM_Batch(SOM_Abstract):
             c.zero_()
             err = errs[e] if with_errors else None
             last = e == n_epochs
-            for xc, rc, bounds in chunks():
-                if last:
-                    if with_errors:
-                        n = _device.rows(xc)
-                        name = 'somgb_compute_errors_f64' if self._is_f64 else 'somgb_compute_errors'
-                        if self._is_f64:
-                            _native.call(name, xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(),
-                                         M, self._penalty, err.data_ptr(), _device.stream())
-                        else:
-                            wsp, wsb = self._ws.for_op(_native.OP_ERRORS, n, M, D, self._algo, device)
-                            _native.call(name, xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(),
-                                         M, self._penalty, self._algo, err.data_ptr(), wsp, wsb, _device.stream())
-                else:
-                    self._epoch_pass(xc, rc, bounds, w, topo, S, c, err if e > 0 else None, device)
+            for xd, rd, bounds, pieces in chunks():
+                if pieces is None:
+                    pieces = [(0, _device.rows(xd))]
+                elif bounds is not None:
+                    # the first sight of an uploaded chunk: its fixed-point bounds, piece by piece
+                    for a, b in pieces:
+                        _native.call('somgb_feature_bounds', xd[a:b].data_ptr(), _device.ptr(rd[a:b] if rd is not None
+                                     else None), b - a, D, bounds.data_ptr(), _device.stream())
+                        self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
+                    if not last:
+                        self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
+                    continue
+                for a, b in pieces:
+                    self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
+                if not last:
+                    self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
             if check_stop and e > 0 and with_errors:
                 qe, te = self._errors_of(errs[e].cpu().numpy())
                 if qe <= sq and te <= st:

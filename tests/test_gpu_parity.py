@@ -325,6 +325,37 @@ def test_accumulate_segmented_sums(cuda, native, M, D, N, weighted, pattern):
         assert np.array_equal(c.cpu().numpy(), c_ref)
 
 
+@pytest.mark.parametrize('D,weighted,dtype', [(16, False, np.float32), (3, True, np.float32), (5, True, np.float64)])
+def test_host_catalogue_in_pieces(cuda, D, weighted, dtype):
+    """A host catalogue above two pieces is copied in pieces whose passes overlap the copy: every output equals the
+    one computed from the same catalogue already on the device (one piece)."""
+    from decontamination_gb300 import _dataset
+    rng = np.random.default_rng(D)
+    N = 2 * _dataset.PIECE_ROWS + 12_345
+    x = _rand(rng, N, D, 'lognormal').astype(dtype)
+    x[rng.integers(0, N, 50)] = np.nan                  # rows that never win
+    rho = rng.random(N) if weighted else None
+    xd = torch.from_numpy(x).to(cuda)
+    rd = torch.from_numpy(rho).to(cuda) if weighted else None
+    xh = torch.from_numpy(x).pin_memory()
+    w0 = x[rng.integers(0, N, 48)].copy()
+    w0[np.isnan(w0)] = 0.0
+    soms = []
+    for data, wts in ((xh, rho), (xd, rd)):
+        som = dg.SOM_Batch(6, 8, D, dtype=dtype, topology='hexagonal')
+        som._weights[...] = w0.reshape(som._weights.shape)
+        som.train(data, dataset_weights=wts, n_epochs=2, use_best_epoch=False)
+        soms.append(som)
+    a, b = soms
+    # BMUs and fixed-point sums are exact; float64 error sums differ only in the order of their atomic additions
+    np.testing.assert_allclose(a.weights, b.weights, rtol=1e-6)
+    np.testing.assert_allclose(a.quantization_errors, b.quantization_errors, rtol=ERR_RTOL)
+    np.testing.assert_allclose(a.topographic_errors, b.topographic_errors, rtol=ERR_RTOL)
+    assert np.array_equal(a.get_winners(x), a.get_winners(xd))
+    np.testing.assert_allclose(a.get_activation_map(x, rho), a.get_activation_map(xd, rd), rtol=1e-12)
+    np.testing.assert_allclose(a.compute_errors(xh, rho), a.compute_errors(xd, rd), rtol=ERR_RTOL)
+
+
 def test_edge_cases_tc_padded(cuda, native):
     """The golden edge cases through the tensor-core pass: two zero features pad D=6 to 8 without changing any
     distance, so every output must equal the reference's."""
