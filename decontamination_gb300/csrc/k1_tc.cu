@@ -272,43 +272,55 @@ void tc_error_coefficients(int d, float* alpha, float* beta) {
 // prep: centre and unit operand
 // ---------------------------------------------------------------------------------------------------------------------
 
-__global__ void tc_center_kernel(const float* __restrict__ w, int64_t m, int d, float* __restrict__ center) {
-    // mean of the finite unit rows, per feature, in float64; then center[d] = the power-of-two scale S that puts the
-    // largest |w - c| coordinate of those rows in [2^5, 2^6)
-    __shared__ double part[256];
-    __shared__ unsigned long long cnt_s;
+// Mean of the finite unit rows, per feature, in float64; then center[d] = the power-of-two scale S that puts the
+// largest |w - c| coordinate of those rows in [2^5, 2^6). One CTA: warps stride over units, lanes over features
+// (d <= 64: two per lane), so every row is read once, coalesced, per pass.
+constexpr int CENTER_THREADS = 1024;
+__global__ void __launch_bounds__(CENTER_THREADS) tc_center_kernel(const float* __restrict__ w, int64_t m, int d,
+                                                                   float* __restrict__ center) {
+    constexpr int NW = CENTER_THREADS / 32;
+    __shared__ double part[NW][64];
+    __shared__ unsigned long long cnt_w[NW];
     __shared__ unsigned int maxbits_s;
-    if (threadIdx.x == 0) { cnt_s = 0; maxbits_s = 0u; }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool k0 = lane < d, k1 = lane + 32 < d;
+    if (threadIdx.x == 0) maxbits_s = 0u;
+    double s0 = 0.0, s1 = 0.0;
+    unsigned long long c = 0;
+    for (int64_t j = warp; j < m; j += NW) {
+        const float v0 = k0 ? w[j * d + lane] : 0.0f, v1 = k1 ? w[j * d + lane + 32] : 0.0f;
+        if (__all_sync(0xffffffffu, isfinite(v0) && isfinite(v1))) {
+            s0 += (double)v0;
+            s1 += (double)v1;
+            ++c;
+        }
+    }
+    part[warp][lane] = s0;
+    part[warp][lane + 32] = s1;
+    if (lane == 0) cnt_w[warp] = c;
     __syncthreads();
-    for (int k = 0; k < d; ++k) {
-        double s = 0.0;
-        unsigned long long c = 0;
-        for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
-            bool ok = true;
-            for (int q = 0; q < d; ++q) ok = ok && isfinite(w[j * d + q]);
-            if (ok) { s += (double)w[j * d + k]; ++c; }
-        }
-        part[threadIdx.x] = s;
-        if (k == 0 && c) atomicAdd(&cnt_s, c);
-        __syncthreads();
-        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-            if ((int)threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) center[k] = cnt_s ? (float)(part[0] / (double)cnt_s) : 0.0f;
-        __syncthreads();
+    unsigned long long cnt = 0;
+    for (int q = 0; q < NW; ++q) cnt += cnt_w[q];
+    for (int k = threadIdx.x; k < d; k += CENTER_THREADS) {
+        double t = 0.0;
+        for (int q = 0; q < NW; ++q) t += part[q][k];
+        center[k] = cnt ? (float)(t / (double)cnt) : 0.0f;
     }
-    for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
-        bool ok = true;
-        for (int q = 0; q < d; ++q) ok = ok && isfinite(w[j * d + q]);
-        if (!ok) continue;
-        for (int k = 0; k < d; ++k) atomicMax(&maxbits_s, __float_as_uint(fabsf(w[j * d + k] - center[k])));
+    __syncthreads();
+    const float c0 = k0 ? center[lane] : 0.0f, c1 = k1 ? center[lane + 32] : 0.0f;
+    unsigned int mx = 0u;
+    for (int64_t j = warp; j < m; j += NW) {
+        const float v0 = k0 ? w[j * d + lane] : 0.0f, v1 = k1 ? w[j * d + lane + 32] : 0.0f;
+        if (__all_sync(0xffffffffu, isfinite(v0) && isfinite(v1)))
+            mx = max(mx, max(__float_as_uint(fabsf(v0 - c0)), __float_as_uint(fabsf(v1 - c1))));
     }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0 && mx) atomicMax(&maxbits_s, mx);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const float mx = __uint_as_float(maxbits_s);
+        const float mxf = __uint_as_float(maxbits_s);
         int e = 0;
-        if (mx > 0.0f && isfinite(mx)) frexpf(mx, &e);   // mx < 2^e
+        if (mxf > 0.0f && isfinite(mxf)) frexpf(mxf, &e);   // mx < 2^e
         else e = 10;
         center[d] = ldexpf(1.0f, min(max(6 - e, -100), 100));
     }
@@ -1138,7 +1150,7 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     if (tc_ws_layout(a.n, a.m, a.d, &W, ws) > ws_bytes) return set_error(SOMGB_ERR_WORKSPACE, "tc workspace too small");
 
     // unit operand
-    tc_center_kernel<<<1, 256, 0, stream>>>(a.w, a.m, a.d, W.center);
+    tc_center_kernel<<<1, CENTER_THREADS, 0, stream>>>(a.w, a.m, a.d, W.center);
     SOMGB_LAUNCH_CHECK();
     tc_prep_b_kernel<<<(unsigned)ceil_div(s.mpad, 128), 128, 0, stream>>>(a.w, a.m, a.d, s.kpad, s.mpad, W.center,
                                                                           W.b);
