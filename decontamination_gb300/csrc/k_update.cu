@@ -220,10 +220,13 @@ __global__ void __launch_bounds__(1024) accumulate_kernel(const float* __restric
 // ranges only the CTA of a sample's range reads its features, and scanning the other ranges' samples costs a few
 // instructions per 128. The bins are flushed to the float64 sums once the samples added since the last flush could
 // reach FX_WINDOW (the limbs' headroom): each sample adds to one unit's bins, so no bin has more adds than that.
+// HOT (maps split into unit ranges): each sample slot also keeps one unit's sums in 64-bit registers (the first unit
+// it meets after a flush), so that a unit winning most samples, as on the contracted maps of early epochs, does not
+// serialise every warp on the same shared-memory words; those sums go to the float64 sums at each flush.
 constexpr int ACC_BATCH = 128;    // samples a warp scans at once (four per lane)
 constexpr int ACC_THREADS = 1024;
 
-template <int DP>
+template <int DP, bool HOT>
 __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const float* __restrict__ x,
                                                                        const double* __restrict__ rho,
                                                                        const int32_t* __restrict__ bmu, int64_t n,
@@ -259,6 +262,8 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
     const float sk = kval ? scale_s[k] : 0.0f;
     const bool vec = ((uintptr_t)bmu & 15u) == 0u;   // chunk starts are multiples of ACC_BATCH samples
     const uint32_t lt_mask = (1u << lane) - 1u;
+    int32_t hot = -1;              // HOT: this slot's register-held unit (relative to lo), -1 before the first sample
+    long long hacc = 0, hw = 0;    // its feature-k sum and its count (or weight sum) in fixed point
     const int64_t s0 = (int64_t)blockIdx.x * chunk;
     const int64_t s1 = min64(n, s0 + chunk);
     for (int64_t w0 = s0; w0 < s1; w0 += SCAN) {
@@ -297,6 +302,24 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
                 for (int t = 0; t < UNR; ++t) {
                     if (e[t] == 0xFFFFFFFFu) continue;
                     const int64_t u = e[t] & 0xFFFFu;
+                    if (HOT) {
+                        if (hot < 0) hot = (int32_t)u;   // the slot's lanes share the sample, so the choice too
+                        if (u == hot) {
+                            if (!rho) {
+                                if (kval) hacc += __float2ll_rn(xv[t] * sk);
+                                if (k == 0) hw += 1;
+                            } else {
+                                const float r = (float)__ldg(rho + base + (e[t] >> 16));
+                                if (kval) {
+                                    const float hi = r * xv[t];
+                                    const float lo_ = fmaf(r, xv[t], -hi);
+                                    hacc += __float2ll_rn(hi * sk) + __float2ll_rn(lo_ * sk);
+                                }
+                                if (k == 0) hw += __float2ll_rn(r * scale_s[d]);
+                            }
+                            continue;
+                        }
+                    }
                     if (!rho) {
                         if (kval) fx_add_float(limbs, nbf, u * d + k, xv[t] * sk);
                         if (k == 0) atomicAdd(csum + u, 1);
@@ -319,6 +342,13 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
         __syncthreads();   // every thread has read added_s
         if (!flush) continue;
         if (threadIdx.x == 0) added_s = 0;
+        if (HOT && hot >= 0) {
+            if (kval && hacc) atomicAdd(S + (lo + hot) * d + k, ldexp((double)hacc, exp_s[k] - FX_BITS));
+            if (k == 0 && hw) atomicAdd(c + lo + hot, rho ? ldexp((double)hw, exp_s[d] - FX_BITS) : (double)hw);
+            hacc = 0;
+            hw = 0;
+            hot = -1;
+        }
         for (int64_t q = threadIdx.x; q < nbf + cnt; q += blockDim.x) {
             long long v;
             int kk;
@@ -588,16 +618,19 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
     const size_t smem = (size_t)(upr * per_unit) + lists;
     const int64_t ctas_per_sm = smem <= 100 * 1024 ? 2 : 1;
     const int64_t ctas_wanted = ctas_per_sm * (int64_t)num_sms();
-    int64_t chunks = std::max<int64_t>(1, ctas_wanted / ranges);
+    // Every unit range gets as many sample chunks as one wave has CTAs: a range that wins most samples (a contracted
+    // early map) is then spread over the whole GPU, and the block scheduler balances the ranges' unequal work.
+    int64_t chunks = std::max<int64_t>(1, ctas_wanted);
     int64_t chunk = std::max<int64_t>(4096, ceil_div(n, chunks));
     chunk = ceil_div(chunk, ACC_BATCH) * ACC_BATCH;
     chunks = ceil_div(n, chunk);
     const dim3 grid((unsigned)chunks, (unsigned)ranges);
     if (lanes) {
-        auto kern = accumulate_lanes_kernel<32>;
-        if (d <= 4) kern = accumulate_lanes_kernel<4>;
-        else if (d <= 8) kern = accumulate_lanes_kernel<8>;
-        else if (d <= 16) kern = accumulate_lanes_kernel<16>;
+        const bool hot = ranges > 1;
+        auto kern = hot ? accumulate_lanes_kernel<32, true> : accumulate_lanes_kernel<32, false>;
+        if (d <= 4) kern = hot ? accumulate_lanes_kernel<4, true> : accumulate_lanes_kernel<4, false>;
+        else if (d <= 8) kern = hot ? accumulate_lanes_kernel<8, true> : accumulate_lanes_kernel<8, false>;
+        else if (d <= 16) kern = hot ? accumulate_lanes_kernel<16, true> : accumulate_lanes_kernel<16, false>;
         if (smem > 48 * 1024)
             SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<grid, ACC_THREADS, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, bounds, S, c);

@@ -279,6 +279,7 @@ ACCUMULATE_CASES = [
     (2304, 24, 200_000, True, 'uniform'),
     (4096, 32, 200_000, True, 'clustered'),
     (64, 3, 500_000, False, 'one-unit'),
+    (4096, 32, 300_000, False, 'one-unit'),   # several unit ranges: the unit's sums held in registers
     (300, 7, 100_000, True, 'with-negatives'),
     (4096, 32, 150_001, False, 'unaligned'),
 ]
