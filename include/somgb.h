@@ -188,6 +188,19 @@ int somgb_find_bmus_noalloc(const float* x, int64_t n, int d, const float* w, in
                             somgb_stream_t stream);
 size_t somgb_find_bmus_noalloc_scratch_bytes(void);
 
+/*
+ * Weighted moments of a catalogue, the sums behind the covariance of the PCA initialisation (replaces Welford's
+ * update Covariance._update_welford_cov_sums, algo/covariance.py:24-44, used by SOM_PCA.train, algo/som_pca.py:181):
+ *   out[0] = W = sum w_i, out[1 .. d] = mean = sum w_i x_i / W,
+ *   out[1 + d .. 1 + d + d*d) = M2 = sum w_i (x_i - mean)(x_i - mean)^T (row-major, symmetric),
+ * over the samples whose features are all finite and whose weight w_i = rho[i] (1 when rho is NULL) is finite and
+ * positive; float64 sums ("="; out is overwritten). The covariance is M2 / (W - ddof); chunks combine on the host.
+ * 1 <= d <= 64. No workspace.
+ */
+int somgb_weighted_moments(const float* x, const double* rho, int64_t n, int d, double* out, somgb_stream_t stream);
+int somgb_weighted_moments_f64(const double* x, const double* rho, int64_t n, int d, double* out,
+                               somgb_stream_t stream);
+
 /* w_out_j = num_j / den_j where den_j > 1e-12, else 0 (algo/som_batch.py:481-486). */
 int somgb_divide(const double* num, const double* den, int64_t m, int d, float* w_out, somgb_stream_t stream);
 int somgb_divide_f64(const double* num, const double* den, int64_t m, int d, double* w_out, somgb_stream_t stream);

@@ -1,0 +1,90 @@
+"""PCA initialisation, covariance and the hyper-parameter grid search against the reference's own outputs
+(tests/golden/pca_*.npz and hyparam_search.npz, written by tests/golden/make_pca_golden.py)."""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+
+def test_pca_grid_weights_from_the_reference_covariance():
+    """The host half of SOM_PCA (eigen-decomposition and grid) reproduces the reference's weights from the same
+    covariance (the reference's own Welford result), without a GPU."""
+    from decontamination_gb300.som_pca import SOM_PCA
+    g = golden('pca_init')
+    c = golden('pca_covariance')
+    cov = c['cov_plain']
+    for tag, m, n, kw in [('plain', 5, 7, {}), ('scaled', 6, 4, dict(scale_by_variance=True, min_weight=-1.0)),
+                          ('cdf', 4, 4, dict(apply_cdf=True, cdf_gain=1.5))]:
+        ev, _, w = SOM_PCA._grid_weights(cov, kw.get('min_weight', 0.0), kw.get('max_weight', 1.0), m, n, 6,
+                                         kw.get('scale_by_variance', False), kw.get('apply_cdf', False),
+                                         kw.get('cdf_gain', 1.0))
+        np.testing.assert_allclose(w.astype(np.float32).reshape(m * n, 6), g[f'{tag}_weights'], rtol=1e-6, atol=1e-7)
+        np.testing.assert_allclose(ev.astype(np.float32), g[f'{tag}_eigenvalues'], rtol=1e-6)
+
+
+def test_grid_points_follow_the_reference():
+    from decontamination_gb300.hyparam_finder_som import HypParamFinder_SOM
+    g = golden('hyparam_search')
+    pts = HypParamFinder_SOM(g['x']).grid()
+    assert len(pts) == 64
+    assert (int(g['m']), float(g['sigma'])) in pts
+    assert all(isinstance(m, int) for m, _ in pts)
+    with pytest.raises(NotImplementedError):
+        HypParamFinder_SOM(g['x'], batch=False).find(1)
+
+
+@pytest.mark.gpu
+def test_covariance_on_the_gpu(cuda):
+    import decontamination_gb300 as dg
+    c = golden('pca_covariance')
+    x, w = c['x'], c['w']
+    np.testing.assert_allclose(dg.Covariance.compute(6, x), c['cov_plain'], rtol=1e-10, atol=1e-13)
+    chunks = lambda: (lambda: (x[a:a + 700] for a in range(0, 3000, 700)))
+    wchunks = lambda: (lambda: (w[a:a + 700] for a in range(0, 3000, 700)))
+    np.testing.assert_allclose(dg.Covariance.compute(6, chunks, wchunks, ddof=0), c['cov_weighted_ddof0'],
+                               rtol=1e-10, atol=1e-13)
+    # device tensors, float64 data, a large catalogue against numpy's float64 two-pass result
+    rng = np.random.default_rng(7)
+    big = rng.standard_normal((3_000_000, 16)).astype(np.float32) * rng.random(16).astype(np.float32) + 3.0
+    ref = np.cov(big.astype(np.float64), rowvar=False, ddof=1)
+    np.testing.assert_allclose(dg.Covariance.compute(16, torch.from_numpy(big).to(cuda)), ref, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(dg.Covariance.compute(6, x.astype(np.float64)), c['cov_plain'], rtol=1e-10, atol=1e-13)
+    with pytest.raises(ValueError):
+        dg.Covariance.compute(6, x[:1])
+
+
+@pytest.mark.gpu
+def test_som_pca_train(cuda):
+    import decontamination_gb300 as dg
+    g = golden('pca_init')
+    for tag, m, n, topo, kw in [('plain', 5, 7, 'hexagonal', {}),
+                                ('scaled', 6, 4, 'square', dict(scale_by_variance=True, min_weight=-1.0)),
+                                ('cdf', 4, 4, 'hexagonal', dict(apply_cdf=True, cdf_gain=1.5))]:
+        som = dg.SOM_PCA(m, n, 6, topology=topo)
+        som.train(g['x'], **kw)
+        np.testing.assert_allclose(som.weights, g[f'{tag}_weights'].reshape(som.weights.shape), rtol=1e-5,
+                                   atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_hyparam_search_matches_the_reference(cuda):
+    import decontamination_gb300 as dg
+    g = golden('hyparam_search')
+    m, alpha, sigma, idx, qes, tes = dg.HypParamFinder_SOM(g['x'], topology='hexagonal').find(2)
+    assert (m, idx) == (int(g['m']), int(g['idx'])) and alpha is None
+    assert sigma == pytest.approx(float(g['sigma']), rel=1e-12)
+    # the reference's pure-Python mode sums distances in float32 (the GPU follows the compiled reference's float64):
+    # the quantization errors agree to float32 rounding, the topographic errors do not on a hexagonal map, whose
+    # nearest neighbours sit at squared topographic distance 1.0, the penalty itself
+    np.testing.assert_allclose(qes, g['qes'], rtol=1e-5)
+    # the winning grid point trained directly gives the same errors
+    x = g['x']
+    pca = dg.SOM_PCA(m, m, 4, topology='hexagonal')
+    pca.train(x)
+    som = dg.SOM_Batch(m, m, 4, topology='hexagonal', sigma=sigma)
+    som.init_from(pca)
+    som.train(x, n_epochs=2)
+    np.testing.assert_allclose(som.quantization_errors, qes, rtol=1e-12)
+    np.testing.assert_allclose(som.topographic_errors, tes, rtol=1e-12)
