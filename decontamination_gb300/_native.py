@@ -49,6 +49,8 @@ SIGNATURES = {
     'somgb_feature_bounds': [P, P, I64, I32, P, P],
     'somgb_accumulate_f64': [P, P, P, I64, I32, I64, P, P, P],
     'somgb_weighted_moments': [P, P, I64, I32, P, P],
+    'somgb_footprint_maps': [P, P, I64, I32, P, I64, I32, P, P, P, P, SZ, P],
+    'somgb_footprint_maps_f64': [P, P, I64, I32, P, I64, P, P, P, P],
     'somgb_weighted_moments_f64': [P, P, I64, I32, P, P],
     'somgb_find_bmus': [P, I64, I32, P, I64, I32, P, P, SZ, P],
     'somgb_find_bmus_f64': [P, I64, I32, P, I64, P, P],

@@ -13,6 +13,8 @@ template <typename T>
 int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
                       const float* bounds, double* S, double* c, cudaStream_t stream);
 int launch_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, cudaStream_t stream);
+int launch_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_w, double* hist_c,
+                          cudaStream_t stream);
 template <typename T>
 int launch_neighbourhood(const double* S, const double* c, const T* topo, int64_t m, int d, double sigma, T* w_out,
                          double* num, double* den, cudaStream_t stream);
@@ -214,6 +216,21 @@ int somgb_count_bmus(const float* x, const double* rho, int64_t n, int d, const 
     PassArgs a{};
     a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.hist = hist; a.outs = OUT_HIST;
     return run_pass(a, algo, W, tc, (cudaStream_t)stream);
+}
+
+int somgb_footprint_maps(const float* x, const double* rho, int64_t n, int d, const float* w, int64_t m, int algo,
+                         int32_t* bmu_out, double* hist_weighted, double* hist_count, void* ws, size_t ws_bytes,
+                         somgb_stream_t stream) {
+    if (n > 0 && !bmu_out) return set_error(SOMGB_ERR_INVALID, "bmu_out is NULL");
+    if (int s = somgb_find_bmus(x, n, d, w, m, algo, bmu_out, ws, ws_bytes, stream)) return s;
+    return launch_bmu_histograms(bmu_out, rho, n, m, hist_weighted, hist_count, (cudaStream_t)stream);
+}
+
+int somgb_footprint_maps_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,
+                             int32_t* bmu_out, double* hist_weighted, double* hist_count, somgb_stream_t stream) {
+    if (n > 0 && !bmu_out) return set_error(SOMGB_ERR_INVALID, "bmu_out is NULL");
+    if (int s = somgb_find_bmus_f64(x, n, d, w, m, bmu_out, stream)) return s;
+    return launch_bmu_histograms(bmu_out, rho, n, m, hist_weighted, hist_count, (cudaStream_t)stream);
 }
 
 int somgb_compute_errors(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,

@@ -575,6 +575,56 @@ __global__ void divide_kernel(const double* __restrict__ num, const double* __re
 
 }  // namespace
 
+// Both activation maps of a footprint from its BMUs (the fused form of two get_activation_map calls,
+// decontamination_som.py:640-641): hist_w[b_i] += rho_i for rho_i > 0, hist_c[b_i] += 1 for every sample. Per-CTA
+// bins in shared memory when the map fits (float64 shared atomics), flushed with one global atomic per non-zero bin.
+constexpr int HIST_THREADS = 1024;
+constexpr int64_t HIST_SMEM_UNITS = 6144;   // 2 x 6144 float64 bins = 96 KB
+
+__global__ void __launch_bounds__(HIST_THREADS) bmu_histograms_kernel(const int32_t* __restrict__ bmu,
+                                                                      const double* __restrict__ rho, int64_t n,
+                                                                      int64_t m, double* __restrict__ hist_w,
+                                                                      double* __restrict__ hist_c) {
+    extern __shared__ double hbins[];   // [2][m] when m <= HIST_SMEM_UNITS
+    const bool local = m <= HIST_SMEM_UNITS;
+    double* hw = local ? hbins : hist_w;
+    double* hc = local ? hbins + m : hist_c;
+    if (local) {
+        for (int64_t q = threadIdx.x; q < 2 * m; q += blockDim.x) hbins[q] = 0.0;
+        __syncthreads();
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = __ldg(bmu + i);
+        if (b < 0 || b >= m) continue;
+        if (hist_c) atomicAdd(hc + b, 1.0);
+        if (hist_w) {
+            const double r = rho ? __ldg(rho + i) : 1.0;
+            if (r > 0.0) atomicAdd(hw + b, r);
+        }
+    }
+    if (local) {
+        __syncthreads();
+        for (int64_t q = threadIdx.x; q < m; q += blockDim.x) {
+            if (hist_w && hbins[q] != 0.0) atomicAdd(hist_w + q, hbins[q]);
+            if (hist_c && hbins[m + q] != 0.0) atomicAdd(hist_c + q, hbins[m + q]);
+        }
+    }
+}
+
+int launch_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_w, double* hist_c,
+                          cudaStream_t stream) {
+    if (n == 0 || m == 0) return SOMGB_OK;
+    const bool local = m <= HIST_SMEM_UNITS;
+    const size_t smem = local ? (size_t)(2 * m) * sizeof(double) : 0;
+    if (smem > 48 * 1024)
+        SOMGB_CUDA_TRY(cudaFuncSetAttribute(bmu_histograms_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+    const int64_t blocks = std::min<int64_t>(ceil_div(n, HIST_THREADS), (int64_t)num_sms());
+    bmu_histograms_kernel<<<(unsigned)blocks, HIST_THREADS, smem, stream>>>(bmu, rho, n, m, hist_w, hist_c);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
 int launch_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, cudaStream_t stream) {
     if (n == 0) return SOMGB_OK;
     if (d <= 32) {

@@ -281,6 +281,36 @@ class SOM_Abstract(object):
         self._check_device()
         return h.astype(self._dtype).reshape((self._m, self._n))
 
+    def get_footprint_maps(self, dataset, dataset_weights=None) -> typing.Tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(weighted activation map, unweighted activation map, winners) of one array in a single BMU pass: the fused
+        form of ``get_activation_map(dataset, dataset_weights)``, ``get_activation_map(dataset)`` and
+        ``get_winners(dataset)`` that Decontamination_SOM calls on its footprint (decontamination_som.py:596,
+        640-641). Same values as the three calls."""
+        device = _device.require_cuda()
+        M, D = self._m * self._n, self._dim
+        x, rho, pieces = device_pieces(dataset, dataset_weights, self._dtype, device)
+        n = _device.rows(x)
+        winners = torch.empty(n, dtype=torch.int32, device=device)
+        hist_w = torch.zeros(M, dtype=torch.float64, device=device)
+        hist_c = torch.zeros(M, dtype=torch.float64, device=device)
+        w = self._device_weights()
+        for a, b in pieces:
+            xp, op = x[a:b], winners[a:b]
+            rp = None if rho is None else rho[a:b]
+            if self._is_f64:
+                _native.call('somgb_footprint_maps_f64', xp.data_ptr(), _device.ptr(rp), b - a, D, w.data_ptr(), M,
+                             op.data_ptr(), hist_w.data_ptr(), hist_c.data_ptr(), _device.stream())
+            else:
+                wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, b - a, M, D, self._algo, device)
+                _native.call('somgb_footprint_maps', xp.data_ptr(), _device.ptr(rp), b - a, D, w.data_ptr(), M,
+                             self._algo, op.data_ptr(), hist_w.data_ptr(), hist_c.data_ptr(), wsp, wsb,
+                             _device.stream())
+        cat = hist_w.cpu().numpy().astype(self._dtype).reshape((self._m, self._n))
+        foot = hist_c.cpu().numpy().astype(self._dtype).reshape((self._m, self._n))
+        res = winners.cpu().numpy()
+        self._check_device()
+        return cat, foot, res
+
     def get_winners(self, dataset, enable_gpu: bool = True,
                     threads_per_blocks: typing.Optional[int] = None) -> np.ndarray:
         """Best matching unit index of every row of `dataset`, int32 (algo/som_abstract.py:670-695)."""

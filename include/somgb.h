@@ -92,6 +92,18 @@ int somgb_find_bmus_f64(const double* x, int64_t n, int d, const double* w, int6
                         somgb_stream_t stream);
 
 /*
+ * Footprint maps in one BMU pass (the fused form of Decontamination_SOM.train's get_winners and compute_gndm's two
+ * get_activation_map calls, decontamination/decontamination_som.py:596, 640-641): bmu_out[i] as somgb_find_bmus,
+ * hist_weighted[b] += rho_i for rho_i > 0 and hist_count[b] += 1 for every sample (both float64 (m,) "+=", either
+ * may be NULL). Workspace: somgb_workspace_bytes(SOMGB_OP_FIND_BMUS, n, m, d, algo).
+ */
+int somgb_footprint_maps(const float* x, const double* rho, int64_t n, int d, const float* w, int64_t m, int algo,
+                         int32_t* bmu_out, double* hist_weighted, double* hist_count, void* ws, size_t ws_bytes,
+                         somgb_stream_t stream);
+int somgb_footprint_maps_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,
+                             int32_t* bmu_out, double* hist_weighted, double* hist_count, somgb_stream_t stream);
+
+/*
  * Activation histogram: hist[bmu(x_i)] += rho_i for rho_i > 0 (rho NULL = all ones); hist is float64 (m,) "+=".
  * Replaces _count_bmus_kernel (algo/som_abstract.py:700-732), called by get_activation_map (:605-666).
  */

@@ -88,3 +88,30 @@ def test_hyparam_search_matches_the_reference(cuda):
     som.train(x, n_epochs=2)
     np.testing.assert_allclose(som.quantization_errors, qes, rtol=1e-12)
     np.testing.assert_allclose(som.topographic_errors, tes, rtol=1e-12)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('N,dtype', [(50_000, np.float32), (2 * (1 << 20) + 777, np.float32), (40_000, np.float64)])
+def test_footprint_maps_fuse_the_three_calls(cuda, N, dtype):
+    """get_footprint_maps (one BMU pass + one histogram kernel) equals get_activation_map weighted and unweighted and
+    get_winners; compute_gndm follows the reference's _compute_gndm arithmetic on them."""
+    import decontamination_gb300 as dg
+    from decontamination_gb300.gndm import compute_gndm
+    rng = np.random.default_rng(N)
+    x = (rng.standard_normal((N, 8)) * 2.0).astype(dtype)
+    x[rng.integers(0, N, 20)] = np.nan
+    rho = rng.random(N) * 3.0
+    rho[rng.integers(0, N, 100)] = 0.0
+    som = dg.SOM_Batch(12, 10, 8, dtype=dtype, topology='square')
+    som.init_rand(seed=5)
+    som._weights[...] = som._weights * 4.0 - 2.0
+    cat, foot, win = som.get_footprint_maps(x, rho)
+    assert np.array_equal(win, som.get_winners(x))
+    np.testing.assert_allclose(cat, som.get_activation_map(x, rho), rtol=1e-12)
+    assert np.array_equal(foot, som.get_activation_map(x))
+    out = compute_gndm(som, x, rho)
+    gnd = np.full(cat.shape, np.nan, dtype=dtype)
+    np.divide(cat, foot, out=gnd, where=foot > 0.0)
+    np.testing.assert_allclose(out['gnd'], gnd, rtol=1e-12)
+    np.testing.assert_allclose(out['gndm'], gnd.reshape(-1)[win], rtol=1e-12)
+    assert out['n_pix'] == N
