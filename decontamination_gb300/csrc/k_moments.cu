@@ -17,7 +17,6 @@ namespace somgb {
 namespace {
 
 constexpr int MOM_THREADS = 256;
-constexpr int MOM_TILE = 128;   // samples per shared-memory tile in pass 2
 
 template <typename T>
 __device__ __forceinline__ bool sample_weight(const double* __restrict__ rho, int64_t i, double& w) {
@@ -78,53 +77,66 @@ __global__ void moments_mean_kernel(int d, double* __restrict__ out) {
     if (k < d) out[1 + k] = out[0] > 0.0 ? out[1 + k] / out[0] : 0.0;
 }
 
-// Pass 2: out[1 + d + j*d + k] += sum w (x_j - mean_j)(x_k - mean_k) for j <= k.
+// Pass 2: out[1 + d + j*d + k] += sum w (x_j - mean_j)(x_k - mean_k) for j <= k. A tile of `tile` samples is read
+// coalesced into shared memory as float64, each sample's weight and validity are taken from it, and the tile is
+// centred and scaled by sqrt(w) in place (zero for samples that do not count). Thread t owns pair t % P (and, when
+// the pairs are more than the block, t + blockDim ...) over the samples g, g + G, ... with g = t / P.
 template <typename T>
-__global__ void __launch_bounds__(MOM_THREADS) moments2_kernel(const T* __restrict__ x, const double* __restrict__ rho,
-                                                               int64_t n, int d, double* __restrict__ out) {
-    extern __shared__ double tile[];   // [MOM_TILE][d]: sqrt(w) (x - mean), zero for samples that do not count
-    const double* mean = out + 1;
+__global__ void __launch_bounds__(1024) moments2_kernel(const T* __restrict__ x, const double* __restrict__ rho,
+                                                        int64_t n, int d, int tile, double* __restrict__ out) {
+    extern __shared__ double sm[];   // [tile][d] centred rows, then [tile] sqrt(w), then [d] mean
+    double* rows = sm;
+    double* sw = sm + (size_t)tile * d;
+    double* mean = sw + tile;
     double* m2 = out + 1 + d;
     const int P = d * (d + 1) / 2;
-    const int groups = P >= MOM_THREADS ? 1 : MOM_THREADS / P;
-    const int g = threadIdx.x / (P >= MOM_THREADS ? MOM_THREADS : P);
-    const int p0 = threadIdx.x % (P >= MOM_THREADS ? MOM_THREADS : P);
-    constexpr int MAXP = 9;   // pairs per thread: d <= 64 gives P <= 2080 <= 9 * 256
+    const int nt = blockDim.x;
+    const int G = P >= nt ? 1 : nt / P;
+    const int g = threadIdx.x / (P >= nt ? nt : P);
+    const int p0 = threadIdx.x % (P >= nt ? nt : P);
+    constexpr int MAXP = 3;   // d <= 64: P <= 2080 <= 3 * 1024 (blocks of fewer threads only when P is smaller)
     double acc[MAXP];
     int pj[MAXP], pk[MAXP];
 #pragma unroll
     for (int q = 0; q < MAXP; ++q) {
         acc[q] = 0.0;
-        int p = p0 + q * MOM_THREADS, j = 0;
-        // pair p of the row-major upper triangle
-        while (p >= d - j && j < d) { p -= d - j; ++j; }
-        pj[q] = j;
-        pk[q] = j + p;
+        int p = p0 + q * nt, j = 0;
+        while (j < d && p >= d - j) { p -= d - j; ++j; }   // pair p of the row-major upper triangle
+        pj[q] = j < d ? j : 0;
+        pk[q] = j < d ? j + p : 0;
     }
-    for (int64_t t0 = (int64_t)blockIdx.x * MOM_TILE; t0 < n; t0 += (int64_t)gridDim.x * MOM_TILE) {
+    for (int k = threadIdx.x; k < d; k += nt) mean[k] = out[1 + k];
+    for (int64_t t0 = (int64_t)blockIdx.x * tile; t0 < n; t0 += (int64_t)gridDim.x * tile) {
+        const int rows_here = (int)min64(tile, n - t0);
         __syncthreads();
-        for (int idx = threadIdx.x; idx < MOM_TILE; idx += MOM_THREADS) {
-            const int64_t i = t0 + idx;
+        for (int q = threadIdx.x; q < tile * d; q += nt)
+            rows[q] = q < rows_here * d ? (double)x[t0 * d + q] : 0.0;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < tile; idx += nt) {
             double w = 0.0;
-            bool ok = i < n && sample_weight<T>(rho, i < n ? i : 0, w);
-            for (int k = 0; ok && k < d; ++k) ok = isfinite((double)x[i * d + k]);
-            const double s = ok ? sqrt(w) : 0.0;
-            for (int k = 0; k < d; ++k) tile[idx * d + k] = ok ? s * ((double)x[i * d + k] - mean[k]) : 0.0;
+            bool ok = idx < rows_here && sample_weight<T>(rho, t0 + (idx < rows_here ? idx : 0), w);
+            for (int k = 0; ok && k < d; ++k) ok = isfinite(rows[idx * d + k]);
+            sw[idx] = ok ? sqrt(w) : 0.0;
         }
         __syncthreads();
-        if (g < groups) {
-            for (int sidx = g; sidx < MOM_TILE; sidx += groups) {
-                const double* r = tile + sidx * d;
+        for (int q = threadIdx.x; q < tile * d; q += nt) {
+            const double s = sw[q / d];
+            rows[q] = s != 0.0 ? s * (rows[q] - mean[q % d]) : 0.0;
+        }
+        __syncthreads();
+        if (g < G) {
+            for (int sidx = g; sidx < rows_here; sidx += G) {
+                const double* r = rows + sidx * d;
 #pragma unroll
                 for (int q = 0; q < MAXP; ++q)
-                    if (p0 + q * MOM_THREADS < P) acc[q] = fma(r[pj[q]], r[pk[q]], acc[q]);
+                    if (p0 + q * nt < P) acc[q] = fma(r[pj[q]], r[pk[q]], acc[q]);
             }
         }
     }
-    if (g < groups) {
+    if (g < G) {
 #pragma unroll
         for (int q = 0; q < MAXP; ++q)
-            if (p0 + q * MOM_THREADS < P && acc[q] != 0.0) atomicAdd(m2 + pj[q] * d + pk[q], acc[q]);
+            if (p0 + q * nt < P && acc[q] != 0.0) atomicAdd(m2 + pj[q] * d + pk[q], acc[q]);
     }
 }
 
@@ -152,11 +164,15 @@ int launch_moments(const T* x, const double* rho, int64_t n, int d, double* out,
     SOMGB_LAUNCH_CHECK();
     moments_mean_kernel<<<1, 64, 0, stream>>>(d, out);
     SOMGB_LAUNCH_CHECK();
-    const size_t smem = (size_t)MOM_TILE * d * sizeof(double);
+    // block: every pair once, repeated over sample groups up to 1024 threads; tile: up to 96 KB of float64 rows
+    const int P = d * (d + 1) / 2;
+    const int threads2 = P >= 1024 ? 1024 : (1024 / P) * P;
+    const int tile = (int)std::max<int64_t>(32, std::min<int64_t>(1024, (96 * 1024) / (8 * d)));
+    const size_t smem = ((size_t)tile * d + tile + d) * sizeof(double);
     auto k2 = moments2_kernel<T>;
     if (smem > 48 * 1024) SOMGB_CUDA_TRY(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t b2 = std::min<int64_t>(ceil_div(n, MOM_TILE), 4 * (int64_t)num_sms());
-    k2<<<(unsigned)b2, MOM_THREADS, smem, stream>>>(x, rho, n, d, out);
+    const int64_t b2 = std::min<int64_t>(ceil_div(n, tile), 2 * (int64_t)num_sms());
+    k2<<<(unsigned)b2, threads2, smem, stream>>>(x, rho, n, d, tile, out);
     SOMGB_LAUNCH_CHECK();
     moments_mirror_kernel<<<(unsigned)ceil_div((int64_t)d * d, 256), 256, 0, stream>>>(d, out);
     SOMGB_LAUNCH_CHECK();
