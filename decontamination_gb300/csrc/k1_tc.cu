@@ -771,8 +771,27 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
                 TC_T(0);
                 ptx::tc_fence_after();
-                // groups of 8 columns: chunks 0 and 2 feed (a1, a2), chunks 1 and 3 feed (b1, b2)
+                // ERR on maps of at most 8 column tiles (resolver-bound): groups of 4 columns, alternately feeding
+                // (a1, a2) and (b1, b2), so that the second-smallest group minimum stays close to the second-smallest
+                // value (fewer candidates for the resolvers). Otherwise groups of 8 (fewer sweep instructions): chunks
+                // 0 and 2 feed (a1, a2), chunks 1 and 3 feed (b1, b2).
                 stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                    if (ERR && !LARGE) {
+#pragma unroll
+                        for (int g4 = 0; g4 < 32; g4 += 4) {
+                            const float g = fminf(fmin3(__uint_as_float(r[g4]), __uint_as_float(r[g4 + 1]),
+                                                        __uint_as_float(r[g4 + 2])),
+                                                  __uint_as_float(r[g4 + 3]));
+                            if ((g4 >> 2) & 1) {
+                                b2 = fminf(b2, fmaxf(b1, g));
+                                b1 = fminf(b1, g);
+                            } else {
+                                a2 = fminf(a2, fmaxf(a1, g));
+                                a1 = fminf(a1, g);
+                            }
+                        }
+                        return;
+                    }
 #pragma unroll
                     for (int g8 = 0; g8 < 32; g8 += 8) {
                         const float g = fmin3(fmin3(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1]),
@@ -804,7 +823,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 M2 = fminf(fminf(M2, p.y), fmaxf(M1, p.x));
                 M1 = fminf(M1, p.x);
             }
-            // ERR: M2 is the second smallest 8-unit group minimum, an upper bound of the second smallest s~ (two
+            // ERR: M2 is the second smallest 4- or 8-unit group minimum, an upper bound of the second smallest s~ (two
             // groups have a unit at or below it), so the threshold derived from it keeps every possible second BMU
             const float mref = ERR ? M2 : M1;
             if (!(M1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
