@@ -37,11 +37,15 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(name='hex 32x32 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=16, 20-epoch schedule',
                 m=32, n=32, d=16, N=12_582_912, topology='hexagonal', sigma0=16.0, schedule=20, seed=2)
 # the larger training configuration (square 64x64 map, D = 32, N = 50,331,648 = HEALPix nside 2048), measured with
-# --workload sq64
+# --workload sq64, and the 64x64, D = 16 map over the default catalogue (--workload sq64d16)
 WORKLOADS = {'hex32': WORKLOAD,
              'sq64': dict(name='square 64x64 SOM, D=32, N=50331648 (HEALPix nside=2048 pixel count), sigma0=32, '
                                '20-epoch schedule', m=64, n=64, d=32, N=50_331_648, topology='square', sigma0=32.0,
-                          schedule=20, seed=3)}
+                          schedule=20, seed=3),
+             # the speed-up target's shape: a 64x64 map with D = 16 over the 12.6 M-row catalogue
+             'sq64d16': dict(name='square 64x64 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=32, '
+                                  '20-epoch schedule', m=64, n=64, d=16, N=12_582_912, topology='square', sigma0=32.0,
+                             schedule=20, seed=2)}
 METRIC = 'SOM epoch Gsample·unit/s'
 # DRAM traffic (bytes read + written) of one tensor-core BMU pass per catalogue row, from an ncu capture of
 # tc_pass_kernel on the 4,194,304-row case of this workload (summary under profiles/). The pass streams every row
