@@ -454,7 +454,7 @@ def serve_arm(args):
         mid = srv.add_map(som)
         # warm-up: every request shape class once (library state, pinned staging buffers)
         for n in (1_000, 100_000, 2_000_000):
-            srv.submit_bmu(mid, pool[:n]).result()
+            srv.submit_bmu(mid, pool[:n], histogram=True).result()
         futs = [None] * n_req
         t0 = time.perf_counter()
 
@@ -463,7 +463,7 @@ def serve_arm(args):
                 delay = t0 + arrivals[i] - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                futs[i] = srv.submit_bmu(mid, pool[starts[i]:starts[i] + sizes[i]])
+                futs[i] = srv.submit_bmu(mid, pool[starts[i]:starts[i] + sizes[i]], histogram=True)
 
         th = threading.Thread(target=feeder)
         th.start()
@@ -486,7 +486,8 @@ def serve_arm(args):
         'passes': len(srv.batch_sizes()), 'dtype': 'f16x3-split/f32acc' if algo_used == 'tc' else 'f32',
         'data': 'synthetic (seeded 5-component Gaussian mixture, D = 16); requests are slices of a pinned 1e7-row '
                 'catalogue', 'config': {'workload': s['name'], 'algo': algo_used, 'rate': args.serve_rate,
-                                         'window_s': args.serve_seconds, 'max_batch_rows': 1 << 20},
+                                         'window_s': args.serve_seconds, 'max_batch_rows': 1 << 20,
+                                         'workers': srv.workers, 'returns': 'int32 BMUs + M-bin activation histogram'},
     }
     print(json.dumps(out), flush=True)
 

@@ -51,6 +51,7 @@ SIGNATURES = {
     'somgb_weighted_moments': [P, P, I64, I32, P, P],
     'somgb_footprint_maps': [P, P, I64, I32, P, I64, I32, P, P, P, P, SZ, P],
     'somgb_footprint_maps_f64': [P, P, I64, I32, P, I64, P, P, P, P],
+    'somgb_bmu_histograms': [P, P, I64, I64, P, P, P],
     'somgb_weighted_moments_f64': [P, P, I64, I32, P, P],
     'somgb_find_bmus': [P, I64, I32, P, I64, I32, P, P, SZ, P],
     'somgb_find_bmus_f64': [P, I64, I32, P, I64, P, P],

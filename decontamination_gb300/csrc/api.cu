@@ -218,6 +218,12 @@ int somgb_count_bmus(const float* x, const double* rho, int64_t n, int d, const 
     return run_pass(a, algo, W, tc, (cudaStream_t)stream);
 }
 
+int somgb_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_weighted,
+                         double* hist_count, somgb_stream_t stream) {
+    if (n < 0 || m < 0 || (n > 0 && !bmu)) return set_error(SOMGB_ERR_INVALID, "bad BMU array");
+    return launch_bmu_histograms(bmu, rho, n, m, hist_weighted, hist_count, (cudaStream_t)stream);
+}
+
 int somgb_footprint_maps(const float* x, const double* rho, int64_t n, int d, const float* w, int64_t m, int algo,
                          int32_t* bmu_out, double* hist_weighted, double* hist_count, void* ws, size_t ws_bytes,
                          somgb_stream_t stream) {

@@ -8,9 +8,12 @@ requests as they arrive, from any thread, and returns futures:
 * requests are admitted in arrival order when their device-memory footprint (catalogue, outputs, workspace) fits the
   budget; a request that can never fit is rejected with ``MemoryError``;
 * consecutive small BMU-assignment requests on the same map are packed into one pinned host buffer and served by one
-  upload, one BMU pass and one download;
-* activation-map and error requests run one at a time on the serving stream; training requests run on their own
-  thread and stream, so that a long training does not hold up assignments;
+  upload, one BMU pass and one download; a BMU request can also return its M-bin activation histogram;
+* ``workers`` serving threads (default 2) take admitted batches as they free up, each on its own stream with its own
+  staging buffers and workspaces, so that a request arriving while another is on the GPU overlaps it on the device;
+  the first worker takes requests in arrival order, the others only packable BMU requests (ahead of larger ones), so
+  that small requests run beside a large one rather than behind it;
+  training requests run on their own thread and stream, so that a long training does not hold up assignments;
 * a request whose computation raises fails alone: its future carries the exception and the loop goes on;
 * latency (submit to result on the host) is recorded per kind; ``stats()`` gives count, p50 and p99.
 """
@@ -42,18 +45,27 @@ def _rows(x):
     return int(x.shape[0])
 
 
-class GpuExecutor:
-    """Runs the requests through libsomgb on a CUDA device (float32 maps)."""
+class _Slot:
+    """One serving worker's device resources: its stream and pinned host buffers."""
 
-    def __init__(self, device=None):
+    def __init__(self, torch, device):
+        self.stream = torch.cuda.Stream(device=device)
+        self.stage = None   # pinned host staging buffer for packed requests
+        self.out = None     # pinned host buffer for packed results
+
+
+class GpuExecutor:
+    """Runs the requests through libsomgb on a CUDA device (float32 maps). `slot` (0 .. workers - 1) selects the
+    calling worker's stream, buffers and per-map workspace and map object, so that workers never share scratch."""
+
+    def __init__(self, device=None, workers=2):
         import torch
         from . import _device, _native
         self._torch, self._dev_mod, self._nat = torch, _device, _native
         self.device = device if device is not None else _device.require_cuda()
-        self.stream = torch.cuda.Stream(device=self.device)
+        self.slots = [_Slot(torch, self.device) for _ in range(max(1, workers))]
+        self.stream = self.slots[0].stream
         self.train_stream = torch.cuda.Stream(device=self.device)
-        self._stage = None      # pinned host staging buffer for packed requests
-        self._out = None        # pinned host buffer for packed results
 
     def free_bytes(self):
         free, _ = self._torch.cuda.mem_get_info(self.device)
@@ -66,15 +78,18 @@ class GpuExecutor:
         from .som_abstract import SOM_Abstract
         if som.dtype != np.float32:
             raise TypeError('the serving loop holds float32 maps')
-        own = SOM_Abstract(som.m, som.n, som.dim, som.dtype, som.topology)
-        own._weights[...] = som._weights
-        own.bmu_algo = som.bmu_algo
+        owns = []
+        for _ in self.slots:
+            own = SOM_Abstract(som.m, som.n, som.dim, som.dtype, som.topology)
+            own._weights[...] = som._weights
+            own.bmu_algo = som.bmu_algo
+            owns.append(own)
         torch = self._torch
         with torch.cuda.stream(self.stream):
-            w = torch.from_numpy(np.ascontiguousarray(own.weights.reshape(-1, own.dim))).to(self.device)
+            w = torch.from_numpy(np.ascontiguousarray(owns[0].weights.reshape(-1, owns[0].dim))).to(self.device)
         self.stream.synchronize()
-        return {'som': own, 'w': w, 'M': own.m * own.n, 'D': own.dim, 'algo': own._algo,
-                'ws': self._dev_mod.Workspace()}
+        return {'soms': owns, 'w': w, 'M': owns[0].m * owns[0].n, 'D': owns[0].dim, 'algo': owns[0]._algo,
+                'ws': [self._dev_mod.Workspace() for _ in self.slots]}
 
     def footprint(self, entry, kind, n, weighted):
         nat = self._nat
@@ -84,27 +99,30 @@ class GpuExecutor:
         return b + nat.workspace_bytes(op, max(n, 1), M, D, entry['algo'])
 
     # --- requests ------------------------------------------------------------------------------------------------------
-    def _pinned(self, attr, nbytes):
+    def _pinned(self, sl, attr, nbytes):
         torch = self._torch
-        buf = getattr(self, attr)
+        buf = getattr(sl, attr)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8).pin_memory()
-            setattr(self, attr, buf)
+            setattr(sl, attr, buf)
         return buf
 
-    def run_bmu(self, entry, xs):
-        """BMUs of every request in `xs` (host arrays or device tensors), packed into one pass."""
+    def run_bmu(self, entry, xs, slot=0, hist=None):
+        """BMUs of every request in `xs` (host arrays or device tensors), packed into one pass; request i also gets
+        its activation histogram (unweighted, float64 (M,)) when hist[i], as a (bmu, histogram) pair."""
         torch, nat = self._torch, self._nat
+        sl = self.slots[slot]
         M, D = entry['M'], entry['D']
         counts = [_rows(x) for x in xs]
         n = sum(counts)
-        with torch.cuda.stream(self.stream):
+        hist = hist or [False] * len(xs)
+        with torch.cuda.stream(sl.stream):
             one = xs[0] if len(xs) == 1 and isinstance(xs[0], torch.Tensor) else None
             if one is not None and (one.is_cuda or one.is_pinned()):
                 # device tensor, or pinned host memory: no staging copy
                 xd = one.to(device=self.device, dtype=torch.float32, non_blocking=True).contiguous()
             else:
-                stage = self._pinned('_stage', n * D * 4)
+                stage = self._pinned(sl, 'stage', n * D * 4)
                 host = stage[:n * D * 4].view(torch.float32).view(n, D)
                 hv = host.numpy()
                 r = 0
@@ -113,28 +131,45 @@ class GpuExecutor:
                     r += c
                 xd = host.to(self.device, non_blocking=True)
             out = torch.empty(n, dtype=torch.int32, device=self.device)
+            nh = sum(1 for h in hist if h)
+            hd = torch.zeros((max(nh, 1), M), dtype=torch.float64, device=self.device) if nh else None
             if n:
-                wsp, wsb = entry['ws'].for_op(nat.OP_FIND_BMUS, n, M, D, entry['algo'], self.device)
+                wsp, wsb = entry['ws'][slot].for_op(nat.OP_FIND_BMUS, n, M, D, entry['algo'], self.device)
                 nat.call('somgb_find_bmus', xd.data_ptr(), n, D, entry['w'].data_ptr(), M, entry['algo'],
-                         out.data_ptr(), wsp, wsb, self.stream.cuda_stream)
-            ob = self._pinned('_out', n * 4)
+                         out.data_ptr(), wsp, wsb, sl.stream.cuda_stream)
+                r, k = 0, 0
+                for c, h in zip(counts, hist):
+                    if h:
+                        nat.call('somgb_bmu_histograms', out[r:].data_ptr(), None, c, M, None, hd[k].data_ptr(),
+                                 sl.stream.cuda_stream)
+                        k += 1
+                    r += c
+            ob = self._pinned(sl, 'out', n * 4 + 8 + nh * M * 8)
             oh = ob[:n * 4].view(torch.int32)
             oh.copy_(out, non_blocking=True)
-        self.stream.synchronize()
+            if nh:
+                hh = ob[n * 4 + (-(n * 4)) % 8:][:nh * M * 8].view(torch.float64).view(nh, M)
+                hh.copy_(hd[:nh], non_blocking=True)
+        sl.stream.synchronize()
         res = oh.numpy().copy()
-        parts, r = [], 0
-        for c in counts:
-            parts.append(res[r:r + c])
+        hres = hh.numpy().copy() if nh else None
+        parts, r, k = [], 0, 0
+        for c, h in zip(counts, hist):
+            if h:
+                parts.append((res[r:r + c], hres[k]))
+                k += 1
+            else:
+                parts.append(res[r:r + c])
             r += c
         return parts
 
-    def run_activation(self, entry, x, rho):
-        with self._torch.cuda.stream(self.stream):
-            return entry['som'].get_activation_map(x, rho)
+    def run_activation(self, entry, x, rho, slot=0):
+        with self._torch.cuda.stream(self.slots[slot].stream):
+            return entry['soms'][slot].get_activation_map(x, rho)
 
-    def run_errors(self, entry, x, rho):
-        with self._torch.cuda.stream(self.stream):
-            return entry['som'].compute_errors(x, rho)
+    def run_errors(self, entry, x, rho, slot=0):
+        with self._torch.cuda.stream(self.slots[slot].stream):
+            return entry['soms'][slot].compute_errors(x, rho)
 
     def run_train(self, som, dataset, rho, kwargs):
         with self._torch.cuda.stream(self.train_stream):
@@ -148,10 +183,12 @@ class SomServer:
     executor: the object that runs requests (default: ``GpuExecutor`` on the current CUDA device).
     hbm_budget: device bytes that admitted requests may hold at once (default: 80 % of the free memory at start).
     max_batch_rows: BMU requests with at most this many rows are packed together, up to this many rows per pass.
+    workers: serving threads taking admitted batches (the executor keeps a stream and buffers per worker).
     """
 
-    def __init__(self, executor=None, hbm_budget=None, max_batch_rows=1 << 20):
-        self._ex = executor if executor is not None else GpuExecutor()
+    def __init__(self, executor=None, hbm_budget=None, max_batch_rows=1 << 20, workers=2):
+        self.workers = max(1, int(workers))
+        self._ex = executor if executor is not None else GpuExecutor(workers=self.workers)
         self.hbm_budget = int(hbm_budget if hbm_budget is not None else 0.8 * self._ex.free_bytes())
         self.max_batch_rows = int(max_batch_rows)
         self._maps = {}
@@ -162,8 +199,9 @@ class SomServer:
         self._closing = False
         self._lat = {k: [] for k in KINDS}
         self._batches = []
-        self._threads = [threading.Thread(target=self._serve_loop, name='somgb-serve', daemon=True),
-                         threading.Thread(target=self._train_loop, name='somgb-train', daemon=True)]
+        self._threads = [threading.Thread(target=self._serve_loop, args=(i,), name=f'somgb-serve-{i}', daemon=True)
+                         for i in range(self.workers)]
+        self._threads.append(threading.Thread(target=self._train_loop, name='somgb-train', daemon=True))
         for t in self._threads:
             t.start()
 
@@ -176,9 +214,10 @@ class SomServer:
             self._maps[mid] = entry
         return mid
 
-    def submit_bmu(self, map_id, x):
-        """Future of the int32 BMU of every row of `x` (``get_winners``)."""
-        return self._submit('bmu', map_id, x, None)
+    def submit_bmu(self, map_id, x, histogram=False):
+        """Future of the int32 BMU of every row of `x` (``get_winners``); with `histogram`, of (BMUs, M-bin
+        activation histogram) (the unweighted ``get_activation_map`` of `x`, flattened, float64)."""
+        return self._submit('bmu', map_id, x, None, {'histogram': bool(histogram)})
 
     def submit_activation(self, map_id, x, rho=None):
         """Future of the activation map of `x` (``get_activation_map``)."""
@@ -245,14 +284,14 @@ class SomServer:
         if self._closing:
             raise RuntimeError('the server is closed')
 
-    def _submit(self, kind, map_id, x, rho):
+    def _submit(self, kind, map_id, x, rho, kwargs=None):
         n = _rows(x)
         with self._cv:
             self._check_open()
             if map_id not in self._maps:
                 raise KeyError(f'unknown map {map_id}')
             entry = self._maps[map_id]
-        req = _Request(kind, map_id, x, rho, n, self._ex.footprint(entry, kind, n, rho is not None))
+        req = _Request(kind, map_id, x, rho, n, self._ex.footprint(entry, kind, n, rho is not None), kwargs)
         with self._cv:
             if req.footprint > self.hbm_budget:
                 req.future.set_exception(MemoryError(f'request needs {req.footprint} device bytes, over the '
@@ -262,19 +301,29 @@ class SomServer:
             self._cv.notify_all()
         return req.future
 
-    def _admit(self, q):
-        """Pops the next batch from `q` once its footprint fits the budget (lock held); None when closing and empty."""
+    def _admit(self, q, small_only=False):
+        """Pops the next batch from `q` once its footprint fits the budget (lock held); None when closing and there
+        is nothing left for this worker. `small_only` (the extra workers): the first packable BMU request in the
+        queue, ahead of any larger one, so that small requests run beside a large one instead of behind it."""
         while True:
+            idx = None
             if q:
-                head = q[0]
+                if not small_only:
+                    idx = 0
+                else:
+                    idx = next((i for i, r in enumerate(q) if r.kind == 'bmu' and r.n <= self.max_batch_rows), None)
+            if idx is not None:
+                head = q[idx]
                 if self._in_flight + head.footprint <= self.hbm_budget:
-                    batch = [q.popleft()]
+                    del q[idx]
+                    batch = [head]
                     total_rows, total_fp = head.n, head.footprint
                     if head.kind == 'bmu' and head.n <= self.max_batch_rows:
-                        while q and q[0].kind == 'bmu' and q[0].map_id == head.map_id and \
-                                total_rows + q[0].n <= self.max_batch_rows and \
-                                self._in_flight + total_fp + q[0].footprint <= self.hbm_budget:
-                            nxt = q.popleft()
+                        while idx < len(q) and q[idx].kind == 'bmu' and q[idx].map_id == head.map_id and \
+                                total_rows + q[idx].n <= self.max_batch_rows and \
+                                self._in_flight + total_fp + q[idx].footprint <= self.hbm_budget:
+                            nxt = q[idx]
+                            del q[idx]
                             batch.append(nxt)
                             total_rows += nxt.n
                             total_fp += nxt.footprint
@@ -298,23 +347,24 @@ class SomServer:
                     self._lat[req.kind].append(t - req.t_submit)
             self._cv.notify_all()
 
-    def _serve_loop(self):
+    def _serve_loop(self, slot):
         while True:
             with self._cv:
-                batch, fp = self._admit(self._queue)
+                batch, fp = self._admit(self._queue, small_only=slot > 0)
             if batch is None:
                 return
             head = batch[0]
             try:
                 entry = self._maps[head.map_id]
                 if head.kind == 'bmu':
-                    res = self._ex.run_bmu(entry, [r.x for r in batch])
+                    res = self._ex.run_bmu(entry, [r.x for r in batch], slot=slot,
+                                           hist=[r.kwargs.get('histogram', False) for r in batch])
                     with self._cv:
                         self._batches.append(len(batch))
                 elif head.kind == 'activation':
-                    res = [self._ex.run_activation(entry, head.x, head.rho)]
+                    res = [self._ex.run_activation(entry, head.x, head.rho, slot=slot)]
                 else:
-                    res = [self._ex.run_errors(entry, head.x, head.rho)]
+                    res = [self._ex.run_errors(entry, head.x, head.rho, slot=slot)]
             except Exception as e:   # the request fails alone
                 self._finish(batch, fp, exc=e)
                 continue

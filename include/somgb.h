@@ -102,6 +102,9 @@ int somgb_footprint_maps(const float* x, const double* rho, int64_t n, int d, co
                          somgb_stream_t stream);
 int somgb_footprint_maps_f64(const double* x, const double* rho, int64_t n, int d, const double* w, int64_t m,
                              int32_t* bmu_out, double* hist_weighted, double* hist_count, somgb_stream_t stream);
+/* The histograms of somgb_footprint_maps from BMUs already computed (bmu[i] outside [0, m) is skipped). */
+int somgb_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_weighted,
+                         double* hist_count, somgb_stream_t stream);
 
 /*
  * Activation histogram: hist[bmu(x_i)] += rho_i for rho_i > 0 (rho NULL = all ones); hist is float64 (m,) "+=".

@@ -30,18 +30,20 @@ class FakeExecutor:
     def footprint(self, entry, kind, n, weighted):
         return 100 * n + (50 if weighted else 0)
 
-    def run_bmu(self, entry, xs):
+    def run_bmu(self, entry, xs, slot=0, hist=None):
         self.release.wait(5)
         self.bmu_batches.append([len(x) for x in xs])
         for x in xs:
             if np.isnan(np.asarray(x)).any():
                 raise ValueError('poisoned request')
-        return [np.full(len(x), int(np.asarray(x)[0, 0]), dtype=np.int32) for x in xs]
+        out = [np.full(len(x), int(np.asarray(x)[0, 0]), dtype=np.int32) for x in xs]
+        return [(o, np.bincount(o, minlength=4).astype(np.float64)) if h else o
+                for o, h in zip(out, hist or [False] * len(xs))]
 
-    def run_activation(self, entry, x, rho):
+    def run_activation(self, entry, x, rho, slot=0):
         return ('activation', entry['name'], len(x))
 
-    def run_errors(self, entry, x, rho):
+    def run_errors(self, entry, x, rho, slot=0):
         return (0.5, 0.25)
 
     def run_train(self, som, dataset, rho, kwargs):
@@ -56,7 +58,7 @@ def _req(v, n=10):
 
 def test_small_requests_on_one_map_are_packed():
     ex = FakeExecutor(block_first=True)
-    srv = SomServer(ex, max_batch_rows=1000)
+    srv = SomServer(ex, max_batch_rows=1000, workers=1)
     m0, m1 = srv.add_map('a'), srv.add_map('b')
     first = srv.submit_bmu(m0, _req(0))
     time.sleep(0.1)   # the loop now holds the first request inside the executor
@@ -74,7 +76,7 @@ def test_small_requests_on_one_map_are_packed():
 
 def test_row_cap_splits_packs():
     ex = FakeExecutor(block_first=True)
-    srv = SomServer(ex, max_batch_rows=100)
+    srv = SomServer(ex, max_batch_rows=100, workers=1)
     m = srv.add_map('a')
     f0 = srv.submit_bmu(m, _req(0, 40))
     time.sleep(0.1)
@@ -87,7 +89,7 @@ def test_row_cap_splits_packs():
     assert ex.bmu_batches == [[40], [40, 40], [40, 40], [40]]
     # a request above the cap is served alone
     ex2 = FakeExecutor()
-    with SomServer(ex2, max_batch_rows=100) as srv2:
+    with SomServer(ex2, max_batch_rows=100, workers=1) as srv2:
         assert len(srv2.submit_bmu(srv2.add_map('a'), _req(3, 150)).result(5)) == 150
     assert ex2.bmu_batches == [[150]]
 
@@ -105,7 +107,7 @@ def test_admission_rejects_what_can_never_fit_and_serves_the_rest():
 
 def test_a_failing_request_fails_alone():
     ex = FakeExecutor(block_first=True)
-    srv = SomServer(ex, max_batch_rows=10)
+    srv = SomServer(ex, max_batch_rows=10, workers=1)
     m = srv.add_map('a')
     f0 = srv.submit_bmu(m, _req(0))
     time.sleep(0.1)
@@ -136,6 +138,64 @@ def test_other_kinds_training_and_stats():
         srv.submit_bmu(m, _req(0))
 
 
+class BarrierExecutor(FakeExecutor):
+    """run_bmu returns only once two calls are in it at the same time (or after 5 s, flagging the timeout)."""
+
+    def __init__(self):
+        super().__init__()
+        self.barrier = threading.Barrier(2, timeout=5)
+        self.timed_out = False
+
+    def run_bmu(self, entry, xs, slot=0, hist=None):
+        try:
+            self.barrier.wait()
+        except threading.BrokenBarrierError:
+            self.timed_out = True
+        return super().run_bmu(entry, xs, slot=slot, hist=hist)
+
+
+def test_two_workers_run_batches_at_the_same_time():
+    ex = BarrierExecutor()
+    with SomServer(ex, max_batch_rows=10, workers=2) as srv:
+        m = srv.add_map('a')
+        f1, f2 = srv.submit_bmu(m, _req(1)), srv.submit_bmu(m, _req(2, 10))
+        assert f1.result(10)[0] == 1 and f2.result(10)[0] == 2
+    assert not ex.timed_out
+
+
+class SlowLargeExecutor(FakeExecutor):
+    """Batches of more than 10 rows wait for `release`; small ones return at once."""
+
+    def run_bmu(self, entry, xs, slot=0, hist=None):
+        if sum(len(x) for x in xs) > 10:
+            self.release.wait(5)
+        self.bmu_batches.append([len(x) for x in xs])
+        return [np.full(len(x), int(np.asarray(x)[0, 0]), dtype=np.int32) for x in xs]
+
+
+def test_small_requests_pass_large_ones_on_the_second_worker():
+    ex = SlowLargeExecutor(block_first=True)
+    with SomServer(ex, max_batch_rows=10, workers=2) as srv:
+        m = srv.add_map('a')
+        big1 = srv.submit_bmu(m, _req(1, 50))
+        time.sleep(0.1)                       # the first worker holds it
+        big2 = srv.submit_bmu(m, _req(2, 50))
+        small = srv.submit_bmu(m, _req(3, 5))
+        assert small.result(2)[0] == 3        # served beside big1, ahead of big2
+        assert not big1.done() and not big2.done()
+        ex.release.set()
+        assert big1.result(5)[0] == 1 and big2.result(5)[0] == 2
+
+
+def test_bmu_requests_with_histograms():
+    ex = FakeExecutor()
+    with SomServer(ex, workers=1) as srv:
+        m = srv.add_map('a')
+        b, h = srv.submit_bmu(m, _req(3), histogram=True).result(5)
+        assert b[0] == 3 and h[3] == 10 and h.sum() == 10
+        assert srv.submit_bmu(m, _req(2)).result(5)[0] == 2
+
+
 class _Som:
     dim, m, n = 2, 2, 2
 
@@ -154,7 +214,7 @@ def test_training_runs_on_its_own_loop_while_assignments_continue():
 
 def test_close_serves_what_is_queued():
     ex = FakeExecutor(block_first=True)
-    srv = SomServer(ex)
+    srv = SomServer(ex, workers=1)
     m = srv.add_map('a')
     futs = [srv.submit_bmu(m, _req(i)) for i in range(4)]
     t = threading.Thread(target=srv.close)
@@ -183,8 +243,13 @@ def test_served_results_match_the_direct_calls(cuda):
         fb = [srv.submit_bmu(mid, p) for p in parts]
         fa = srv.submit_activation(mid, x, rho)
         fe = srv.submit_errors(mid, x)
+        fh = [srv.submit_bmu(mid, p, histogram=True) for p in parts]
         for p, f in zip(parts, fb):
             assert np.array_equal(f.result(120), som.get_winners(p))
+        for p, f in zip(parts, fh):
+            b, h = f.result(120)
+            assert np.array_equal(b, som.get_winners(p))
+            assert np.array_equal(h, som.get_activation_map(p).reshape(-1).astype(np.float64))
         assert np.array_equal(fa.result(120), som.get_activation_map(x, rho))
         np.testing.assert_allclose(fe.result(120), som.compute_errors(x), rtol=1e-12)
         # a training request gives the same map as training directly
