@@ -13,7 +13,8 @@ requests as they arrive, from any thread, and returns futures:
   staging buffers and workspaces, so that a request arriving while another is on the GPU overlaps it on the device;
   the first worker takes requests in arrival order, the others only packable BMU requests (ahead of larger ones), so
   that small requests run beside a large one rather than behind it;
-  training requests run on their own thread and stream, so that a long training does not hold up assignments;
+  training requests run on their own threads and streams (``train_workers``, default 2), so that a long training
+  does not hold up assignments and small trainings overlap;
 * a request whose computation raises fails alone: its future carries the exception and the loop goes on;
 * latency (submit to result on the host) is recorded per kind; ``stats()`` gives count, p50 and p99.
 """
@@ -58,14 +59,14 @@ class GpuExecutor:
     """Runs the requests through libsomgb on a CUDA device (float32 maps). `slot` (0 .. workers - 1) selects the
     calling worker's stream, buffers and per-map workspace and map object, so that workers never share scratch."""
 
-    def __init__(self, device=None, workers=2):
+    def __init__(self, device=None, workers=2, train_workers=2):
         import torch
         from . import _device, _native
         self._torch, self._dev_mod, self._nat = torch, _device, _native
         self.device = device if device is not None else _device.require_cuda()
         self.slots = [_Slot(torch, self.device) for _ in range(max(1, workers))]
         self.stream = self.slots[0].stream
-        self.train_stream = torch.cuda.Stream(device=self.device)
+        self.train_streams = [torch.cuda.Stream(device=self.device) for _ in range(max(1, train_workers))]
 
     def free_bytes(self):
         free, _ = self._torch.cuda.mem_get_info(self.device)
@@ -171,9 +172,11 @@ class GpuExecutor:
         with self._torch.cuda.stream(self.slots[slot].stream):
             return entry['soms'][slot].compute_errors(x, rho)
 
-    def run_train(self, som, dataset, rho, kwargs):
-        with self._torch.cuda.stream(self.train_stream):
+    def run_train(self, som, dataset, rho, kwargs, slot=0):
+        st = self.train_streams[slot]
+        with self._torch.cuda.stream(st):
             som.train(dataset, rho, **kwargs)
+        st.synchronize()
         return som
 
 
@@ -184,11 +187,14 @@ class SomServer:
     hbm_budget: device bytes that admitted requests may hold at once (default: 80 % of the free memory at start).
     max_batch_rows: BMU requests with at most this many rows are packed together, up to this many rows per pass.
     workers: serving threads taking admitted batches (the executor keeps a stream and buffers per worker).
+    train_workers: training threads (each on its own stream), so that small trainings overlap on the device.
     """
 
-    def __init__(self, executor=None, hbm_budget=None, max_batch_rows=1 << 20, workers=2):
+    def __init__(self, executor=None, hbm_budget=None, max_batch_rows=1 << 20, workers=2, train_workers=2):
         self.workers = max(1, int(workers))
-        self._ex = executor if executor is not None else GpuExecutor(workers=self.workers)
+        self.train_workers = max(1, int(train_workers))
+        self._ex = executor if executor is not None else GpuExecutor(workers=self.workers,
+                                                                     train_workers=self.train_workers)
         self.hbm_budget = int(hbm_budget if hbm_budget is not None else 0.8 * self._ex.free_bytes())
         self.max_batch_rows = int(max_batch_rows)
         self._maps = {}
@@ -201,7 +207,8 @@ class SomServer:
         self._batches = []
         self._threads = [threading.Thread(target=self._serve_loop, args=(i,), name=f'somgb-serve-{i}', daemon=True)
                          for i in range(self.workers)]
-        self._threads.append(threading.Thread(target=self._train_loop, name='somgb-train', daemon=True))
+        self._threads += [threading.Thread(target=self._train_loop, args=(i,), name=f'somgb-train-{i}', daemon=True)
+                          for i in range(self.train_workers)]
         for t in self._threads:
             t.start()
 
@@ -370,7 +377,7 @@ class SomServer:
                 continue
             self._finish(batch, fp, results=res)
 
-    def _train_loop(self):
+    def _train_loop(self, slot):
         while True:
             with self._cv:
                 batch, fp = self._admit(self._train_queue)
@@ -379,7 +386,7 @@ class SomServer:
             req = batch[0]
             som, dataset = req.x
             try:
-                res = self._ex.run_train(som, dataset, req.rho, req.kwargs)
+                res = self._ex.run_train(som, dataset, req.rho, req.kwargs, slot=slot)
             except Exception as e:
                 self._finish(batch, fp, exc=e)
                 continue

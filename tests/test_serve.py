@@ -46,7 +46,7 @@ class FakeExecutor:
     def run_errors(self, entry, x, rho, slot=0):
         return (0.5, 0.25)
 
-    def run_train(self, som, dataset, rho, kwargs):
+    def run_train(self, som, dataset, rho, kwargs, slot=0):
         time.sleep(0.05)
         self.trained.append((som, len(dataset), kwargs))
         return som
@@ -252,6 +252,26 @@ def test_served_results_match_the_direct_calls(cuda):
             assert np.array_equal(h, som.get_activation_map(p).reshape(-1).astype(np.float64))
         assert np.array_equal(fa.result(120), som.get_activation_map(x, rho))
         np.testing.assert_allclose(fe.result(120), som.compute_errors(x), rtol=1e-12)
+        # mixed training jobs (grid sizes, topologies, feature counts, catalogue sizes) served together give the maps
+        # of the same trainings run alone
+        jobs = [(8, 8, 4, 'square', 20_000, 6), (16, 16, 8, 'hexagonal', 120_000, 4), (32, 32, 16, 'hexagonal',
+                200_000, 3), (12, 12, 32, 'square', 60_000, 5)]
+        futs, alone = [], []
+        for i, (mm, nn, dd, topo, nrow, ep) in enumerate(jobs):
+            xj = np.ascontiguousarray(synthetic.gaussian_mixture(nrow, dd, 10 + i))
+            for target in (futs, alone):
+                s_ = dg.SOM_Batch(mm, nn, dd, topology=topo)
+                s_.init_rand(seed=i)
+                if target is futs:
+                    target.append(srv.submit_train(s_, xj, n_epochs=ep))
+                else:
+                    s_.train(xj, n_epochs=ep)
+                    target.append(s_)
+        for f, s_ in zip(futs, alone):
+            t_ = f.result(300)
+            # BMUs and fixed-point sums are exact; the float64 flush order may move a weight by a float32 ulp
+            np.testing.assert_allclose(t_.weights, s_.weights, rtol=1e-6, atol=1e-7)
+            np.testing.assert_allclose(t_.quantization_errors, s_.quantization_errors, rtol=1e-9)
         # a training request gives the same map as training directly
         a = dg.SOM_Batch(8, 8, 16, topology='square')
         b = dg.SOM_Batch(8, 8, 16, topology='square')
