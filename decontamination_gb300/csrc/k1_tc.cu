@@ -545,6 +545,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         if (lane == 0 && n_my > 0) {
             ptx::prefetch_tensormap(&tmap);
             const int BST = LARGE ? P.bstages : 0;
+            const int BSTD = BST > 0 ? BST : 1;   // divisor in the ring arithmetic (used only when BST > 0)
             if (BST == 0) {
                 ptx::mbar_arrive_expect_tx(b_full, P.b_bytes);
                 for (uint32_t off = 0; off < P.b_bytes; off += 32768u) {
@@ -575,8 +576,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     while (ok && issued < n_my && issued <= it + 1) ok = issue_x(issued);
                     for (int sweep = 0; ok && sweep < 2; ++sweep) {
                         for (int u = 0; u < U && !*abort_v; ++u, ++kb) {
-                            const int st = (int)(kb % BST);
-                            if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BST - 1) & 1))) {
+                            const int st = (int)(kb % BSTD);
+                            if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BSTD - 1) & 1))) {
                                 fail(4096u);
                                 ok = false;
                                 break;
@@ -597,7 +598,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 for (int64_t k = issued > XSTAGES ? issued - XSTAGES : 0; k < issued; ++k)
                     ptx::mbar_wait(x_full + (int)(k % XSTAGES), (uint32_t)((k / XSTAGES) & 1));
                 for (int64_t k = kb > BST ? kb - BST : 0; BST > 0 && k < kb; ++k)
-                    ptx::mbar_wait(bs_full + (int)(k % BST), (uint32_t)((k / BST) & 1));
+                    ptx::mbar_wait(bs_full + (int)(k % BSTD), (uint32_t)((k / BSTD) & 1));
             }
         }
     } else if (warp == MMA_WARP) {
@@ -776,7 +777,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 // value (fewer candidates for the resolvers). Otherwise groups of 8 (fewer sweep instructions): chunks
                 // 0 and 2 feed (a1, a2), chunks 1 and 3 feed (b1, b2).
                 stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
-                    if (ERR && !LARGE) {
+                    if constexpr (ERR && !LARGE) {
 #pragma unroll
                         for (int g4 = 0; g4 < 32; g4 += 4) {
                             const float g = fminf(fmin3(__uint_as_float(r[g4]), __uint_as_float(r[g4 + 1]),
@@ -790,21 +791,21 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                                 a1 = fminf(a1, g);
                             }
                         }
-                        return;
-                    }
+                    } else {
 #pragma unroll
-                    for (int g8 = 0; g8 < 32; g8 += 8) {
-                        const float g = fmin3(fmin3(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1]),
-                                                    __uint_as_float(r[g8 + 2])),
-                                              fmin3(__uint_as_float(r[g8 + 3]), __uint_as_float(r[g8 + 4]),
-                                                    __uint_as_float(r[g8 + 5])),
-                                              fminf(__uint_as_float(r[g8 + 6]), __uint_as_float(r[g8 + 7])));
-                        if (c & 1) {
-                            if (ERR) b2 = fminf(b2, fmaxf(b1, g));
-                            b1 = fminf(b1, g);
-                        } else {
-                            if (ERR) a2 = fminf(a2, fmaxf(a1, g));
-                            a1 = fminf(a1, g);
+                        for (int g8 = 0; g8 < 32; g8 += 8) {
+                            const float g = fmin3(fmin3(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1]),
+                                                        __uint_as_float(r[g8 + 2])),
+                                                  fmin3(__uint_as_float(r[g8 + 3]), __uint_as_float(r[g8 + 4]),
+                                                        __uint_as_float(r[g8 + 5])),
+                                                  fminf(__uint_as_float(r[g8 + 6]), __uint_as_float(r[g8 + 7])));
+                            if (c & 1) {
+                                if (ERR) b2 = fminf(b2, fmaxf(b1, g));
+                                b1 = fminf(b1, g);
+                            } else {
+                                if (ERR) a2 = fminf(a2, fmaxf(a1, g));
+                                a1 = fminf(a1, g);
+                            }
                         }
                     }
                 });
@@ -893,8 +894,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
             }
             // The row's non-zero candidate-mask words (from the summary bits) are first copied to the resolver's own
-            // buffer, which hands the masks back to the sweeps early; more than KW of them send the row to the exact
-            // recheck.
+            // buffer, which hands the masks back to the sweeps early. A warp with a row of more than KW such words
+            // (early epochs of large maps) keeps the masks until its rows are decided and reads every row's
+            // candidates from them.
             const bool flagged = sFlag[row] != 0;
             int nw = 0;
             // column tiles 0-7, then (for more than 8) 8-15: each part's two halves fit one 64-bit word
@@ -917,8 +919,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     }
                 }
             }
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(m_empty);
+            const bool ovf = live && !flagged && nw > KW;
+            const bool any_ovf = __any_sync(0xffffffffu, ovf);
+            if (!any_ovf) {
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(m_empty);
+            }
             // Then the candidates, one per lane and iteration (the next copied word fetched in the same iteration),
             // each one's float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found.
             // A row with more than CAPR candidates stops there and goes to the exact recheck.
@@ -933,7 +939,34 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     else { f2 = df; j2 = j; }
                 } else { f3 = df; j3 = j; }
             };
-            {
+            if (any_ovf) {
+                // the masks are still this warp's: words from the summary bits, as in the copy above
+                for (int part = 0; part < parts; ++part) {
+                    const uint32_t* ss = sSum + part * HALVES * TM;
+                    uint64_t S = (flagged || !live) ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
+                    uint32_t word = 0u;
+                    int jtop = 0;
+                    bool more = S != 0ull && cnt <= CAPR;
+                    while (__any_sync(0xffffffffu, more)) {
+                        const bool need = word == 0u;
+                        const int b = __ffsll((long long)S) - 1;
+                        const int bb = b < 0 ? 0 : b;
+                        const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
+                        const uint32_t nwd = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
+                        word = need ? (b >= 0 ? nwd : 0u) : word;
+                        jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
+                        S = need ? (S & (S - 1ull)) : S;
+                        const int j = jtop - (__ffs(word) - 1);
+                        const bool take = more && word != 0u && j < (int)a.m;
+                        word &= word - 1u;
+                        if (take) {
+                            ++cnt;
+                            push(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr), j);
+                        }
+                        more = (word != 0u || S != 0ull) && cnt <= CAPR;
+                    }
+                }
+            } else {
                 const int nwc = nw <= KW ? nw : 0;
                 int wi = 0, jtop = 0;
                 uint32_t word = 0u;
@@ -955,8 +988,28 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     more = (word != 0u || wi < nwc) && cnt <= CAPR;
                 }
             }
-            // every candidate of the row again (the rare slower paths)
+            // every candidate of the row again (the rare slower paths): from the copied words, or from the masks
+            // (still held) for a warp with an overflowing row
             auto for_each_cand = [&](auto&& f) {
+                if (any_ovf) {
+                    for (int part = 0; part < parts; ++part) {
+                        const uint32_t* ss = sSum + part * HALVES * TM;
+                        uint64_t S = (uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32);
+                        while (S) {
+                            const int bb = __ffsll((long long)S) - 1;
+                            S &= S - 1ull;
+                            const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
+                            uint32_t word = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
+                            const int jt = ub * TN + hh * 128 + wb * 32 + 31;
+                            while (word) {
+                                const int j = jt - (__ffs(word) - 1);
+                                word &= word - 1u;
+                                if (j < (int)a.m) f(j);
+                            }
+                        }
+                    }
+                    return;
+                }
                 for (int w = 0; w < nw; ++w) {
                     uint32_t word = pw[w * TM];
                     const int jt = pt[w * TM];
@@ -968,7 +1021,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 }
             };
             TC_T(9);
-            if (live && (flagged || nw > KW || cnt == 0 || cnt > CAPR)) {
+            const bool recheck = live && (flagged || cnt == 0 || cnt > CAPR);
+            if (recheck) {
                 const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                 P.rows[slotq] = (int32_t)grow;
             } else if (live) {
@@ -1038,6 +1092,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 }
                 TC_T(10);
                 emit_sample32(a, grow, rho_v, r1, r2, rd1, tr1, tr2, e0, e1, e2);
+            }
+            if (any_ovf) {   // the warp's rows are decided: the masks go back to the sweeps
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(m_empty);
             }
             TC_T(7);
         }
