@@ -22,21 +22,24 @@
 // error sums, the second best) only if s~_j <= m + 2 (alpha |x'|^2 + beta (m + |x'|^2) + gamma) / (1 - beta), m
 // being the best (second-best) s~ of the row.
 //
-// Epilogue, per row tile: sweep 1 streams the TMEM tiles and keeps the best (and second-best) s~ per row with
-// FP32 min/max (full-rate ALU); sweep 2 recomputes the same MMAs (the tensor pipe has slack) and collects every
-// unit under that threshold — the only units that can be the reference's BMU (or second BMU). Each candidate's
-// distance is then evaluated on CUDA cores with float32 differences (the reference's terms) and, when two
-// candidates are within float32 rounding of each other, with the reference's float64 sum. Rows with more than
-// CAPR candidates, non-finite features or overflowing distances go to an exact per-row recheck.
+// Epilogue, per row tile: sweep 1 streams the TMEM tiles and keeps each row's smallest s~ (and, for the error sums,
+// the second-smallest 4- or 8-unit group minimum) with FP32 min/max; sweep 2 recomputes the same MMAs (the tensor pipe
+// has slack) and marks every unit under the threshold in a bit mask — the only units that can be the reference's
+// BMU (or second BMU). Each candidate's distance is then evaluated on CUDA cores with float32 differences (the
+// reference's terms) and ranked; ranks within float32 rounding of each other are decided by compensated float32 sums
+// and, failing that, by the reference's float64 sum. Rows with more than CAPR candidates, non-finite features or
+// overflowing distances go to an exact per-row recheck.
 //
 // Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
-//   warp 13     TMA producer: the unit operand B once (bulk copy), sample tiles (2-D tiled TMA, 2-stage ring);
+//   warp 13     TMA producer: the unit operand B (resident: one bulk copy; LARGE maps: a ring of column tiles),
+//               sample tiles (2-D tiled TMA, 2-stage ring);
 //   warp 12     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
-//   warps 0-7   converters (FP32 tile -> centred split-BF16 A tile) and sweeps; warp e reads TMEM lanes
-//               32(e&3).. and column half e>>2, and writes the candidates of its rows into a double buffer;
-//   warps 8-11  resolvers: thread r of warp 8+q decides row 32q+r of row tile t (distances from the unit rows in
-//               L2, ranking, outputs) while the sweeps already work on row tile t+1, so that the L2 latency of
-//               the candidate rows overlaps the tensor and sweep work.
+//   warps 0-7   converters (FP32 tile -> centred split-FP16 A tile) and sweeps; warp e reads TMEM lanes
+//               32(e&3).. and column half e>>2 and writes its rows' mask words and per-row summary bits;
+//   warps 8-11  resolvers: thread r of warp 8+q decides row 32q+r of row tile t while the sweeps already work on
+//               row tile t+1: it copies the row's non-zero mask words (handing the masks back), computes the
+//               candidates' distances from the unit rows (shared memory when they fit, else L2), ranks them,
+//               decides and writes the outputs.
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
@@ -422,29 +425,6 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     float r;
     asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
-}
-
-// NQ candidates at once (every row's loads issued before any chain): the same chain as cand_dist32v.
-template <int DT, int NQ>
-__device__ __forceinline__ void cand_dist32_multi(const float* __restrict__ w, const int32_t (&jj)[NQ],
-                                                  const float (&xr)[DT], float (&dd)[NQ]) {
-    float4 r[NQ][DT / 4];
-#pragma unroll
-    for (int i = 0; i < NQ; ++i)
-#pragma unroll
-        for (int k4 = 0; k4 < DT / 4; ++k4) r[i][k4] = ((const float4*)(w + (int64_t)jj[i] * DT))[k4];
-#pragma unroll
-    for (int i = 0; i < NQ; ++i) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int k4 = 0; k4 < DT / 4; ++k4) {
-            float t = r[i][k4].x - xr[4 * k4]; acc = fmaf(t, t, acc);
-            t = r[i][k4].y - xr[4 * k4 + 1]; acc = fmaf(t, t, acc);
-            t = r[i][k4].z - xr[4 * k4 + 2]; acc = fmaf(t, t, acc);
-            t = r[i][k4].w - xr[4 * k4 + 3]; acc = fmaf(t, t, acc);
-        }
-        dd[i] = acc;
-    }
 }
 
 // (da, ja) ranks before (db, jb): lexicographic, empty entries (unit < 0) last

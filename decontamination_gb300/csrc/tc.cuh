@@ -1,4 +1,4 @@
-// K1: tensor-core (tcgen05, split-BF16) BMU search.
+// K1: tensor-core (tcgen05, split-FP16) BMU search.
 #pragma once
 
 #include "pass.cuh"
