@@ -42,17 +42,7 @@ class Covariance(object):
             name = 'somgb_weighted_moments_f64' if f64 else 'somgb_weighted_moments'
             _native.call(name, xd.data_ptr(), _device.ptr(rd), _device.rows(xd), dim, out.data_ptr(), _device.stream())
             o = out.cpu().numpy()
-            wc, mc, m2c = float(o[0]), o[1:1 + dim], o[1 + dim:].reshape(dim, dim)
-            if wc <= 0.0:
-                continue
-            if W == 0.0:
-                W, mean, M2 = wc, mc.copy(), m2c.copy()
-                continue
-            delta = mc - mean
-            tot = W + wc
-            M2 = M2 + m2c + np.outer(delta, delta) * (W * wc / tot)
-            mean = mean + delta * (wc / tot)
-            W = tot
+            W, mean, M2 = combine_moments(W, mean, M2, float(o[0]), o[1:1 + dim], o[1 + dim:].reshape(dim, dim))
         return W, mean, M2
 
     @staticmethod
@@ -81,6 +71,18 @@ class Covariance(object):
     def project_pca(dataset: np.ndarray, eigenvectors: np.ndarray) -> np.ndarray:
         """The dataset in the PCA basis, dataset . eigenvectors (algo/covariance.py:243-258)."""
         return np.dot(dataset, eigenvectors)
+
+
+def combine_moments(W, mean, M2, wc, mc, m2c):
+    """Moments (weight sum, mean, centred second moments) of two sample sets from each set's (Chan et al.'s pairwise
+    update): M2 = M2_a + M2_b + d d^T W_a W_b / (W_a + W_b), d = mean_b - mean_a."""
+    if wc <= 0.0:
+        return W, mean, M2
+    if W == 0.0:
+        return wc, np.array(mc, dtype=np.float64), np.array(m2c, dtype=np.float64)
+    delta = mc - mean
+    tot = W + wc
+    return tot, mean + delta * (wc / tot), M2 + m2c + np.outer(delta, delta) * (W * wc / tot)
 
 
 def _len(a):

@@ -24,6 +24,29 @@ def test_pca_grid_weights_from_the_reference_covariance():
         np.testing.assert_allclose(ev.astype(np.float32), g[f'{tag}_eigenvalues'], rtol=1e-6)
 
 
+def test_chunk_moments_combine_to_the_whole():
+    """The host-side pairwise update of chunk moments gives the moments of the whole weighted catalogue."""
+    from decontamination_gb300.covariance import combine_moments
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((5000, 5)) * [1.0, 3.0, 0.5, 2.0, 1.0] + 7.0
+    w = rng.random(5000)
+
+    def moments(xs, ws):
+        W = ws.sum()
+        mu = (ws[:, None] * xs).sum(0) / W
+        c = xs - mu
+        return W, mu, (ws[:, None] * c).T @ c
+
+    W, mu, M2 = 0.0, np.zeros(5), np.zeros((5, 5))
+    for a in range(0, 5000, 1300):
+        W, mu, M2 = combine_moments(W, mu, M2, *moments(x[a:a + 1300], w[a:a + 1300]))
+    W0, mu0, M20 = moments(x, w)
+    assert W == pytest.approx(W0, rel=1e-14)
+    np.testing.assert_allclose(mu, mu0, rtol=1e-13)
+    np.testing.assert_allclose(M2, M20, rtol=1e-12)
+    assert combine_moments(W, mu, M2, 0.0, mu * 0, M2 * 0)[0] == W   # an empty chunk changes nothing
+
+
 def test_grid_points_follow_the_reference():
     from decontamination_gb300.hyparam_finder_som import HypParamFinder_SOM
     g = golden('hyparam_search')
