@@ -363,6 +363,14 @@ def gpu_arm(args, ws, rank, local):
                 'peak_source': f'{peak_kind} bf16_tflops_sustained (dense FP16 and BF16 share the rate)',
                 'hbm_bytes_algorithmic': N * D * 4 + N * 4,
                 'hbm_frac': (N * D * 4 + N * 4) / (k_ms * 1e-3) / 1e9 / peaks.get('hbm_gbs', 6800.0)}
+    if used_algo == 'tc':
+        # what the tensor pipe actually executes: two sweeps (the second recomputes the MMAs) of the split-FP16
+        # contraction over the padded map, K = 16 x K-steps (lo.hi, hi.lo, hi.hi blocks and the |w|^2 step)
+        k_steps = 3 * (D // 16) + 1 if D % 16 == 0 else (3 * D + 2 + 15) // 16
+        m_pad = (M + 255) // 256 * 256
+        executed = 2 * 2.0 * N * m_pad * (16 * k_steps) / (k_ms * 1e-3) / 1e12
+        roofline['executed_tensor_tflops'] = executed
+        roofline['executed_frac'] = executed / peak
     out = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
