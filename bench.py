@@ -243,6 +243,8 @@ class EpochRunner:
         self.wsp = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
         self.wsb = nbytes
         self.penalty = 2.0 if w['topology'] == 'square' else 1.0
+        nb = int(native.lib().somgb_neighbourhood_grid_workspace_bytes(w['m'], w['n'], self.D))
+        self.upd_ws = torch.empty(nb, dtype=torch.uint8, device=device)
         self.epoch = 0
 
     def step(self, err_slot, timer=None, phases=None):
@@ -267,8 +269,9 @@ class EpochRunner:
             phases[2].record()
         e = self.epoch % self.w['schedule']
         sigma = float(np.float32(self.w['sigma0'])) / (1.0 + 2.0 * e / self.w['schedule'])
-        nat.call('somgb_neighbourhood_update', self.S.data_ptr(), self.c.data_ptr(), self.topo.data_ptr(), self.M,
-                 self.D, max(sigma, 1e-12), self.wnext.data_ptr(), None, None, s)
+        nat.call('somgb_neighbourhood_update_grid', self.S.data_ptr(), self.c.data_ptr(), self.topo.data_ptr(),
+                 self.w['m'], self.w['n'], self.D, max(sigma, 1e-12), self.wnext.data_ptr(), None, None,
+                 self.upd_ws.data_ptr(), self.upd_ws.numel(), s)
         if phases is not None:
             phases[3].record()
         self.wcur, self.wnext = self.wnext, self.wcur

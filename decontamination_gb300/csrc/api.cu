@@ -13,6 +13,11 @@ template <typename T>
 int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
                       const float* bounds, double* S, double* c, cudaStream_t stream);
 int launch_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, cudaStream_t stream);
+template <typename T>
+int launch_neighbourhood_grid(const double* S, const double* c, const T* topo, int64_t rows, int64_t cols, int d,
+                              double sigma, T* w_out, double* num, double* den, void* ws, size_t ws_bytes,
+                              cudaStream_t stream);
+size_t grid_neighbourhood_workspace(int64_t rows, int64_t cols, int d);
 int launch_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_w, double* hist_c,
                           cudaStream_t stream);
 template <typename T>
@@ -322,6 +327,30 @@ int somgb_neighbourhood_update(const double* S, const double* c, const float* to
     if (!S || !c || !topo || !w_out) return set_error(SOMGB_ERR_INVALID, "NULL argument");
     if (!(sigma > 0.0)) return set_error(SOMGB_ERR_INVALID, "sigma must be > 0");
     return launch_neighbourhood<float>(S, c, topo, m, d, sigma, w_out, num, den, (cudaStream_t)stream);
+}
+
+size_t somgb_neighbourhood_grid_workspace_bytes(int64_t rows, int64_t cols, int d) {
+    return rows > 0 && cols > 0 && d > 0 ? grid_neighbourhood_workspace(rows, cols, d) : 0;
+}
+
+int somgb_neighbourhood_update_grid(const double* S, const double* c, const float* topo, int64_t rows, int64_t cols,
+                                    int d, double sigma, float* w_out, double* num, double* den, void* ws,
+                                    size_t ws_bytes, somgb_stream_t stream) {
+    if (rows <= 0 || cols <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if (!S || !c || !topo || !w_out) return set_error(SOMGB_ERR_INVALID, "NULL argument");
+    if (!(sigma > 0.0)) return set_error(SOMGB_ERR_INVALID, "sigma must be > 0");
+    return launch_neighbourhood_grid<float>(S, c, topo, rows, cols, d, sigma, w_out, num, den, ws, ws_bytes,
+                                            (cudaStream_t)stream);
+}
+
+int somgb_neighbourhood_update_grid_f64(const double* S, const double* c, const double* topo, int64_t rows,
+                                        int64_t cols, int d, double sigma, double* w_out, double* num, double* den,
+                                        void* ws, size_t ws_bytes, somgb_stream_t stream) {
+    if (rows <= 0 || cols <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if (!S || !c || !topo || !w_out) return set_error(SOMGB_ERR_INVALID, "NULL argument");
+    if (!(sigma > 0.0)) return set_error(SOMGB_ERR_INVALID, "sigma must be > 0");
+    return launch_neighbourhood_grid<double>(S, c, topo, rows, cols, d, sigma, w_out, num, den, ws, ws_bytes,
+                                             (cudaStream_t)stream);
 }
 
 int somgb_train_iter_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,

@@ -695,6 +695,109 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
     return SOMGB_OK;
 }
 
+// ---------------------------------------------------------------------------------------------------------------------
+// Neighbourhood contraction on a grid topography, by separation. On the reference's square and hexagonal grids the
+// x coordinate of unit (i, j) (unit i*cols + j) depends only on (i, j mod 2) and the y coordinate only on j, so
+//   h = exp(-(dx^2 + dy^2) / (2 sigma^2)) = exp(-dx^2 / (2 sigma^2)) * exp(-dy^2 / (2 sigma^2))
+// (dx^2, dy^2 the float32 squares of the float32 differences, as the reference types them) and num = H S becomes two
+// one-dimensional contractions: T[i, j', p] = sum_i' Ex[(i, p), (i', j' mod 2)] S[i', j'] for the two parities p of
+// the output column, then num[i, j] = sum_j' Ey[j, j'] T[i, j', j mod 2]: rows*cols*(rows + cols) terms instead of
+// (rows*cols)^2, and (2 rows)^2 + cols^2 exponentials. Same float64 arithmetic per term; h differs from the exponential
+// of the sum by a few float64 ulps.
+// ---------------------------------------------------------------------------------------------------------------------
+
+template <typename T>
+__global__ void grid_tables_kernel(const T* __restrict__ topo, int64_t rows, int64_t cols, double inv2s2,
+                                   double* __restrict__ ex, double* __restrict__ ey) {
+    const int64_t nx = 2 * rows, total = nx * nx + cols * cols;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        if (q < nx * nx) {
+            const int64_t a = q / nx, b = q % nx;   // (i, p) and (i', p')
+            const int64_t ua = (a >> 1) * cols + ((a & 1) < cols ? (a & 1) : 0);
+            const int64_t ub = (b >> 1) * cols + ((b & 1) < cols ? (b & 1) : 0);
+            const T dx = topo[2 * ua] - topo[2 * ub];
+            ex[q] = exp(-(double)(dx * dx) * inv2s2);
+        } else {
+            const int64_t r = q - nx * nx, j = r / cols, jp = r % cols;
+            const T dy = topo[2 * j + 1] - topo[2 * jp + 1];
+            ey[r] = exp(-(double)(dy * dy) * inv2s2);
+        }
+    }
+}
+
+// tmp[((i * cols + j') * 2 + p) * (d + 1) + k] = sum_i' ex[(2i + p) * 2 rows + 2i' + j' mod 2] * S_k[i' * cols + j']
+// (feature k = d: the count c)
+__global__ void grid_step1_kernel(const double* __restrict__ S, const double* __restrict__ c, int64_t rows,
+                                  int64_t cols, int d, const double* __restrict__ ex, double* __restrict__ tmp) {
+    const int64_t total = rows * cols * 2 * (d + 1);
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % (d + 1));
+        const int64_t r = q / (d + 1);
+        const int p = (int)(r & 1);
+        const int64_t jp = (r >> 1) % cols, i = (r >> 1) / cols;
+        const double* erow = ex + (2 * i + p) * (2 * rows) + (jp & 1);
+        double acc = 0.0;
+        for (int64_t ip = 0; ip < rows; ++ip) {
+            const int64_t u = ip * cols + jp;
+            acc = fma(erow[2 * ip], k < d ? S[u * d + k] : c[u], acc);
+        }
+        tmp[q] = acc;
+    }
+}
+
+// num[i * cols + j][k] = sum_j' ey[j * cols + j'] * tmp[i, j', j mod 2][k]; w_out = num / den where den > 1e-12
+template <typename T>
+__global__ void grid_step2_kernel(const double* __restrict__ tmp, int64_t rows, int64_t cols, int d,
+                                  const double* __restrict__ ey, T* __restrict__ w_out, double* __restrict__ num_out,
+                                  double* __restrict__ den_out) {
+    const int64_t total = rows * cols * d;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % d);
+        const int64_t u = q / d, j = u % cols, i = u / cols;
+        const double* eyr = ey + j * cols;
+        const double* trow = tmp + (i * cols * 2 + (j & 1)) * (d + 1);
+        double num = 0.0, den = 0.0;
+        for (int64_t jp = 0; jp < cols; ++jp) {
+            const double* t = trow + jp * 2 * (d + 1);
+            num = fma(eyr[jp], t[k], num);
+            den = fma(eyr[jp], t[d], den);
+        }
+        if (num_out) num_out[u * d + k] = num;
+        if (den_out && k == 0) den_out[u] = den;
+        w_out[u * d + k] = den > FLOAT_EPS ? (T)(num / den) : (T)0;
+    }
+}
+
+size_t grid_neighbourhood_workspace(int64_t rows, int64_t cols, int d) {
+    return (size_t)(4 * rows * rows + cols * cols + rows * cols * 2 * (d + 1)) * sizeof(double);
+}
+
+template <typename T>
+int launch_neighbourhood_grid(const double* S, const double* c, const T* topo, int64_t rows, int64_t cols, int d,
+                              double sigma, T* w_out, double* num, double* den, void* ws, size_t ws_bytes,
+                              cudaStream_t stream) {
+    if (rows <= 0 || cols <= 0 || d <= 0) return SOMGB_OK;
+    if (!ws || ws_bytes < grid_neighbourhood_workspace(rows, cols, d))
+        return set_error(SOMGB_ERR_WORKSPACE, "grid neighbourhood workspace too small");
+    const double inv2s2 = 1.0 / (2.0 * sigma * sigma);
+    double* ex = (double*)ws;
+    double* ey = ex + 4 * rows * rows;
+    double* tmp = ey + cols * cols;
+    const int64_t nt = 4 * rows * rows + cols * cols;
+    grid_tables_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(nt, 256), 4 * (int64_t)num_sms()), 256, 0, stream>>>(
+        topo, rows, cols, inv2s2, ex, ey);
+    SOMGB_LAUNCH_CHECK();
+    const int64_t n1 = rows * cols * 2 * (d + 1);
+    grid_step1_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n1, 256), 8 * (int64_t)num_sms()), 256, 0, stream>>>(
+        S, c, rows, cols, d, ex, tmp);
+    SOMGB_LAUNCH_CHECK();
+    const int64_t n2 = rows * cols * d;
+    grid_step2_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n2, 256), 8 * (int64_t)num_sms()), 256, 0, stream>>>(
+        tmp, rows, cols, d, ey, w_out, num, den);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
 template <typename T>
 int launch_neighbourhood(const double* S, const double* c, const T* topo, int64_t m, int d, double sigma, T* w_out,
                          double* num, double* den, cudaStream_t stream) {
@@ -754,6 +857,10 @@ template int launch_iter<float>(const float*, const double*, const int32_t*, int
                                 double, int64_t, int64_t, double*, double*, cudaStream_t);
 template int launch_iter<double>(const double*, const double*, const int32_t*, int64_t, int, const double*, int64_t,
                                  double, int64_t, int64_t, double*, double*, cudaStream_t);
+template int launch_neighbourhood_grid<float>(const double*, const double*, const float*, int64_t, int64_t, int, double,
+                                              float*, double*, double*, void*, size_t, cudaStream_t);
+template int launch_neighbourhood_grid<double>(const double*, const double*, const double*, int64_t, int64_t, int,
+                                               double, double*, double*, double*, void*, size_t, cudaStream_t);
 template int launch_divide<float>(const double*, const double*, int64_t, int, float*, cudaStream_t);
 template int launch_divide<double>(const double*, const double*, int64_t, int, double*, cudaStream_t);
 

@@ -150,10 +150,15 @@ class SOM_Batch(SOM_Abstract):
                      n, D, M, bounds.data_ptr(), S.data_ptr(), c.data_ptr(), _device.stream())
 
     def _update(self, S, c, topo, sigma, w_out):
-        M, D = self._m * self._n, self._dim
-        name = 'somgb_neighbourhood_update_f64' if self._is_f64 else 'somgb_neighbourhood_update'
-        _native.call(name, S.data_ptr(), c.data_ptr(), topo.data_ptr(), M, D, sigma, w_out.data_ptr(), None, None,
-                     _device.stream())
+        """num = H S, den = H c, w = num / den, with the map's grid topography factorised by axis."""
+        D = self._dim
+        nbytes = int(_native.lib().somgb_neighbourhood_grid_workspace_bytes(self._m, self._n, D))
+        if getattr(self, '_upd_ws', None) is None:
+            self._upd_ws = _device.Workspace()
+        wsp, wsb = self._upd_ws.get(nbytes, w_out.device)
+        name = 'somgb_neighbourhood_update_grid_f64' if self._is_f64 else 'somgb_neighbourhood_update_grid'
+        _native.call(name, S.data_ptr(), c.data_ptr(), topo.data_ptr(), self._m, self._n, D, sigma,
+                     w_out.data_ptr(), None, None, wsp, wsb, _device.stream())
 
     @staticmethod
     def _errors_of(err_host):

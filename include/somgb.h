@@ -177,6 +177,21 @@ int somgb_neighbourhood_update_f64(const double* S, const double* c, const doubl
                                    double sigma, double* w_out, double* num, double* den, somgb_stream_t stream);
 
 /*
+ * The same update on a grid topography (unit i*cols + j; x coordinate a function of (i, j mod 2) only and y a function
+ * of j only, as on the reference's square and hexagonal grids, algo/som_abstract.py:81-111): the Gaussian factorises
+ * into x and y parts and the contraction runs as two one-dimensional ones, rows*cols*(rows + cols) terms instead of
+ * (rows*cols)^2. Results equal somgb_neighbourhood_update's to a few float64 ulps. ws: device scratch of
+ * somgb_neighbourhood_grid_workspace_bytes(rows, cols, d) bytes (8-byte aligned).
+ */
+size_t somgb_neighbourhood_grid_workspace_bytes(int64_t rows, int64_t cols, int d);
+int somgb_neighbourhood_update_grid(const double* S, const double* c, const float* topo, int64_t rows, int64_t cols,
+                                    int d, double sigma, float* w_out, double* num, double* den, void* ws,
+                                    size_t ws_bytes, somgb_stream_t stream);
+int somgb_neighbourhood_update_grid_f64(const double* S, const double* c, const double* topo, int64_t rows,
+                                        int64_t cols, int d, double sigma, double* w_out, double* num, double* den,
+                                        void* ws, size_t ws_bytes, somgb_stream_t stream);
+
+/*
  * Iteration ("n_vectors") mode over a chunk: sample i of the chunk has sigma_i = sigma0 * 1/(1+2(cur+i)/n_vectors)
  * (clamped >= 1e-12) and adds rho_i * h_j(i) * x_i to num[j] and rho_i * h_j(i) to den[j] for every unit j
  * (float64 "+="). Replaces _train_step1_iter_kernel (algo/som_batch.py:154-210). sigma0 is the map dtype's value.

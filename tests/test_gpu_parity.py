@@ -357,6 +357,42 @@ def test_host_catalogue_in_pieces(cuda, D, weighted, dtype):
     np.testing.assert_allclose(a.compute_errors(xh, rho), a.compute_errors(xd, rd), rtol=ERR_RTOL)
 
 
+@pytest.mark.parametrize('m,n,topology,dtype', [(32, 32, 'hexagonal', np.float32), (64, 64, 'square', np.float32),
+                                                 (7, 1, 'hexagonal', np.float32), (5, 9, 'hexagonal', np.float64),
+                                                 (12, 10, 'square', np.float64)])
+def test_grid_neighbourhood_update_matches_the_pairwise_one(cuda, native, m, n, topology, dtype):
+    """The axis-factorised contraction gives the pairwise num = H S, den = H c to a few float64 ulps, and the
+    same weights."""
+    rng = np.random.default_rng(m * 100 + n)
+    M, D = m * n, 6
+    som = dg.SOM_Batch(m, n, D, dtype=dtype, topology=topology)
+    topo = torch.from_numpy(som._topography).to(cuda)
+    c = np.where(rng.random(M) < 0.3, 0.0, rng.integers(1, 500, M)).astype(np.float64)
+    S = rng.standard_normal((M, D)) * c[:, None]
+    Sd, cd = torch.from_numpy(S).to(cuda), torch.from_numpy(c).to(cuda)
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    sfx = '_f64' if dtype == np.float64 else ''
+    s = torch.cuda.current_stream().cuda_stream
+    for sigma in (0.7, 3.0, 40.0):
+        w1, w2 = (torch.empty((M, D), dtype=tdt, device=cuda) for _ in range(2))
+        n1, n2 = (torch.empty((M, D), dtype=torch.float64, device=cuda) for _ in range(2))
+        d1, d2 = (torch.empty(M, dtype=torch.float64, device=cuda) for _ in range(2))
+        native.call('somgb_neighbourhood_update' + sfx, Sd.data_ptr(), cd.data_ptr(), topo.data_ptr(), M, D, sigma,
+                    w1.data_ptr(), n1.data_ptr(), d1.data_ptr(), s)
+        nb = int(native.lib().somgb_neighbourhood_grid_workspace_bytes(m, n, D))
+        ws = torch.empty(nb, dtype=torch.uint8, device=cuda)
+        native.call('somgb_neighbourhood_update_grid' + sfx, Sd.data_ptr(), cd.data_ptr(), topo.data_ptr(), m, n, D,
+                    sigma, w2.data_ptr(), n2.data_ptr(), d2.data_ptr(), ws.data_ptr(), nb, s)
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(n2.cpu().numpy(), n1.cpu().numpy(), rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(d2.cpu().numpy(), d1.cpu().numpy(), rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(w2.cpu().numpy(), w1.cpu().numpy(), rtol=1e-6 if dtype == np.float32 else 1e-12,
+                                   atol=1e-7)
+    with pytest.raises(native.SomgbError):
+        native.call('somgb_neighbourhood_update_grid' + sfx, Sd.data_ptr(), cd.data_ptr(), topo.data_ptr(), m, n, D,
+                    1.0, w2.data_ptr(), None, None, ws.data_ptr(), nb - 8, s)
+
+
 def test_edge_cases_tc_padded(cuda, native):
     """The golden edge cases through the tensor-core pass: two zero features pad D=6 to 8 without changing any
     distance, so every output must equal the reference's."""
