@@ -395,6 +395,38 @@ def gpu_arm(args, ws, rank, local):
         out['fp32_form'] = {'value': N * M / (t32 / n32 * 1e-3) / 1e9, 'ms_per_step': t32 / n32,
                             'bmu_kernel_ms': statistics.mean(k32), 'phases': ph32}
         out['speedup_vs_fp32_form'] = out['fp32_form']['ms_per_step'] / ms_per_step
+        # matched BMUs: both forms on the tensor-core run's final map, every row of the catalogue
+        b_tc = torch.empty(N, dtype=torch.int32, device=device)
+        b_32 = torch.empty(N, dtype=torch.int32, device=device)
+        for algo_name, dst in (('tc', b_tc), ('fp32', b_32)):
+            nb = _native.workspace_bytes(_native.OP_FIND_BMUS, N, M, D, _native.ALGOS[algo_name])
+            wsb = torch.empty(nb + 256, dtype=torch.uint8, device=device)
+            _native.call('somgb_find_bmus', xd.data_ptr(), N, D, runner.wcur.data_ptr(), M, _native.ALGOS[algo_name],
+                         dst.data_ptr(), wsb.data_ptr() + (-wsb.data_ptr()) % 256, nb,
+                         torch.cuda.current_stream().cuda_stream)
+            del wsb
+        out['fp32_form']['bmu_mismatches'] = int((b_tc != b_32).sum().item())
+        out['fp32_form']['bmu_rows_compared'] = N
+        del b_tc, b_32
+
+    # --- trained weights against the same training on a float64 map (this library's float64 path): the difference
+    #     includes the two typings' different BMUs at near-ties, so it bounds, not measures, the float32 path's error ---
+    if not args.skip_fp32:
+        sub = min(N, 200_000)
+        e_w = 3
+        errs64 = {}
+        maps = {}
+        for dt_ in (np.float32, np.float64):
+            som_ = dg.SOM_Batch(w['m'], w['n'], D, dtype=dt_, topology=w['topology'], sigma=w['sigma0'])
+            som_.bmu_algo = args.algo
+            som_._weights[...] = w0.astype(dt_)
+            som_.train(x[:sub].astype(dt_), n_epochs=e_w, use_best_epoch=False)
+            maps[dt_] = som_.weights.reshape(-1, D).astype(np.float64)
+        rel = np.abs(maps[np.float32] - maps[np.float64]) / np.maximum(np.abs(maps[np.float64]), 1e-6)
+        out['weights_vs_fp64'] = {'max_rel': float(rel.max()), 'rms_rel': float(np.sqrt(np.mean(rel ** 2))),
+                                  'rows': sub, 'epochs': e_w,
+                                  'against': 'the same training on a float64 map (float64 distances, so BMUs at '
+                                             'near-ties can differ from the float32 typing)'}
 
     # --- end to end through the public API ------------------------------------------------------------------------------
     if not args.skip_e2e:
