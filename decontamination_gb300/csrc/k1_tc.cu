@@ -56,9 +56,10 @@ __device__ unsigned int g_tc_status;
 
 // Optional per-phase cycle counters of the epilogue warps (compiled in only with -DSOMGB_TC_PHASE_TIMING; read with
 // cudaMemcpyFromSymbol). Sweep warps: 0 wait for TMEM (sweep 1), 1 sweep 1, 2 wait (sweep 2), 3 sweep 2, 4 convert,
-// 5 half exchange and candidate-buffer wait; resolver warps: 6 wait for candidates, 7 resolution and outputs.
+// 5 half exchange and candidate-buffer wait; resolver warps: 6 wait for candidates, 7 emit, 8 recheck listing,
+// 9 candidate loop, 10 decision; the MMA thread: 12 wait for a free TMEM accumulator, 13 wait for a unit-operand tile.
 #ifdef SOMGB_TC_PHASE_TIMING
-constexpr int TC_PHASES = 12;
+constexpr int TC_PHASES = 14;
 __device__ unsigned long long g_tc_phase_cycles[TC_PHASES];
 #define TC_T0() _tc_t0 = clock64()
 #define TC_T(ph)                                    \
@@ -86,6 +87,8 @@ constexpr int KW = 8;             // non-zero candidate-mask words a resolver co
 constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
 constexpr int MAX_U = 16;         // column tiles per row tile (candidate summaries: 32-bit words of 8 tiles per half)
 constexpr int NBARS = 40;         // mbarrier slots
+constexpr int BMAX = 4;           // deepest ring of streamed unit-operand tiles (slots 28 .. 28 + 2 BMAX - 1)
+static_assert(28 + 2 * BMAX <= NBARS, "mbarrier slots");
 constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
 constexpr int RES_WARPS = 4;
@@ -166,10 +169,11 @@ TcShape tc_shape(int64_t m, int d) {
     s.b_tile = (size_t)TN * s.kpad * 2;
     s.a_bytes = (size_t)TM * s.kpad * 2;
     s.x_bytes = align_up((size_t)TM * d * 4, 128);
-    // the whole unit operand when it fits, else a ring of 3 (or 2) column tiles streamed from L2 by the TMA warp
+    // the whole unit operand when it fits, else a ring of BMAX (down to 2) column tiles streamed from L2 by the TMA
+    // warp
     size_t off = tc_layout(s, s.b_bytes);
     if (off + 128 > SMEM_LIMIT) {
-        for (int st = 3; st >= 2; --st) {
+        for (int st = BMAX; st >= 2; --st) {
             s.bstages = st;
             off = tc_layout(s, (size_t)st * align_up(s.b_tile, 1024));
             if (off + 128 <= SMEM_LIMIT) break;
@@ -460,8 +464,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint64_t* m_empty = bars + 16;  // the resolvers have read them
     uint64_t* drain = bars + 19;
     uint64_t* p_full = bars + 20;   // [2][4]: both halves of a lane quarter have published (m1, m2)
-    uint64_t* bs_full = bars + 28;  // [3]: a column tile of the unit operand has landed (streamed operand)
-    uint64_t* bs_empty = bars + 31; // [3]: the MMAs reading it have completed
+    uint64_t* bs_full = bars + 28;  // [BMAX]: a column tile of the unit operand has landed (streamed operand)
+    uint64_t* bs_empty = bars + 28 + BMAX; // [BMAX]: the MMAs reading it have completed
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_s;
 
@@ -475,7 +479,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
     if (tid == 0) {
         ptx::mbar_init(b_full, 1);
-        for (int s = 0; s < 3; ++s) {
+        for (int s = 0; s < BMAX; ++s) {
             ptx::mbar_init(bs_full + s, 1);
             ptx::mbar_init(bs_empty + s, 1);
         }
@@ -600,16 +604,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 for (int sweep = 0; ok && sweep < 2; ++sweep) {
                     for (int u = 0; u < U; ++u, ++g) {
                         const int buf = (int)(g & 1);
+                        TC_T0();
                         if (g >= 2 && !ptx::mbar_wait(t_empty + buf, (uint32_t)(((g >> 1) - 1) & 1))) {
                             fail(8u);
                             ok = false;
                             break;
                         }
+                        TC_T(12);
                         if (LARGE && BST > 0 && !ptx::mbar_wait(bs_full + bst, bpar)) {
                             fail(8192u);
                             ok = false;
                             break;
                         }
+                        TC_T(13);
                         ptx::tc_fence_after();
                         const uint32_t dt = tbase + (uint32_t)(buf * TN);
                         const uint32_t bu = (LARGE && BST > 0) ? b_addr + (uint32_t)bst * b_stride
@@ -1094,7 +1101,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         }
     }
 #ifdef SOMGB_TC_PHASE_TIMING
-    if (lane == 0 && warp < SWEEP_WARPS + RES_WARPS)
+    if (lane == 0 && warp <= MMA_WARP)
         for (int ph = 0; ph < TC_PHASES; ++ph) atomicAdd(&g_tc_phase_cycles[ph], _tc_acc[ph]);
 #endif
 
