@@ -414,10 +414,13 @@ TC_STRESS = [
     ('far-offset', 4, 20, 20, 100_000),
     ('uniform', 32, 8, 16, 60_000),
     ('duplicates', 8, 10, 10, 50_000),
-    # maps whose unit operand streams through shared memory (64x64 at D = 16 and 32), more than 8 column tiles with
-    # a resident operand (64x64 at D = 4), and 9 column tiles (48x48)
+    # maps whose unit operand streams through shared memory (64x64 at D = 8 and 16: rings of 4 column tiles; D = 32:
+    # 2 tiles; 32x64 at D = 16: 8 streamed tiles), more than 8 column tiles with a resident operand (64x64 at D = 4),
+    # and 9 column tiles (48x48)
     ('large-streamed', 16, 64, 64, 30_000),
     ('large-streamed', 32, 64, 64, 20_000),
+    ('large-streamed', 8, 64, 64, 30_000),
+    ('large-streamed', 16, 32, 64, 30_000),
     ('large-streamed', 4, 64, 64, 30_000),
     ('large-streamed', 16, 48, 48, 30_000),
 ]
