@@ -152,6 +152,23 @@ def dist_env():
     return ws, rank, local
 
 
+def slowest_rank(t, ws, device=None):
+    """The time `t` maximised over the ranks of the process group (`t` itself for one rank): the job's time is its
+    slowest replica's."""
+    if ws == 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(ws, n, m, ms_per_step):
+    """Gsample·unit/s of the whole job: every one of the ws ranks processes n samples against m units per step."""
+    return ws * n * m / (ms_per_step * 1e-3) / 1e9
+
+
 def make_data(N, w):
     from decontamination_gb300 import synthetic
     x = synthetic.correlated_lognormal(N, w['d'], w['seed'])
@@ -342,13 +359,8 @@ def gpu_arm(args, ws, rank, local):
         total_ms, kernel_ms, launches, errs, phases = time_epochs(torch, runner, args.warmup, args.steps)
     barrier()
     clocks = clk.summary()
-    t_max = total_ms
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    ms_per_step = t_max / args.steps
-    value = ws * N * M / (ms_per_step * 1e-3) / 1e9
+    ms_per_step = slowest_rank(total_ms, ws, device) / args.steps
+    value = whole_job_rate(ws, N, M, ms_per_step)
     rechecks = np.zeros(1, dtype=np.int64)
     _native.call('somgb_last_recheck_count', rechecks.ctypes.data, torch.cuda.current_stream().cuda_stream)
 
@@ -441,10 +453,10 @@ def gpu_arm(args, ws, rank, local):
             som._weights[...] = w0
             som.train(xh, n_epochs=1, use_best_epoch=False)
         barrier()
-        dt = (time.perf_counter() - t0) / e2e_steps
+        dt = slowest_rank((time.perf_counter() - t0) / e2e_steps, ws, device)
         h2d = x.nbytes + w0.nbytes + topo_np.nbytes
         d2h = 2 * w0.nbytes + 3 * 8 * 2
-        out['e2e'] = {'value': ws * N * M / dt / 1e9, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+        out['e2e'] = {'value': whole_job_rate(ws, N, M, dt * 1e3), 'unit': UNIT, 'h2d_bytes_per_step': h2d,
                       'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3,
                       'call': 'SOM_Batch.train(pinned host tensor, n_epochs=1): upload, training pass, error pass, '
                               'weights/history/errors back to the host'}
