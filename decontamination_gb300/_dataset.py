@@ -45,6 +45,13 @@ def _host_tensor(a, np_dtype):
     return t.contiguous()
 
 
+def piece_edges(n):
+    """Row edges [0, e1, ..., n] of the pieces of an n-row host chunk (n >= 2 * PIECE_ROWS): between 2 and
+    MAX_PIECES pieces of about equal size, interior edges rounded up to multiples of 16 rows."""
+    k = max(2, min(MAX_PIECES, n // PIECE_ROWS))
+    return [min(n, (n * p // k + 15) // 16 * 16) for p in range(k)] + [n]
+
+
 def device_pieces(x, rho, dtype, device, weight_dtype=np.float64):
     """(x_dev, rho_dev, pieces): one chunk as device tensors, and an iterable of row ranges (a, b) that yields each
     range once its rows are on the device for the current stream (rho_dev is None without weights).
@@ -69,8 +76,8 @@ def device_pieces(x, rho, dtype, device, weight_dtype=np.float64):
     xd.record_stream(cs)
     if rd is not None:
         rd.record_stream(cs)
-    k = max(2, min(MAX_PIECES, n // PIECE_ROWS))
-    edges = [min(n, (n * p // k + 15) // 16 * 16) for p in range(k)] + [n]
+    edges = piece_edges(n)
+    k = len(edges) - 1
 
     def gen():
         events = []

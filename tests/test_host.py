@@ -78,3 +78,19 @@ def test_hdf5_round_trip(tmp_path):
     other.load(path)
     assert other.m == 3 and other.n == 4 and other.sigma == 1.5 and other.topology == 'square'
     assert np.array_equal(other.weights, som.weights)
+
+
+@pytest.mark.parametrize('n', [2 * _dataset.PIECE_ROWS, 2 * _dataset.PIECE_ROWS + 7, 3 * _dataset.PIECE_ROWS - 1,
+                               12_582_912, 12_582_912 + 13, 50_331_648, 7 * _dataset.PIECE_ROWS + 1])
+def test_piece_edges_cover_the_chunk(n):
+    """Host chunks are copied in 2 .. MAX_PIECES pieces whose interior edges are multiples of 16 rows (16-byte aligned
+    rows for any D), covering every row once."""
+    e = _dataset.piece_edges(n)
+    k = len(e) - 1
+    assert 2 <= k <= _dataset.MAX_PIECES
+    assert k == max(2, min(_dataset.MAX_PIECES, n // _dataset.PIECE_ROWS))
+    assert e[0] == 0 and e[-1] == n
+    assert all(a <= b for a, b in zip(e, e[1:]))
+    assert all(v % 16 == 0 for v in e[:-1])
+    sizes = [b - a for a, b in zip(e, e[1:])]
+    assert max(sizes) - min(sizes) <= 32
