@@ -1180,7 +1180,7 @@ bool tc_supported(int64_t n, int64_t m, int d, int algo) {
 }
 
 #ifdef SOMGB_TC_PHASE_TIMING
-// Instrumented builds only: copies out (and optionally clears) the eight phase counters.
+// Instrumented builds only: copies out (and optionally clears) the TC_PHASES phase counters.
 extern "C" int somgb_tc_phase_cycles(unsigned long long* out8, int reset) {
     SOMGB_CUDA_TRY(cudaDeviceSynchronize());
     SOMGB_CUDA_TRY(cudaMemcpyFromSymbol(out8, g_tc_phase_cycles, TC_PHASES * sizeof(unsigned long long)));

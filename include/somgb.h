@@ -43,8 +43,9 @@ typedef struct CUstream_st* somgb_stream_t; /* == cudaStream_t; NULL = legacy de
 
 /* distance-search algorithms */
 #define SOMGB_ALGO_FP32 0       /* CUDA cores: float32 direct differences, margin-gated float64 recheck */
-#define SOMGB_ALGO_TC 1         /* tcgen05 split-FP16 distance GEMM, margin-gated recheck */
-#define SOMGB_ALGO_AUTO 2       /* TC where its shape limits allow, FP32 otherwise */
+#define SOMGB_ALGO_TC 1         /* tcgen05 split-FP16 distance GEMM, margin-gated recheck (D in {4, 8, 16, 32},
+                                   M <= 4096; somgb_algo_supported tells) */
+#define SOMGB_ALGO_AUTO 2       /* TC where its shape limits allow and N*M >= 2^22, FP32 otherwise */
 
 /* workspace query operations */
 #define SOMGB_OP_FIND_BMUS 0
