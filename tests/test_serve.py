@@ -212,6 +212,75 @@ def test_training_runs_on_its_own_loop_while_assignments_continue():
     assert srv.stats()['train']['count'] == 1
 
 
+class CountingExecutor(FakeExecutor):
+    """Records how many run_bmu calls were inside it at once."""
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.inside = 0
+        self.most = 0
+        self.lock = threading.Lock()
+
+    def run_bmu(self, entry, xs, slot=0, hist=None):
+        with self.lock:
+            self.inside += 1
+            self.most = max(self.most, self.inside)
+        try:
+            return super().run_bmu(entry, xs, slot=slot, hist=hist)
+        finally:
+            with self.lock:
+                self.inside -= 1
+
+
+def test_in_flight_bytes_hold_back_a_request_until_it_fits():
+    """Two 2000-byte requests under a 2500-byte budget: the second worker may not start the second one while the
+    first is on the device, however idle it is; it runs once the first has finished."""
+    ex = CountingExecutor(block_first=True)
+    with SomServer(ex, hbm_budget=2500, max_batch_rows=10, workers=2) as srv:
+        m = srv.add_map('a')
+        f0 = srv.submit_bmu(m, _req(0, 20))
+        time.sleep(0.1)
+        f1 = srv.submit_bmu(m, _req(1, 20))
+        time.sleep(0.2)
+        assert not f1.done()
+        ex.release.set()
+        assert f0.result(5)[0] == 0 and f1.result(5)[0] == 1
+    assert ex.most == 1
+
+
+def test_unknown_map_and_oversized_training_are_refused():
+    ex = FakeExecutor()
+    with SomServer(ex, hbm_budget=10_000) as srv:
+        with pytest.raises(KeyError):
+            srv.submit_bmu(3, _req(0))
+        big = srv.submit_train(_Som(), _req(0, 10_000), n_epochs=1)
+        with pytest.raises(MemoryError):
+            big.result(5)
+        small = srv.submit_train(_Som(), _req(0, 12), n_epochs=1)
+        assert isinstance(small.result(5), _Som)
+
+
+class FailingTrainExecutor(FakeExecutor):
+    def run_train(self, som, dataset, rho, kwargs, slot=0):
+        if kwargs.get('n_epochs') == 0:
+            raise ValueError('no epochs')
+        return super().run_train(som, dataset, rho, kwargs, slot=slot)
+
+
+def test_a_failing_training_fails_alone():
+    ex = FailingTrainExecutor()
+    with SomServer(ex) as srv:
+        m = srv.add_map('a')
+        bad = srv.submit_train(_Som(), _req(0, 5), n_epochs=0)
+        good = srv.submit_train(_Som(), _req(0, 5), n_epochs=2)
+        fb = srv.submit_bmu(m, _req(3))
+        with pytest.raises(ValueError):
+            bad.result(5)
+        assert isinstance(good.result(5), _Som)
+        assert fb.result(5)[0] == 3
+    assert srv.stats()['train']['count'] == 1
+
+
 def test_close_serves_what_is_queued():
     ex = FakeExecutor(block_first=True)
     srv = SomServer(ex, workers=1)
