@@ -58,6 +58,27 @@ def test_grid_points_follow_the_reference():
         HypParamFinder_SOM(g['x'], batch=False).find(1)
 
 
+def test_gndm_arithmetic_follows_the_reference():
+    """compute_gndm's densities from given maps (decontamination_som.py:603-626): n_gal and n_pix are the map sums,
+    gnd = catalogue / footprint where the footprint map is positive and NaN elsewhere, gndm = gnd at each winner."""
+    from decontamination_gb300.gndm import compute_gndm
+
+    class Som:
+        m, n, dtype = 2, 3, np.float32
+
+        def get_footprint_maps(self, x, rho):
+            cat = np.array([[4.0, 0.0, 3.0], [1.5, 2.0, 0.0]], dtype=np.float32)
+            foot = np.array([[2.0, 0.0, 3.0], [3.0, 0.0, 1.0]], dtype=np.float32)
+            return cat, foot, np.array([0, 2, 3, 1, 5, 0], dtype=np.int32)
+
+    r = compute_gndm(Som(), None, None)
+    assert r['n_gal'] == np.float32(10.5) and r['n_pix'] == np.float32(9.0)
+    want = np.array([[2.0, np.nan, 1.0], [0.5, np.nan, 0.0]], dtype=np.float32)
+    assert r['gnd'].dtype == np.float32
+    np.testing.assert_array_equal(r['gnd'], want)
+    np.testing.assert_array_equal(r['gndm'], want.ravel()[[0, 2, 3, 1, 5, 0]])
+
+
 @pytest.mark.gpu
 def test_covariance_on_the_gpu(cuda):
     import decontamination_gb300 as dg
