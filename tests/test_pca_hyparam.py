@@ -58,6 +58,25 @@ def test_grid_points_follow_the_reference():
         HypParamFinder_SOM(g['x'], batch=False).find(1)
 
 
+def test_argument_errors_are_the_reference_ones():
+    """The reference's ValueErrors (algo/covariance.py:152,239, algo/som_pca.py:54,253,257), raised before any
+    device work; online grids are not provided."""
+    from decontamination_gb300 import Covariance, HypParamFinder_SOM, SOM_PCA
+    with pytest.raises(ValueError):
+        Covariance.compute(3, np.zeros((4, 3), dtype=np.float32), ddof=-1)
+    with pytest.raises(ValueError):
+        Covariance.diagonalize(np.zeros((3, 2)))
+    with pytest.raises(ValueError):
+        SOM_PCA(4, 4, 1)
+    pca = SOM_PCA(4, 4, 3)
+    with pytest.raises(ValueError):
+        pca.train_from_cov_matrix(np.eye(3), min_weight=1.0, max_weight=1.0)
+    with pytest.raises(ValueError):
+        pca.train_from_cov_matrix(np.eye(3), apply_cdf=True, cdf_gain=0.0)
+    with pytest.raises(NotImplementedError):
+        HypParamFinder_SOM(np.zeros((100, 3), dtype=np.float32), batch=False).find(2)
+
+
 def test_gndm_arithmetic_follows_the_reference():
     """compute_gndm's densities from given maps (decontamination_som.py:603-626): n_gal and n_pix are the map sums,
     gnd = catalogue / footprint where the footprint map is positive and NaN elsewhere, gndm = gnd at each winner."""
