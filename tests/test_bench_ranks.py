@@ -1,4 +1,5 @@
-"""The multi-rank logic of bench.py on the CPU: two gloo ranks stand for two replicas.
+"""bench.py's host logic on the CPU: the multi-rank path (two gloo ranks stand for two replicas) and the reference
+arm's JSON line.
 
 Under torchrun every rank runs an independent replica of the workload. The job's time is the slowest rank's (a MAX
 all-reduce), its rate counts the units of all ranks, and the reference arm runs on rank 0 alone.
@@ -66,3 +67,22 @@ def test_reference_arm_runs_on_rank_zero_only():
     with contextlib.redirect_stdout(out):
         bench.reference_arm(Args(), 2, 1)
     assert out.getvalue() == ''
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the reference's CPU formulation, the oracle port) prints one JSON line with the
+    bench keys, the reference tag, its CPU baseline and an end-to-end figure with no device copies."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', '--steps', '1',
+                          '--warmup', '0', '--n', '20000'], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith('{')]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ('metric', 'value', 'unit', 'n_gpus', 'steps', 'warmup', 'ms_per_step', 'higher_is_better', 'scaling',
+              'vs_baseline', 'dtype', 'data', 'config', 'cpu_baseline', 'e2e'):
+        assert k in d, k
+    assert d['impl'] == 'reference' and d['metric'] == bench.METRIC and d['higher_is_better'] is True
+    assert d['value'] > 0 and d['cpu_baseline']['kind'] == 'port' and d['cpu_baseline']['cores'] >= 1
+    assert d['e2e'] == {'value': d['value'], 'unit': d['unit'], 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
