@@ -206,14 +206,16 @@ int somgb_train_iter_pass_f64(const double* x, const double* rho, int64_t n, int
                               double* num, double* den, void* ws, size_t ws_bytes, somgb_stream_t stream);
 
 /*
- * somgb_find_bmus for callers that cannot allocate device memory (code inside a stream capture, a host framework
- * with a fixed device-memory budget, a pipeline that only owns its input and output buffers). It has no counterpart
- * in the reference: it is the same computation as somgb_find_bmus, but its scratch is one static device array of
- * somgb_find_bmus_noalloc_scratch_bytes() bytes (4 MiB) inside the library, held by every GPU that loads it until the
- * process exits. Inputs with more rows than fit are processed in chunks; a map whose unit operand does not fit is
- * refused with SOMGB_ERR_WORKSPACE. The array is looked up once per device on the first call made with that device
- * current (make that first call before any stream capture). Every call on a device shares the array: calls that
- * overlap on the GPU (on different streams) race; calls in stream order do not. Nothing is allocated or freed.
+ * somgb_find_bmus for callers that cannot allocate device memory: a host framework that hands out a fixed
+ * device-memory budget up front and owns every allocation, or a pipeline that only holds the input and output buffers
+ * it passes in and has no allocator to call. It has no counterpart in the reference: it is the same computation as
+ * somgb_find_bmus, but its scratch is one static device array of somgb_find_bmus_noalloc_scratch_bytes() bytes
+ * (4 MiB) inside the library, held by every GPU that loads it until the process exits. Inputs with more rows than fit
+ * are processed in chunks; a map whose unit operand does not fit is refused with SOMGB_ERR_WORKSPACE. The first call
+ * on a device, with that device current, looks up the array's address (a failed lookup is retried by the next call);
+ * make that first call before any stream capture: during a capture it is refused with SOMGB_ERR_INVALID. Every call
+ * on a device shares the array: calls that overlap on the GPU (on different streams) race; calls in stream order do
+ * not. Nothing is allocated or freed.
  */
 int somgb_find_bmus_noalloc(const float* x, int64_t n, int d, const float* w, int64_t m, int algo, int32_t* bmu_out,
                             somgb_stream_t stream);

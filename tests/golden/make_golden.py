@@ -229,7 +229,8 @@ def make_cases(SOM_Batch):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default='/root/reference')
+    ap.add_argument('--reference', default=os.environ.get('DECONTAMINATION_REFERENCE'), required=not os.environ.get('DECONTAMINATION_REFERENCE'),
+                    help='checkout of lpsc-euclid/decontamination 0.0.1 (or set DECONTAMINATION_REFERENCE)')
     ap.add_argument('--out', default=HERE)
     args = ap.parse_args()
     SOM_Batch = load_reference(args.reference)

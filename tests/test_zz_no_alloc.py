@@ -1,8 +1,8 @@
 """The allocation-free BMU entry point (somgb_find_bmus_noalloc) against somgb_find_bmus.
 
-Callers that cannot allocate device memory (inside a stream capture, under a fixed device-memory budget, or holding
-only their own input and output buffers) use this entry point; its scratch is a static array inside the library that
-every call shares. This file is collected last so that a failure here does not hide any other test, and it passes both
+Callers that cannot allocate device memory (a framework that owns a fixed device-memory budget, or a pipeline that
+holds only its own input and output buffers) use this entry point; its scratch is a static array inside the library
+that every call shares. This file is collected last so that a failure here does not hide any other test, and it passes both
 alone in a fresh process and after the rest of the suite: each call must give exactly the BMUs of the workspace-based
 entry point, whatever an earlier call left in the shared array.
 """
@@ -36,7 +36,8 @@ def test_noalloc_matches_workspace_entry_point_twice(cuda, native, algo_name):
     assert native.lib().somgb_find_bmus_noalloc_scratch_bytes() == 4 << 20
     rng = np.random.default_rng(1234)
     cases = []
-    for n, m, d in ((300_000, 256, 16), (1_300_000, 1024, 8)):   # the second needs two chunks of the 4 MiB array
+    # the second needs two chunks of the 4 MiB array; the third leaves a last chunk of one row
+    for n, m, d in ((300_000, 256, 16), (1_300_000, 1024, 8), (1_300_001, 1024, 8)):
         x = np.exp(0.3 * rng.standard_normal((n, d))).astype(np.float32)
         w = x[rng.integers(0, n, m)] * (1 + 0.01 * rng.standard_normal((m, d))).astype(np.float32)
         cases.append((torch.from_numpy(x).to(cuda), torch.from_numpy(np.ascontiguousarray(w)).to(cuda)))
