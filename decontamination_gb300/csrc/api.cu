@@ -72,7 +72,8 @@ int num_sms() {
 
 namespace {
 
-// Workspace layout: [0, 256) header (u64 recheck counter), then op-specific arrays, each 256-byte aligned.
+// Workspace layout: [0, 256) header (u64 recheck counter at 0, u32 status word of the call at 8), then op-specific
+// arrays, each 256-byte aligned.
 constexpr size_t WS_HEADER = 256;
 
 struct Workspace {
@@ -128,8 +129,9 @@ int check_common(const void* x, int64_t n, int d, const void* w, int64_t m, int 
 }
 
 int run_pass(PassArgs a, int algo, const Workspace& ws, bool tc, cudaStream_t stream) {
-    SOMGB_CUDA_TRY(cudaMemsetAsync(ws.counter, 0, sizeof(unsigned long long), stream));
+    SOMGB_CUDA_TRY(cudaMemsetAsync(ws.counter, 0, 16, stream));   // recheck counter and status word
     a.recheck_count = ws.counter;
+    a.status = (unsigned int*)(ws.counter + 1);
     // the tensor-core pass reads sample and unit rows as float4 and topographic coordinates as float2
     const bool aligned = ((uintptr_t)a.x) % 16 == 0 && ((uintptr_t)a.w) % 16 == 0 &&
                          (!(a.outs & OUT_ERR) || ((uintptr_t)a.topo) % 8 == 0);
@@ -140,6 +142,7 @@ int run_pass(PassArgs a, int algo, const Workspace& ws, bool tc, cudaStream_t st
     if (algo == SOMGB_ALGO_TC)
         return set_error(SOMGB_ERR_UNSUPPORTED, "tensor-core path unsupported for n=%lld m=%lld d=%d on this device",
                          (long long)a.n, (long long)a.m, a.d);
+    a.pairs = nullptr;   // the plain FP32 form neither uses nor updates seeds
     return launch_k0_pass(a, stream);
 }
 
@@ -296,6 +299,42 @@ int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, co
     a.err3 = err3; a.train_bmu = bmu_out;
     a.outs = OUT_TRAIN | (err3 ? OUT_ERR : 0);
     return run_pass(a, algo, W, tc, (cudaStream_t)stream);
+}
+
+int somgb_train_bmu_pass_seeded(const float* x, const double* rho, int64_t n, int d, const float* w,
+                                const float* topo, int64_t m, double penalty, int algo, int32_t* bmu_out,
+                                double* err3, int32_t* pairs, int pairs_in, void* ws, size_t ws_bytes,
+                                somgb_stream_t stream) {
+    if (int s = check_common(x, n, d, w, m, algo)) return s;
+    if (!bmu_out && !err3) return set_error(SOMGB_ERR_INVALID, "bmu_out and err3 are both NULL");
+    if (err3 && !topo) return set_error(SOMGB_ERR_INVALID, "topo is NULL");
+    if (n > 0 && !pairs) return set_error(SOMGB_ERR_INVALID, "pairs is NULL");
+    if (((uintptr_t)pairs) % 8) return set_error(SOMGB_ERR_INVALID, "pairs must be 8-byte aligned");
+    Workspace W;
+    bool tc = false;
+    if (int s = carve(ws, ws_bytes, SOMGB_OP_FIND_BMUS, n, m, d, algo, &W, &tc)) return s;
+    if (n == 0) return SOMGB_OK;
+    PassArgs a{};
+    a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.topo = topo; a.penalty = penalty;
+    a.err3 = err3; a.train_bmu = bmu_out; a.pairs = pairs; a.pairs_in = pairs_in != 0;
+    a.outs = (bmu_out ? OUT_TRAIN : 0) | (err3 ? OUT_ERR : 0);
+    return run_pass(a, algo, W, tc, (cudaStream_t)stream);
+}
+
+int somgb_workspace_status(const void* ws, unsigned int* status, int clear, somgb_stream_t stream) {
+    if (!ws || !status) return set_error(SOMGB_ERR_INVALID, "ws/status is NULL");
+    if (((uintptr_t)ws) % 256) return set_error(SOMGB_ERR_INVALID, "workspace pointer must be 256-byte aligned");
+    unsigned int* word = (unsigned int*)((char*)ws + 8);
+    SOMGB_CUDA_TRY(cudaMemcpyAsync(status, word, sizeof(unsigned int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    SOMGB_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    if (clear) SOMGB_CUDA_TRY(cudaMemsetAsync(word, 0, sizeof(unsigned int), (cudaStream_t)stream));
+    return SOMGB_OK;
+}
+
+int somgb_debug_tc_withhold(int64_t row_tile, unsigned int wait_limit) {
+    if (row_tile < 0 || wait_limit == 0) return set_error(SOMGB_ERR_INVALID, "row_tile must be >= 0, wait_limit > 0");
+    tc_debug_withhold(row_tile, wait_limit);
+    return SOMGB_OK;
 }
 
 int somgb_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, somgb_stream_t stream) {

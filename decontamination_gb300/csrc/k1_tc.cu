@@ -19,27 +19,36 @@
 // Using |w'_j|^2 <= 2|x'|^2 + 2 d'_j (d'_j = |x' - w'_j|^2) every term is bounded by
 //   |s~_j - s_j| <= alpha |x'|^2 + beta d'_j + gamma,
 // with alpha, beta computed on the host (tc_error_coefficients). A unit can beat the tile's best (or, for the
-// error sums, the second best) only if s~_j <= m + 2 (alpha |x'|^2 + beta (m + |x'|^2) + gamma) / (1 - beta), m
-// being the best (second-best) s~ of the row.
+// error sums, the second best) only if s~_j <= thr(m) = m + 2 (alpha |x'|^2 + beta (m + |x'|^2) + gamma) / (1 - beta)
+// + gamma, m being the best (second-best) s~ of the row; thr is non-decreasing in m, so any upper bound of m gives a
+// threshold that keeps every such unit.
 //
-// Epilogue, per row tile: sweep 1 streams the TMEM tiles and keeps each row's smallest s~ (and, for the error sums,
-// the second-smallest 4- or 8-unit group minimum) with FP32 min/max; sweep 2 recomputes the same MMAs (the tensor pipe
-// has slack) and marks every unit under the threshold in a bit mask — the only units that can be the reference's
-// BMU (or second BMU). Each candidate's distance is then evaluated on CUDA cores with float32 differences (the
-// reference's terms) and ranked; ranks within float32 rounding of each other are decided by compensated float32 sums
-// and, failing that, by the reference's float64 sum. Rows with more than CAPR candidates, non-finite features or
-// overflowing distances go to an exact per-row recheck.
+// Epilogue. Each sweep warp reads its rows' s~ in 32-column chunks and keeps, per row, the running minimum (for the
+// error sums, the two smallest 8-unit group minima: an upper bound of the second-best s~). When a row of the warp can
+// have a candidate in a chunk (chunk minimum at or under its threshold), the warp builds the chunk's candidate bit
+// masks and every row with a non-zero mask appends (mask word, chunk minimum, chunk) to its own short list. Two forms:
+//   seeded passes (one sweep): the threshold starts at thr of the row's seed (an upper bound of m from the units that
+//     were best under an earlier map, tc_seed_kernel) and falls with the chunks swept; a chunk's mask is built
+//     against the threshold known before it and built again, against the one that takes the chunk in, only where
+//     that fell by more than a small slack (a loose or missing seed);
+//   passes without seeds (two sweeps, every MMA issued twice): the first sweep finds each row's bounds, the two
+//     column halves combine them into the final threshold, the second sweep builds the lists against it.
+// A full list first drops the entries whose chunk minimum is above the current threshold. The resolvers take each
+// row's entries whose chunk minimum is at or under the row's final threshold (both halves and the seed combined),
+// evaluate those candidates on CUDA cores with float32 differences (the reference's terms) and rank them; ranks
+// within float32 rounding of each other are decided by compensated float32 sums and, failing that, by the
+// reference's float64 sum. Rows with more than CAPR candidates, a full list, non-finite features or overflowing
+// distances go to an exact per-row recheck.
 //
-// Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
-//   warp 13     TMA producer: the unit operand B (resident: one bulk copy; LARGE maps: a ring of column tiles),
-//               sample tiles (2-D tiled TMA, 2-stage ring);
-//   warp 12     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
+// Pipeline (one persistent CTA per SM, 576 threads, every hand-off an mbarrier):
+//   warp 17     TMA producer: the unit operand B (resident: one bulk copy; else a ring of column tiles in the MMAs'
+//               order), sample tiles (2-D tiled TMA, 2-stage ring);
+//   warp 16     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
 //   warps 0-7   converters (FP32 tile -> centred split-FP16 A tile) and sweeps; warp e reads TMEM lanes
-//               32(e&3).. and column half e>>2 and writes its rows' mask words and per-row summary bits;
-//   warps 8-11  resolvers: thread r of warp 8+q decides row 32q+r of row tile t while the sweeps already work on
-//               row tile t+1: it copies the row's non-zero mask words (handing the masks back), computes the
-//               candidates' distances from the unit rows (shared memory when they fit, else L2), ranks them,
-//               decides and writes the outputs.
+//               32(e&3).. and column half e>>2 and writes its rows' candidate lists (two list buffers);
+//   warps 8-15  resolvers in two groups of four, group g taking the row tiles t with t % 2 == g (list buffer g):
+//               thread r of the group's warp q decides row 32q+r: candidates' distances from the unit rows (shared
+//               memory when they fit, else L2), ranking, decision, outputs.
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
@@ -55,9 +64,9 @@ namespace somgb {
 __device__ unsigned int g_tc_status;
 
 // Optional per-phase cycle counters of the epilogue warps (compiled in only with -DSOMGB_TC_PHASE_TIMING; read with
-// cudaMemcpyFromSymbol). Sweep warps: 0 wait for TMEM (sweep 1), 1 sweep 1, 2 wait (sweep 2), 3 sweep 2, 4 convert,
-// 5 half exchange and candidate-buffer wait; resolver warps: 6 wait for candidates, 7 emit, 8 recheck listing,
-// 9 candidate loop, 10 decision; the MMA thread: 12 wait for a free TMEM accumulator, 13 wait for a unit-operand tile.
+// cudaMemcpyFromSymbol). Sweep warps: 0 wait for TMEM, 1 sweep, 4 convert, 5 wait for a free list buffer; resolver
+// warps: 6 wait for candidates, 7 emit, 8 recheck listing, 9 candidate loop, 10 decision; the MMA thread: 12 wait for
+// a free TMEM accumulator, 13 wait for a unit-operand tile.
 #ifdef SOMGB_TC_PHASE_TIMING
 constexpr int TC_PHASES = 14;
 __device__ unsigned long long g_tc_phase_cycles[TC_PHASES];
@@ -83,15 +92,17 @@ constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
 constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
 constexpr int CAPR = 24;          // candidates a resolver ranks per row
-constexpr int KW = 8;             // non-zero candidate-mask words a resolver copies per row
+constexpr int CAP = 4;            // candidate-list entries per row and column half
 constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
-constexpr int MAX_U = 16;         // column tiles per row tile (candidate summaries: 32-bit words of 8 tiles per half)
+constexpr int MAX_U = 64;         // column tiles per row tile (a list entry names its chunk, 4 per tile and half, in a byte)
 constexpr int NBARS = 40;         // mbarrier slots
 constexpr int BMAX = 4;           // deepest ring of streamed unit-operand tiles (slots 28 .. 28 + 2 BMAX - 1)
 static_assert(28 + 2 * BMAX <= NBARS, "mbarrier slots");
+static_assert(4 * MAX_U <= 256, "chunk ids are bytes");
 constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
-constexpr int RES_WARPS = 4;
+constexpr int RES_GROUP = 4;               // resolver warps per row tile (one thread per row)
+constexpr int RES_WARPS = 2 * RES_GROUP;   // two groups, alternate row tiles (each owns one list buffer)
 constexpr int MMA_WARP = SWEEP_WARPS + RES_WARPS;
 constexpr int TMA_WARP = MMA_WARP + 1;
 constexpr int NUM_THREADS = (TMA_WARP + 1) * 32;
@@ -100,7 +111,7 @@ constexpr float Q_COLUMN = 2048.0f;   // A's value in the two q columns (B holds
 constexpr float GAMMA = 0.00390625f;  // 2^-8: absolute error bound of the FP16 subnormal range, in scaled units
 constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go to the exact recheck
 constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN);
-
+constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded mbarrier wait (each at most about 1 us)
 // K layout of the operands (elements per row, FP16). D a multiple of 16: A = [x_hi | x_lo | q columns],
 // B = [-2w_hi | -2w_lo | q_hi q_lo 0...], and the MMA K-steps pair the blocks (lo.hi, hi.lo, hi.hi, then q), so no
 // block is stored twice. Other D: A = [x_lo | x_hi | x_hi | 2^11 2^11 | 0...], B = [-2w_hi | -2w_lo | -2w_hi | q_hi
@@ -132,8 +143,8 @@ struct TcShape {
     int utiles = 0;
     int bstages = 0;   // 0: the whole unit operand resident in shared memory; else a ring of this many column tiles
     size_t b_bytes = 0, b_tile = 0, a_bytes = 0, x_bytes = 0;
-    size_t off_a = 0, off_x = 0, off_mask = 0, off_sum = 0, off_flag = 0, off_rlist = 0, off_part = 0, off_center = 0,
-           off_bar = 0, off_w = 0, smem = 0;
+    size_t off_a = 0, off_x = 0, off_lw = 0, off_lm = 0, off_part = 0, off_row = 0, off_lc = 0, off_cnt = 0,
+           off_flag = 0, off_center = 0, off_bar = 0, off_w = 0, smem = 0;
 };
 
 // Layout after a unit-operand region of `bregion` bytes; returns the end offset (before the unit rows).
@@ -143,18 +154,24 @@ size_t tc_layout(TcShape& s, size_t bregion) {
     off += 2 * align_up(s.a_bytes, 1024);
     s.off_x = off;
     off += XSTAGES * s.x_bytes;
-    s.off_mask = off;
-    off += (size_t)HALVES * s.utiles * 4 * TM * 4;
-    s.off_sum = off;
-    off += (size_t)2 * HALVES * TM * 4;
-    s.off_flag = off;
-    off += TM;
-    s.off_rlist = off;
-    off += (size_t)KW * TM * 6;
+    // candidate lists, [buffer][half][entry][row]: mask words, chunk minima, chunk ids; per buffer, half and row the
+    // (a1, a2) of the half and the entry count; per buffer and row |x'|^2, the seed bound and the recheck flag
+    s.off_lw = off;
+    off += (size_t)2 * HALVES * CAP * TM * 4;
+    s.off_lm = off;
+    off += (size_t)2 * HALVES * CAP * TM * 4;
     s.off_part = off;
-    off += (size_t)HALVES * TM * 8;
-    s.off_center = off;
-    off += align_up((size_t)(s.d + 1) * 4, 16);
+    off += (size_t)2 * HALVES * TM * 8;
+    s.off_row = off;
+    off += (size_t)2 * TM * 8;
+    s.off_lc = off;
+    off += (size_t)2 * HALVES * CAP * TM;
+    s.off_cnt = off;
+    off += (size_t)2 * HALVES * TM;
+    s.off_flag = off;
+    off += (size_t)2 * TM;
+    s.off_center = align_up(off, 16);
+    off = s.off_center + align_up((size_t)(s.d + 1) * 4, 16);
     s.off_bar = align_up(off, 8);
     return s.off_bar + NBARS * 8;
 }
@@ -169,32 +186,31 @@ TcShape tc_shape(int64_t m, int d) {
     s.b_tile = (size_t)TN * s.kpad * 2;
     s.a_bytes = (size_t)TM * s.kpad * 2;
     s.x_bytes = align_up((size_t)TM * d * 4, 128);
-    // the whole unit operand when it fits, else a ring of BMAX (down to 2) column tiles streamed from L2 by the TMA
-    // warp
-    size_t off = tc_layout(s, s.b_bytes);
-    if (off + 128 > SMEM_LIMIT) {
-        for (int st = BMAX; st >= 2; --st) {
+    const size_t w_bytes = (size_t)m * d * 4;   // the float32 unit rows, for the resolvers' candidate distances
+    // In order of preference: the unit operand resident with the unit rows; a ring of BMAX (down to 2) column tiles
+    // streamed from L2 with the unit rows; then the same without the unit rows (the resolvers read them from L2).
+    for (int rows = 1; rows >= 0; --rows) {
+        for (int st : {0, BMAX, BMAX - 1, 2}) {
             s.bstages = st;
-            off = tc_layout(s, (size_t)st * align_up(s.b_tile, 1024));
-            if (off + 128 <= SMEM_LIMIT) break;
+            size_t off = tc_layout(s, st == 0 ? s.b_bytes : (size_t)st * align_up(s.b_tile, 1024));
+            s.off_w = 0;
+            if (rows) {
+                s.off_w = align_up(off, 16);
+                off = s.off_w + w_bytes;
+            }
+            s.smem = off + 128;   // slack for aligning the dynamic base to 128 bytes (TMA tile destinations)
+            if (s.smem <= SMEM_LIMIT) return s;
         }
     }
-    // the float32 unit rows, for the resolvers' candidate distances, when they fit (otherwise read from L2)
-    const size_t w_bytes = (size_t)m * d * 4;
-    const size_t off_w = align_up(off, 16);
-    if (off_w + w_bytes + 128 <= SMEM_LIMIT) {
-        s.off_w = off_w;
-        off = off_w + w_bytes;
-    }
-    s.smem = off + 128;   // slack for aligning the dynamic base to 128 bytes (TMA tile destinations)
-    return s;
+    return s;   // does not fit (smem > SMEM_LIMIT): refused by tc_shape_ok
 }
 
-// Scratch: [B operand | centre (d floats) and scale | recheck row list (n int32)]
+// Scratch: [B operand | centre (d floats) and scale | recheck row list (n int32) | seed bounds (n floats)]
 struct TcWs {
     uint8_t* b = nullptr;
     float* center = nullptr;
     int32_t* rows = nullptr;
+    float* seed = nullptr;
 };
 
 size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
@@ -206,11 +222,14 @@ size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
     off += align_up((size_t)(d + 1) * 4, 256);   // centre and scale
     size_t orow = off;
     off += align_up((size_t)std::max<int64_t>(n, 1) * 4, 256);
+    size_t oseed = off;
+    off += align_up((size_t)std::max<int64_t>(n, 1) * 4, 256);
     if (out && base) {
         uint8_t* p = (uint8_t*)base;
         out->b = p + ob;
         out->center = (float*)(p + oc);
         out->rows = (int32_t*)(p + orow);
+        out->seed = (float*)(p + oseed);
     }
     return off;
 }
@@ -376,6 +395,53 @@ __global__ void tc_prep_b_kernel(const float* __restrict__ w, int64_t m, int d, 
     put(qc + 1, (float)(qs - (double)__half2float(qh)));
 }
 
+// Seed bounds for a pass whose rows' best units under an earlier map are known (pairs[2i], pairs[2i+1]; -1 or out of
+// range when not). For ERR passes the bound covers the second-best s~: both units valid and distinct, the larger of
+// their bounds (two distinct units lie at or under it); otherwise the bound of the first unit covers the best s~.
+// With d' = |x' - w'_b|^2 and |x'|^2 evaluated in float32 (relative error below eps = (D + 4) 2^-23 each), the GEMM
+// value of unit b satisfies s~_b <= d'(1 + eps)(1 + beta) - |x'|^2 (1 - eps) + alpha |x'|^2 (1 + eps) + gamma, and the
+// float32 evaluation of that expression is covered by a further 2^-20 (d' + |x'|^2). Any unit gives a valid bound,
+// so a stale or wrong pair only loosens the search, never changes a result. +inf where no bound is known.
+template <int DT>
+__global__ void tc_seed_kernel(const float* __restrict__ x, int64_t n, const float* __restrict__ w, int64_t m,
+                               const float* __restrict__ center, const int32_t* __restrict__ pairs, int need_two,
+                               float alpha, float beta, float* __restrict__ seed) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 pr = __ldg((const int2*)pairs + i);
+    const bool ok1 = pr.x >= 0 && pr.x < m;
+    const bool ok2 = pr.y >= 0 && pr.y < m && pr.y != pr.x;
+    if (!ok1 || (need_two && !ok2)) {
+        seed[i] = INFINITY;
+        return;
+    }
+    const float scale = center[DT];
+    const float* xr = x + i * DT;
+    const float* w1 = w + (int64_t)pr.x * DT;
+    const float* w2 = w + (int64_t)(need_two ? pr.y : pr.x) * DT;
+    float xn = 0.0f, d1 = 0.0f, d2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < DT; ++k) {
+        const float ck = center[k];
+        const float xp = (__ldg(xr + k) - ck) * scale;
+        xn = fmaf(xp, xp, xn);
+        const float t1 = xp - (__ldg(w1 + k) - ck) * scale;
+        d1 = fmaf(t1, t1, d1);
+        const float t2 = xp - (__ldg(w2 + k) - ck) * scale;
+        d2 = fmaf(t2, t2, d2);
+    }
+    const float dd = fmaxf(d1, d2);
+    if (!(dd < 1.0e30f) || !(xn < 1.0e30f)) {
+        seed[i] = INFINITY;
+        return;
+    }
+    const float eps = (float)(DT + 4) * 1.1920929e-7f;   // (D + 4) 2^-23
+    const float up = 1.0f + eps;
+    const float ub = dd * up * (1.0f + beta) - xn * (1.0f - eps) + alpha * xn * up + GAMMA +
+                     9.5367432e-7f * (dd + xn);   // 2^-20 (d' + |x'|^2)
+    seed[i] = ub;
+}
+
 // ---------------------------------------------------------------------------------------------------------------------
 // main pass
 // ---------------------------------------------------------------------------------------------------------------------
@@ -386,14 +452,25 @@ struct TcArgs {
     const float* center;
     int32_t* rows;
     unsigned long long* row_count;
+    const float* seed;       // per-row seed bounds, or NULL (the two-sweep form)
     int kpad;
     int utiles;
-    float alpha, beta;
-    size_t off_a, off_x, off_mask, off_sum, off_flag, off_rlist, off_part, off_center, off_bar, off_w, a_stride, x_stride;
+    float alpha, beta, kthr;   // kthr = 2 / (1 - beta), rounded up
+    size_t off_a, off_x, off_lw, off_lm, off_part, off_row, off_lc, off_cnt, off_flag, off_center, off_bar, off_w,
+        a_stride, x_stride;
     uint32_t b_bytes;
     uint32_t b_tile;         // bytes of one column tile of the unit operand
     int bstages;             // 0: resident unit operand; else the ring depth
+    uint32_t wait_limit;     // polls of the protocol waits (WAIT_LIMIT; shorter only under the test hook)
+    int64_t withhold_tile;   // test hook: the row tile whose samples the producer never loads (-1: none)
 };
+
+// thr(m): the largest s~ a unit can have and still be the best (second best) unit of a row whose best (second-best)
+// s~ is m; axg = alpha |x'|^2 + gamma. Non-decreasing in m (every operation is, in round-to-nearest).
+__device__ __forceinline__ float thr_of(float mref, float xn, float axg, float beta, float kthr) {
+    const float dref = fmaxf(0.0f, mref + xn);
+    return fmaf(kthr, fmaf(beta, dref, axg), mref) + GAMMA;
+}
 
 // float32 distance over the reference's float32 differences: four FMA chains (features k mod 4) summed at the end,
 // so the dependent chain is D/4 + 2 long; any summation order keeps |df - d_ref| <= (D+2) 2^-24 d_ref
@@ -436,22 +513,46 @@ __device__ __forceinline__ bool lex_before(float da, int32_t ja, float db, int32
     return ja >= 0 && (jb < 0 || da < db || (da == db && ja < jb));
 }
 
+// minimum of v[B .. B + 16) (NaN ignored)
+template <int B>
+__device__ __forceinline__ float min16(const uint32_t (&v)[32]) {
+    auto f = [&](int i) { return __uint_as_float(v[B + i]); };
+    const float t0 = fmin3(f(0), f(1), f(2)), t1 = fmin3(f(3), f(4), f(5)), t2 = fmin3(f(6), f(7), f(8));
+    const float t3 = fmin3(f(9), f(10), f(11)), t4 = fmin3(f(12), f(13), f(14));
+    return fminf(fmin3(t0, t1, t2), fmin3(t3, t4, f(15)));
+}
 
-// LARGE: the unit operand streams through a ring (more than fits in shared memory) or the map has more than 8 column
-// tiles; the other instantiations (resident operand, at most 8 column tiles) carry none of that logic.
-template <bool ERR, int DT, bool LARGE>
+// minimum of v[b .. b + 8) (NaN ignored)
+__device__ __forceinline__ float min8(const uint32_t (&v)[32], int b) {
+    auto f = [&](int i) { return __uint_as_float(v[b + i]); };
+    return fmin3(fmin3(f(0), f(1), f(2)), fmin3(f(3), f(4), f(5)), fminf(f(6), f(7)));
+}
+
+// One sweep warp's row: its running state over the chunks of its column half.
+struct RowSweep {
+    float a1, a2;     // smallest and second-smallest group minimum (ERR) / the running minimum (a1)
+    float thr;        // running threshold (never rises)
+    int cnt;          // list entries
+    bool ovf;         // more chunks with candidates than CAP
+};
+
+// The tensor-core pass. ERR: the error sums (second BMU ranked too); the bound of the second-best s~ is the
+// second-smallest 8-unit group minimum. TWO (passes without seeds): every column tile is computed twice, the first
+// sweep finds each row's final threshold and the second builds the candidate lists against it; otherwise (seeded
+// passes) one sweep builds them against the running threshold of the seed and the chunks already swept.
+template <bool ERR, int DT, bool TWO>
 __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs P) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
-    uint32_t* sMask = (uint32_t*)(smem + P.off_mask);   // [half][u][4][TM]: bit 31-i of word w: column 32w+i is a candidate
-    uint32_t* sSum = (uint32_t*)(smem + P.off_sum);     // [u / 8][half][TM]: bit 4(u%8)+w set when mask word (u, w) is
-                                                        // non-zero (the second pair only for more than 8 column tiles)
-    uint8_t* sFlag = smem + P.off_flag;                 // [TM]: the row goes to the exact recheck
-    uint32_t* sWords = (uint32_t*)(smem + P.off_rlist);  // [KW][TM]: the resolvers' copies of the non-zero mask words
-    uint16_t* sWtop = (uint16_t*)(sWords + KW * TM);      // [KW][TM]: the unit of bit 0 of each, plus 31
-    float2* sPart = (float2*)(smem + P.off_part);       // [half][TM]: (m1, m2) of the half
+    uint32_t* sLw = (uint32_t*)(smem + P.off_lw);   // [2][HALVES][CAP][TM] mask words: bit 31-i = column 32c+i
+    float* sLm = (float*)(smem + P.off_lm);         // [2][HALVES][CAP][TM] the chunk's minimum s~
+    uint8_t* sLc = smem + P.off_lc;                 // [2][HALVES][CAP][TM] chunk id u * 4 + c
+    uint8_t* sCnt = smem + P.off_cnt;               // [2][HALVES][TM] entries; bit 7: the list overflowed
+    float2* sPart = (float2*)(smem + P.off_part);   // [2][HALVES][TM] (a1, a2) of the half
+    float2* sRow = (float2*)(smem + P.off_row);     // [2][TM] (|x'|^2, seed bound)
+    uint8_t* sFlag = smem + P.off_flag;             // [2][TM] the row goes to the exact recheck
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
     uint64_t* x_full = bars + 1;    // [XSTAGES]
@@ -460,10 +561,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint64_t* a_empty = bars + 9;   // [2]
     uint64_t* t_full = bars + 11;   // [2]
     uint64_t* t_empty = bars + 13;  // [2]
-    uint64_t* m_full = bars + 15;   // the sweeps have written the candidate masks of a row tile
-    uint64_t* m_empty = bars + 16;  // the resolvers have read them
+    uint64_t* m_full = bars + 15;   // [2]: the sweeps have written the candidate lists of a row tile
+    uint64_t* m_empty = bars + 17;  // [2]: the resolvers are done with them
     uint64_t* drain = bars + 19;
-    uint64_t* p_full = bars + 20;   // [2][4]: both halves of a lane quarter have published (m1, m2)
+    uint64_t* p_full = bars + 20;   // [2][4] two-sweep form: both halves of a lane quarter have published (a1, a2)
     uint64_t* bs_full = bars + 28;  // [BMAX]: a column tile of the unit operand has landed (streamed operand)
     uint64_t* bs_empty = bars + 28 + BMAX; // [BMAX]: the MMAs reading it have completed
     __shared__ uint32_t tmem_base_s;
@@ -473,7 +574,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int d = DT;
     constexpr int kpad = k_width(DT);
+    constexpr int SWEEPS = TWO ? 2 : 1;
     const int U = P.utiles;
+    const uint32_t lim = P.wait_limit;
     const int64_t num_tiles = (a.n + TM - 1) / TM;
     const int64_t n_my = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
@@ -492,10 +595,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             ptx::mbar_init(a_empty + s, 1);
             ptx::mbar_init(t_full + s, 1);
             ptx::mbar_init(t_empty + s, SWEEP_WARPS);
+            ptx::mbar_init(m_full + s, SWEEP_WARPS);
+            ptx::mbar_init(m_empty + s, RES_GROUP);
             for (int qq = 0; qq < 4; ++qq) ptx::mbar_init(p_full + s * 4 + qq, HALVES);
         }
-        ptx::mbar_init(m_full, SWEEP_WARPS);
-        ptx::mbar_init(m_empty, RES_WARPS);
         ptx::mbar_init(drain, 1);
         ptx::fence_mbar_init();
         abort_s = 0;
@@ -518,8 +621,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     volatile int* abort_v = &abort_s;
     auto fail = [&](unsigned code) {
         atomicOr(&g_tc_status, code);
+        if (a.status) atomicOr(a.status, code);
         *abort_v = 1;
     };
+    // Whole-warp forms for the sweep and resolver warps: a wait's outcome and the abort flag are made the same for
+    // every lane, so that no lane leaves a loop whose warp-wide votes the others still execute.
+    auto wwait = [&](uint64_t* bar, uint32_t parity) -> bool {
+        return __all_sync(0xffffffffu, ptx::mbar_wait(bar, parity, lim));
+    };
+    auto waborted = [&]() -> bool { return __any_sync(0xffffffffu, *abort_v != 0); };
 #ifdef SOMGB_TC_PHASE_TIMING
     unsigned long long _tc_acc[TC_PHASES] = {};
     long long _tc_t0 = 0;
@@ -528,7 +638,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     if (warp == TMA_WARP) {
         if (lane == 0 && n_my > 0) {
             ptx::prefetch_tensormap(&tmap);
-            const int BST = LARGE ? P.bstages : 0;
+            const int BST = P.bstages;
             const int BSTD = BST > 0 ? BST : 1;   // divisor in the ring arithmetic (used only when BST > 0)
             if (BST == 0) {
                 ptx::mbar_arrive_expect_tx(b_full, P.b_bytes);
@@ -538,18 +648,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 }
             }
             const uint32_t b_stride = (P.b_tile + 1023u) & ~1023u;
-            int64_t issued = 0, kb = 0;
+            int64_t issued = 0, kb = 0, withheld = -1;
             bool ok = true;
             auto issue_x = [&](int64_t it) -> bool {
                 const int s = (int)(it % XSTAGES);
-                if (it >= XSTAGES && !ptx::mbar_wait(x_empty + s, (uint32_t)((it / XSTAGES - 1) & 1))) {
+                if (it >= XSTAGES && !ptx::mbar_wait(x_empty + s, (uint32_t)((it / XSTAGES - 1) & 1), lim)) {
                     fail(1u);
                     return false;
                 }
                 const int64_t t = blockIdx.x + it * gridDim.x;
+                issued = it + 1;
+                if (t == P.withhold_tile) {   // test hook: this tile is never loaded, so its consumer's wait runs out
+                    withheld = it;
+                    return true;
+                }
                 ptx::mbar_arrive_expect_tx(x_full + s, (uint32_t)(TM * d * 4));
                 ptx::tma_load_2d(smem + P.off_x + s * P.x_stride, &tmap, 0, (int32_t)(t * TM), x_full + s);
-                issued = it + 1;
                 return true;
             };
             if (BST == 0) {
@@ -558,37 +672,37 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 // sample tiles one row tile ahead of the unit-operand tiles, which go in the MMAs' order
                 for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
                     while (ok && issued < n_my && issued <= it + 1) ok = issue_x(issued);
-                    for (int sweep = 0; ok && sweep < 2; ++sweep) {
-                        for (int u = 0; u < U && !*abort_v; ++u, ++kb) {
-                            const int st = (int)(kb % BSTD);
-                            if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BSTD - 1) & 1))) {
-                                fail(4096u);
-                                ok = false;
-                                break;
-                            }
-                            ptx::mbar_arrive_expect_tx(bs_full + st, P.b_tile);
-                            const uint8_t* src = P.b + (size_t)u * P.b_tile;
-                            for (uint32_t off = 0; off < P.b_tile; off += 32768u) {
-                                const uint32_t len = P.b_tile - off < 32768u ? P.b_tile - off : 32768u;
-                                ptx::bulk_g2s(sB + (size_t)st * b_stride + off, src + off, len, bs_full + st);
-                            }
+                    for (int uu = 0; ok && uu < SWEEPS * U && !*abort_v; ++uu, ++kb) {
+                        const int u = uu >= U ? uu - U : uu;
+                        const int st = (int)(kb % BSTD);
+                        if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BSTD - 1) & 1), lim)) {
+                            fail(4096u);
+                            ok = false;
+                            break;
+                        }
+                        ptx::mbar_arrive_expect_tx(bs_full + st, P.b_tile);
+                        const uint8_t* src = P.b + (size_t)u * P.b_tile;
+                        for (uint32_t off = 0; off < P.b_tile; off += 32768u) {
+                            const uint32_t len = P.b_tile - off < 32768u ? P.b_tile - off : 32768u;
+                            ptx::bulk_g2s(sB + (size_t)st * b_stride + off, src + off, len, bs_full + st);
                         }
                     }
                 }
             }
             if (*abort_v || !ok) {
-                // let the copies still in flight land before the CTA releases its shared memory
+                // let the copies still in flight land before the CTA releases its shared memory (these waits end:
+                // every copy waited for was issued)
                 if (BST == 0) ptx::mbar_wait(b_full, 0);
                 for (int64_t k = issued > XSTAGES ? issued - XSTAGES : 0; k < issued; ++k)
-                    ptx::mbar_wait(x_full + (int)(k % XSTAGES), (uint32_t)((k / XSTAGES) & 1));
+                    if (k != withheld) ptx::mbar_wait(x_full + (int)(k % XSTAGES), (uint32_t)((k / XSTAGES) & 1));
                 for (int64_t k = kb > BST ? kb - BST : 0; BST > 0 && k < kb; ++k)
                     ptx::mbar_wait(bs_full + (int)(k % BSTD), (uint32_t)((k / BSTD) & 1));
             }
         }
     } else if (warp == MMA_WARP) {
         if (lane == 0 && n_my > 0) {
-            const int BST = LARGE ? P.bstages : 0;
-            bool ok = BST > 0 || ptx::mbar_wait(b_full, 0);
+            const int BST = P.bstages;
+            bool ok = BST > 0 || ptx::mbar_wait(b_full, 0, lim);
             if (!ok) fail(2u);
             const uint32_t sbo = (uint32_t)(kpad / 8) * 128u;
             const uint32_t b_addr = ptx::smem_u32(sB);
@@ -598,44 +712,43 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             uint32_t bpar = 0;
             for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
                 const int s = (int)(it & 1);
-                if (!ptx::mbar_wait(a_full + s, (uint32_t)((it >> 1) & 1))) { fail(4u); break; }
+                if (!ptx::mbar_wait(a_full + s, (uint32_t)((it >> 1) & 1), lim)) { fail(4u); break; }
                 ptx::tc_fence_after();
                 const uint32_t a_addr = ptx::smem_u32(smem + P.off_a + s * P.a_stride);
-                for (int sweep = 0; ok && sweep < 2; ++sweep) {
-                    for (int u = 0; u < U; ++u, ++g) {
-                        const int buf = (int)(g & 1);
-                        TC_T0();
-                        if (g >= 2 && !ptx::mbar_wait(t_empty + buf, (uint32_t)(((g >> 1) - 1) & 1))) {
-                            fail(8u);
-                            ok = false;
-                            break;
-                        }
-                        TC_T(12);
-                        if (LARGE && BST > 0 && !ptx::mbar_wait(bs_full + bst, bpar)) {
-                            fail(8192u);
-                            ok = false;
-                            break;
-                        }
-                        TC_T(13);
-                        ptx::tc_fence_after();
-                        const uint32_t dt = tbase + (uint32_t)(buf * TN);
-                        const uint32_t bu = (LARGE && BST > 0) ? b_addr + (uint32_t)bst * b_stride
-                                                               : b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
+                for (int uu = 0; uu < SWEEPS * U; ++uu, ++g) {
+                    const int u = uu >= U ? uu - U : uu;
+                    const int buf = (int)(g & 1);
+                    TC_T0();
+                    if (g >= 2 && !ptx::mbar_wait(t_empty + buf, (uint32_t)(((g >> 1) - 1) & 1), lim)) {
+                        fail(8u);
+                        ok = false;
+                        break;
+                    }
+                    TC_T(12);
+                    if (BST > 0 && !ptx::mbar_wait(bs_full + bst, bpar, lim)) {
+                        fail(8192u);
+                        ok = false;
+                        break;
+                    }
+                    TC_T(13);
+                    ptx::tc_fence_after();
+                    const uint32_t dt = tbase + (uint32_t)(buf * TN);
+                    const uint32_t bu = BST > 0 ? b_addr + (uint32_t)bst * b_stride
+                                                : b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
 #pragma unroll
-                        for (int ks = 0; ks < k_steps(DT); ++ks) {
-                            int ka, kb;
-                            k_step_cols(DT, ks, ka, kb);
-                            const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
-                            const uint64_t bd = ptx::smem_desc(bu + (uint32_t)(kb / 8) * 128u, 128, sbo);
-                            ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
-                        }
-                        ptx::mma_commit(t_full + buf);
-                        if (LARGE && BST > 0) {
-                            ptx::mma_commit(bs_empty + bst);   // the stage is free once these MMAs have completed
-                            if (++bst == BST) {
-                                bst = 0;
-                                bpar ^= 1u;
-                            }
+                    for (int ks = 0; ks < k_steps(DT); ++ks) {
+                        int ka, kb;
+                        k_step_cols(DT, ks, ka, kb);
+                        const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
+                        const uint64_t bd = ptx::smem_desc(bu + (uint32_t)(kb / 8) * 128u, 128, sbo);
+                        ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
+                    }
+                    ptx::mma_commit(t_full + buf);
+                    if (BST > 0) {
+                        ptx::mma_commit(bs_empty + bst);   // the stage is free once these MMAs have completed
+                        if (++bst == BST) {
+                            bst = 0;
+                            bpar ^= 1u;
                         }
                     }
                 }
@@ -646,18 +759,21 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             if (!ptx::mbar_wait(drain, 0)) fail(256u);
         }
     } else if (warp < SWEEP_WARPS) {
-        // ------------------------------ converter + sweeps (warps 0..7) ---------------------------------------------
+        // ------------------------------ converter + sweep (warps 0..7) ----------------------------------------------
         // warp e: TMEM lane quarter q = e & 3 (rows 32q..32q+31), column half h = e >> 2 (128 of each 256 columns)
         const int q = warp & 3, h = warp >> 2;
         const int row = q * 32 + lane;
         const uint32_t lane_base = (uint32_t)(q * 32) << 16;
 
         // centred, scaled split-FP16 A row of `row`: this thread writes the 16-byte chunks kc = h, h + 2, ... of
-        // kpad / 8; returns |x'|^2 (infinite when a coordinate is not finite or outside the FP16 split's range)
-        auto convert = [&](int64_t it, float& xn_out) -> bool {
+        // kpad / 8; returns |x'|^2 (infinite when a coordinate is not finite or outside the FP16 split's range) and
+        // the row's seed bound (+inf when there is none)
+        auto convert = [&](int64_t it, float& xn_out, float& seed_out) -> bool {
             const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
-            if (it >= 2 && !ptx::mbar_wait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
-            if (!ptx::mbar_wait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
+            const int64_t grow = (blockIdx.x + it * gridDim.x) * TM + row;
+            seed_out = (P.seed && grow < a.n) ? __ldg(P.seed + grow) : INFINITY;   // used one row tile later
+            if (it >= 2 && !wwait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
+            if (!wwait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
             const float4* xs4 = (const float4*)(smem + P.off_x + s3 * P.x_stride) + row * (DT / 4);
             const float scale = sCenter[DT];
             float xp[DT];
@@ -741,138 +857,160 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             process(3, rb);
         };
 
-        int64_t gcons = 0;   // TMEM tiles consumed
-        float xn_next = 0.0f;
-        bool ok = n_my > 0 ? convert(0, xn_next) : true;
-        for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
-            const float xn = xn_next;
-            const int cb = (int)(it & 1);
-            TC_T0();
-            if (it + 1 < n_my && !(ok = convert(it + 1, xn_next))) break;
-            TC_T(4);
-            bool flagged = !(xn < HUGE_S);
+        // the chunk's minimum; for ERR it also folds the chunk's four 8-unit group minima into the running two
+        // smallest (a1, a2), else the minimum into a1
+        auto chunk_min = [&](const uint32_t (&r)[32], float& a1, float& a2) -> float {
+            if constexpr (ERR) {
+                const float g0 = min8(r, 0), g1 = min8(r, 8), g2 = min8(r, 16), g3 = min8(r, 24);
+                const float l01 = fminf(g0, g1), h01 = fmaxf(g0, g1), l23 = fminf(g2, g3), h23 = fmaxf(g2, g3);
+                const float c1 = fminf(l01, l23), c2 = fmin3(fmaxf(l01, l23), h01, h23);   // the chunk's two smallest
+                a2 = fmin3(a2, c2, fmaxf(a1, c1));
+                a1 = fminf(a1, c1);
+                return c1;
+            } else {
+                const float c = fminf(min16<0>(r), min16<16>(r));
+                a1 = fminf(a1, c);
+                return c;
+            }
+        };
 
-            // ---- sweep 1: smallest (and second-smallest 8-unit group minimum of) s~ over this warp's columns -----
-            float a1 = INFINITY, a2 = INFINITY, b1 = INFINITY, b2 = INFINITY;
-            for (int u = 0; u < U && ok; ++u, ++gcons) {
-                const int buf = (int)(gcons & 1);
-                if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
-                TC_T(0);
-                ptx::tc_fence_after();
-                // ERR on maps of at most 8 column tiles (resolver-bound): groups of 4 columns, alternately feeding
-                // (a1, a2) and (b1, b2), so that the second-smallest group minimum stays close to the second-smallest
-                // value (fewer candidates for the resolvers). Otherwise groups of 8 (fewer sweep instructions): chunks
-                // 0 and 2 feed (a1, a2), chunks 1 and 3 feed (b1, b2).
-                stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
-                    if constexpr (ERR && !LARGE) {
-#pragma unroll
-                        for (int g4 = 0; g4 < 32; g4 += 4) {
-                            const float g = fminf(fmin3(__uint_as_float(r[g4]), __uint_as_float(r[g4 + 1]),
-                                                        __uint_as_float(r[g4 + 2])),
-                                                  __uint_as_float(r[g4 + 3]));
-                            if ((g4 >> 2) & 1) {
-                                b2 = fminf(b2, fmaxf(b1, g));
-                                b1 = fminf(b1, g);
-                            } else {
-                                a2 = fminf(a2, fmaxf(a1, g));
-                                a1 = fminf(a1, g);
+        int64_t gcons = 0;   // TMEM tiles consumed
+        float xn_next = 0.0f, seed_next = INFINITY;
+        bool ok = n_my > 0 ? convert(0, xn_next, seed_next) : true;
+        for (int64_t it = 0; ok && it < n_my && !waborted(); ++it) {
+            const float xn = xn_next, seedub = seed_next;
+            const int lb = (int)(it & 1);
+            TC_T0();
+            if (it + 1 < n_my && !(ok = convert(it + 1, xn_next, seed_next))) break;
+            TC_T(4);
+            // the resolvers are done with buffer lb (row tile it - 2): its lists, and in the two-sweep form the half
+            // exchange below, may be rewritten
+            if (it >= 2 && !wwait(m_empty + lb, (uint32_t)(((it >> 1) - 1) & 1))) { fail(512u); break; }
+            TC_T(5);
+            const bool flagged = !(xn < HUGE_S);
+            const float axg = fmaf(P.alpha, xn, GAMMA);
+            RowSweep rs;
+            rs.a1 = INFINITY;
+            rs.a2 = INFINITY;
+            rs.thr = flagged ? -INFINITY : thr_of(seedub, xn, axg, P.beta, P.kthr);
+            rs.cnt = 0;
+            rs.ovf = false;
+            if constexpr (TWO) {
+                // ---- sweep 1: the row's bounds over this half's columns ----------------------------------------
+                for (int u = 0; u < U && ok; ++u, ++gcons) {
+                    const int buf = (int)(gcons & 1);
+                    if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
+                    TC_T(0);
+                    ptx::tc_fence_after();
+                    stream_tile(buf, [&](int, const uint32_t (&r)[32]) { chunk_min(r, rs.a1, rs.a2); });
+                    TC_T(1);
+                }
+                if (!ok) break;
+                // both halves' bounds: the row's final threshold
+                sPart[(lb * HALVES + h) * TM + row] = make_float2(rs.a1, rs.a2);
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
+                if (!wwait(p_full + lb * 4 + q, (uint32_t)((it >> 1) & 1))) { fail(2048u); break; }
+                const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
+                const float M1 = fminf(p0.x, p1.x);
+                const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
+                rs.thr = fminf(rs.thr, thr_of(ERR ? M2 : M1, xn, axg, P.beta, P.kthr));
+            }
+            const size_t lbase = (size_t)((lb * HALVES + h) * CAP) * TM + row;
+            uint32_t* lw = sLw + lbase;
+            float* lm = sLm + lbase;
+            uint8_t* lc = sLc + lbase;
+            float thr_up = nextafterf(rs.thr, INFINITY);
+            // A chunk's candidate mask word, built only when a row of the warp can have a candidate there: first
+            // against the threshold known before the chunk (so that it does not wait for the chunk's own minimum), and
+            // again against `t`, the threshold that takes the chunk in, where that fell by more than `slack` (a loose
+            // or missing seed: the chunk holds a new minimum far under the old threshold).
+            const float slack = 2.0f * P.kthr * axg;
+            auto candidates = [&](int u, int c, const uint32_t (&r)[32], float cm, float t) {
+                if (__any_sync(0xffffffffu, cm <= rs.thr)) {
+                    uint32_t mw = sign_mask32(r, thr_up);
+                    if (__any_sync(0xffffffffu, mw != 0u && t < rs.thr - slack))
+                        mw = sign_mask32(r, nextafterf(t, INFINITY));
+                    if (mw != 0u) {
+                        if (rs.cnt == CAP) {   // full: drop the entries a lower threshold has ruled out
+                            int k = 0;
+                            for (int e = 0; e < CAP; ++e) {
+                                const float cme = lm[e * TM];
+                                if (cme <= t) {
+                                    if (k != e) {
+                                        lw[k * TM] = lw[e * TM];
+                                        lm[k * TM] = cme;
+                                        lc[k * TM] = lc[e * TM];
+                                    }
+                                    ++k;
+                                }
                             }
+                            rs.cnt = k;
                         }
-                    } else {
-#pragma unroll
-                        for (int g8 = 0; g8 < 32; g8 += 8) {
-                            const float g = fmin3(fmin3(__uint_as_float(r[g8]), __uint_as_float(r[g8 + 1]),
-                                                        __uint_as_float(r[g8 + 2])),
-                                                  fmin3(__uint_as_float(r[g8 + 3]), __uint_as_float(r[g8 + 4]),
-                                                        __uint_as_float(r[g8 + 5])),
-                                                  fminf(__uint_as_float(r[g8 + 6]), __uint_as_float(r[g8 + 7])));
-                            if (c & 1) {
-                                if (ERR) b2 = fminf(b2, fmaxf(b1, g));
-                                b1 = fminf(b1, g);
-                            } else {
-                                if (ERR) a2 = fminf(a2, fmaxf(a1, g));
-                                a1 = fminf(a1, g);
-                            }
+                        if (rs.cnt < CAP) {
+                            lw[rs.cnt * TM] = mw;
+                            lm[rs.cnt * TM] = cm;
+                            lc[rs.cnt * TM] = (uint8_t)(u * 4 + c);
+                            ++rs.cnt;
+                        } else {
+                            rs.ovf = true;
                         }
                     }
-                });
+                }
+            };
+            for (int u = 0; u < U && ok; ++u, ++gcons) {
+                const int buf = (int)(gcons & 1);
+                if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
+                TC_T(0);
+                ptx::tc_fence_after();
+                if constexpr (TWO) {
+                    // ---- sweep 2: candidate lists against the final threshold -----------------------------------
+                    stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                        candidates(u, c, r, fminf(min16<0>(r), min16<16>(r)), rs.thr);
+                    });
+                } else {
+                    // ---- the one sweep: lists against the running threshold, which then takes the chunk in ------
+                    stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                        const float cm = chunk_min(r, rs.a1, rs.a2);
+                        const float t = fminf(rs.thr, thr_of(ERR ? rs.a2 : rs.a1, xn, axg, P.beta, P.kthr));
+                        candidates(u, c, r, cm, t);
+                        if (t < rs.thr) {
+                            rs.thr = t;
+                            thr_up = nextafterf(t, INFINITY);
+                        }
+                    });
+                }
                 TC_T(1);
             }
             if (!ok) break;
-            sPart[h * TM + row] =
-                make_float2(fminf(a1, b1), fminf(fmaxf(a1, b1), fminf(a2, b2)));
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(p_full + cb * 4 + q);
-            if (!ptx::mbar_wait(p_full + cb * 4 + q, (uint32_t)((it >> 1) & 1))) { fail(2048u); break; }
-            float M1 = INFINITY, M2 = INFINITY;
-#pragma unroll
-            for (int t = 0; t < HALVES; ++t) {
-                const float2 p = sPart[t * TM + row];
-                M2 = fminf(fminf(M2, p.y), fmaxf(M1, p.x));
-                M1 = fminf(M1, p.x);
+            if constexpr (!TWO) sPart[(lb * HALVES + h) * TM + row] = make_float2(rs.a1, rs.a2);
+            sCnt[(lb * HALVES + h) * TM + row] = (uint8_t)(rs.cnt | (rs.ovf ? 0x80 : 0));
+            if (h == 0) {
+                sRow[lb * TM + row] = make_float2(xn, seedub);
+                sFlag[lb * TM + row] = flagged ? 1 : 0;
             }
-            // ERR: M2 is the second smallest 4- or 8-unit group minimum, an upper bound of the second smallest s~ (two
-            // groups have a unit at or below it), so the threshold derived from it keeps every possible second BMU
-            const float mref = ERR ? M2 : M1;
-            if (!(M1 + xn < HUGE_S) || !(mref < HUGE_S)) flagged = true;
-            const float dref = fmaxf(0.0f, mref + xn);
-            const float thr =
-                flagged ? -INFINITY : mref + 2.0f * (P.alpha * xn + P.beta * dref + GAMMA) / (1.0f - P.beta) + GAMMA;
-            // the resolvers have taken the candidate masks of the previous row tile
-            if (it >= 1 && !ptx::mbar_wait(m_empty, (uint32_t)((it - 1) & 1))) { fail(512u); break; }
-            TC_T(5);
-
-            // ---- sweep 2: mask of this warp's columns at or under the threshold -------------------------------------
-            // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
-            // floats never rounds to zero), so each value costs one subtraction and one shift-or of its sign bit.
-            const float thr_up = nextafterf(thr, INFINITY);
-            uint32_t summary = 0, summary_hi = 0;   // column tiles 0-7 and 8-15
-            for (int u = 0; u < U && ok; ++u, ++gcons) {
-                const int buf = (int)(gcons & 1);
-                if (!ptx::mbar_wait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
-                TC_T(2);
-                ptx::tc_fence_after();
-                uint32_t* mrow = sMask + (size_t)((h * U + u) * 4) * TM + row;
-                stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
-                    const uint32_t mw = sign_mask32(r, thr_up);
-                    mrow[c * TM] = mw;
-                    if (LARGE) {
-                        const uint32_t bit = (mw != 0u ? 1u : 0u) << ((u & 7) * 4 + c);
-                        if (u < 8) summary |= bit;
-                        else summary_hi |= bit;
-                    } else {
-                        summary |= (mw != 0u ? 1u : 0u) << (u * 4 + c);
-                    }
-                });
-                TC_T(3);
-            }
-            if (!ok) break;
-            sSum[h * TM + row] = flagged ? 0u : summary;
-            if (LARGE && U > 8) sSum[(HALVES + h) * TM + row] = flagged ? 0u : summary_hi;
-            if (h == 0) sFlag[row] = flagged ? 1 : 0;
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(m_full);
+            if (lane == 0) ptx::mbar_arrive(m_full + lb);
         }
     } else if (warp < SWEEP_WARPS + RES_WARPS) {
-        // ------------------------------ resolvers (warps 8..11): row tile it while the sweeps run it + 1 -------------
-        // thread r of resolver warp q owns row 32q + r: float32 distances of its candidates, the decision, the outputs
-        const int q = warp - SWEEP_WARPS;
+        // ------------------------------ resolvers (warps 8..15): group g takes the row tiles it with it % 2 == g ------
+        // (list buffer g) while the sweeps run the next ones; thread r of the group's warp q owns row 32q + r: float32
+        // distances of its candidates, the decision, the outputs
+        const int grp = (warp - SWEEP_WARPS) / RES_GROUP, q = (warp - SWEEP_WARPS) % RES_GROUP;
         const int row = q * 32 + lane;
         const float g32 = (float)(d + 2) * 5.9604645e-8f;
         const float fac = 1.0f + 8.0f * g32;
         DFAcc e0, e1, e2;
-        uint32_t* pw = sWords + row;
-        uint16_t* pt = sWtop + row;
         const float* wrows = P.off_w ? (const float*)(smem + P.off_w) : a.w;   // unit rows: shared memory or L2
-        for (int64_t it = 0; it < n_my && !*abort_v; ++it) {
+        for (int64_t it = grp; it < n_my && !waborted(); it += 2) {
+            const int lb = grp;
             TC_T0();
-            if (!ptx::mbar_wait(m_full, (uint32_t)(it & 1))) { fail(1024u); break; }
+            if (!wwait(m_full + lb, (uint32_t)((it >> 1) & 1))) { fail(1024u); break; }
             TC_T(6);
             const int64_t grow = (blockIdx.x + it * gridDim.x) * TM + row;
             const bool live = grow < a.n;
             const double rho_v = (live && a.rho) ? __ldg(a.rho + grow) : 1.0;   // issued early, used at the end
-            // the sample row from global memory (just read by the tile load, so in L2): the shared-memory stage is
-            // released by the converters, which decouples the resolvers from the sample-tile ring
+            // the sample row from global memory (just read by the tile load, so in L2)
             const float* xg = a.x + (live ? grow : 0) * DT;
             float xr[DT];   // loads issued before the candidate extraction, whose latency they overlap
 #pragma unroll
@@ -880,41 +1018,31 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const float4 t = __ldg((const float4*)xg + k4);
                 xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
             }
-            // The row's non-zero candidate-mask words (from the summary bits) are first copied to the resolver's own
-            // buffer, which hands the masks back to the sweeps early. A warp with a row of more than KW such words
-            // (early epochs of large maps) keeps the masks until its rows are decided and reads every row's
-            // candidates from them.
-            const bool flagged = sFlag[row] != 0;
-            int nw = 0;
-            // column tiles 0-7, then (for more than 8) 8-15: each part's two halves fit one 64-bit word
-            const int parts = LARGE ? (U + 7) / 8 : 1;
-            for (int part = 0; part < parts; ++part) {
-                const uint32_t* ss = sSum + part * HALVES * TM;
-                uint64_t S = (flagged || !live) ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
-                while (__any_sync(0xffffffffu, S != 0ull)) {
-                    const int b = __ffsll((long long)S) - 1;
-                    const int bb = b < 0 ? 0 : b;
-                    const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
-                    const uint32_t word = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
-                    if (b >= 0) {
-                        if (nw < KW) {
-                            pw[nw * TM] = word;
-                            pt[nw * TM] = (uint16_t)(ub * TN + hh * 128 + wb * 32 + 31);
-                        }
-                        ++nw;
-                        S &= S - 1ull;
-                    }
-                }
-            }
-            const bool ovf = live && !flagged && nw > KW;
-            const bool any_ovf = __any_sync(0xffffffffu, ovf);
-            if (!any_ovf) {
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(m_empty);
-            }
-            // Then the candidates, one per lane and iteration (the next copied word fetched in the same iteration),
-            // each one's float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found.
-            // A row with more than CAPR candidates stops there and goes to the exact recheck.
+            // the row's final threshold from both halves' bounds and its seed
+            const float2 rw = sRow[lb * TM + row];
+            const float xn = rw.x;
+            const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
+            const float M1 = fminf(p0.x, p1.x);
+            const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
+            const float mref = fminf(ERR ? M2 : M1, rw.y);
+            const bool flagged = sFlag[lb * TM + row] != 0 || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
+            const float thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
+            const uint8_t c0 = sCnt[(lb * HALVES + 0) * TM + row], c1 = sCnt[(lb * HALVES + 1) * TM + row];
+            const bool ovf = ((c0 | c1) & 0x80) != 0;
+            const int n0 = c0 & 0x7f, nwc = n0 + (c1 & 0x7f);
+            // list entry wi of the row (half 0's entries, then half 1's): its index in the list arrays
+            auto entry = [&](int wi) -> size_t {
+                const int hh = wi >= n0 ? 1 : 0;
+                return (size_t)((lb * HALVES + hh) * CAP + (wi - hh * n0)) * TM + row;
+            };
+            auto entry_top = [&](int wi, size_t ix) -> int {   // the unit of bit 0 of the entry's word
+                const int ch = sLc[ix];
+                return (ch >> 2) * TN + (wi >= n0 ? 128 : 0) + (ch & 3) * 32 + 31;
+            };
+            // The candidates, one per lane and iteration (the next entry fetched in the same iteration), each one's
+            // float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found. Entries
+            // whose chunk minimum is above the final threshold hold no candidate and are skipped. A row with more than
+            // CAPR candidates stops there and goes to the exact recheck.
             int cnt = 0;
             float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
             int32_t j1 = -1, j2 = -1, j3 = -1;
@@ -926,44 +1054,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     else { f2 = df; j2 = j; }
                 } else { f3 = df; j3 = j; }
             };
-            if (any_ovf) {
-                // the masks are still this warp's: words from the summary bits, as in the copy above
-                for (int part = 0; part < parts; ++part) {
-                    const uint32_t* ss = sSum + part * HALVES * TM;
-                    uint64_t S = (flagged || !live) ? 0ull : ((uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32));
-                    uint32_t word = 0u;
-                    int jtop = 0;
-                    bool more = S != 0ull && cnt <= CAPR;
-                    while (__any_sync(0xffffffffu, more)) {
-                        const bool need = word == 0u;
-                        const int b = __ffsll((long long)S) - 1;
-                        const int bb = b < 0 ? 0 : b;
-                        const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
-                        const uint32_t nwd = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
-                        word = need ? (b >= 0 ? nwd : 0u) : word;
-                        jtop = need ? ub * TN + hh * 128 + wb * 32 + 31 : jtop;
-                        S = need ? (S & (S - 1ull)) : S;
-                        const int j = jtop - (__ffs(word) - 1);
-                        const bool take = more && word != 0u && j < (int)a.m;
-                        word &= word - 1u;
-                        if (take) {
-                            ++cnt;
-                            push(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr), j);
-                        }
-                        more = (word != 0u || S != 0ull) && cnt <= CAPR;
-                    }
-                }
-            } else {
-                const int nwc = nw <= KW ? nw : 0;
+            {
                 int wi = 0, jtop = 0;
                 uint32_t word = 0u;
-                bool more = nwc > 0;
+                bool more = live && !flagged && !ovf && nwc > 0;
                 while (__any_sync(0xffffffffu, more)) {
                     const bool need = word == 0u;
-                    const uint32_t nwd = pw[(wi < KW ? wi : KW - 1) * TM];
-                    const int ntop = pt[(wi < KW ? wi : KW - 1) * TM];
-                    word = need ? (wi < nwc ? nwd : 0u) : word;
-                    jtop = need ? ntop : jtop;
+                    if (need && wi < nwc) {
+                        const size_t ix = entry(wi);
+                        word = sLm[ix] <= thr ? sLw[ix] : 0u;
+                        jtop = entry_top(wi, ix);
+                    }
                     wi += need ? 1 : 0;
                     const int j = jtop - (__ffs(word) - 1);
                     const bool take = more && word != 0u && j < (int)a.m;
@@ -972,34 +1073,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         ++cnt;
                         push(cand_dist32v<DT>(wrows + (int64_t)j * DT, xr), j);
                     }
-                    more = (word != 0u || wi < nwc) && cnt <= CAPR;
+                    more = more && (word != 0u || wi < nwc) && cnt <= CAPR;
                 }
             }
-            // every candidate of the row again (the rare slower paths): from the copied words, or from the masks
-            // (still held) for a warp with an overflowing row
+            // every candidate of the row again (the rare slower paths)
             auto for_each_cand = [&](auto&& f) {
-                if (any_ovf) {
-                    for (int part = 0; part < parts; ++part) {
-                        const uint32_t* ss = sSum + part * HALVES * TM;
-                        uint64_t S = (uint64_t)ss[row] | ((uint64_t)ss[TM + row] << 32);
-                        while (S) {
-                            const int bb = __ffsll((long long)S) - 1;
-                            S &= S - 1ull;
-                            const int hh = bb >> 5, ub = part * 8 + ((bb & 31) >> 2), wb = bb & 3;
-                            uint32_t word = sMask[(size_t)((hh * U + ub) * 4 + wb) * TM + row];
-                            const int jt = ub * TN + hh * 128 + wb * 32 + 31;
-                            while (word) {
-                                const int j = jt - (__ffs(word) - 1);
-                                word &= word - 1u;
-                                if (j < (int)a.m) f(j);
-                            }
-                        }
-                    }
-                    return;
-                }
-                for (int w = 0; w < nw; ++w) {
-                    uint32_t word = pw[w * TM];
-                    const int jt = pt[w * TM];
+                for (int wi = 0; wi < nwc; ++wi) {
+                    const size_t ix = entry(wi);
+                    if (!(sLm[ix] <= thr)) continue;
+                    uint32_t word = sLw[ix];
+                    const int jt = entry_top(wi, ix);
                     while (word) {
                         const int j = jt - (__ffs(word) - 1);
                         word &= word - 1u;
@@ -1008,7 +1091,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 }
             };
             TC_T(9);
-            const bool recheck = live && (flagged || cnt == 0 || cnt > CAPR);
+            const bool recheck = live && (flagged || ovf || cnt == 0 || cnt > CAPR);
+            int32_t r1 = -1, r2 = -1;
             if (recheck) {
                 const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                 P.rows[slotq] = (int32_t)grow;
@@ -1024,7 +1108,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const bool gap12 = j2 < 0 || !(f2 <= c1lim);
                 const bool separated = ERR ? (gap12 && (j3 < 0 || !(f3 <= c2lim))) : gap12;
                 const float climit = ERR ? c2lim : c1lim;
-                int32_t r1, r2;
                 float2 tr1 = make_float2(0.0f, 0.0f), tr2 = tr1;
                 DFloat rd1{0.0f, 0.0f};
                 if (separated) {
@@ -1080,10 +1163,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 TC_T(10);
                 emit_sample32(a, grow, rho_v, r1, r2, rd1, tr1, tr2, e0, e1, e2);
             }
-            if (any_ovf) {   // the warp's rows are decided: the masks go back to the sweeps
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(m_empty);
-            }
+            // the row's best two units for the next pass's seeds (for BMU-only passes the second is the float32
+            // runner-up among the candidates: any unit gives a valid seed); rechecked rows are written by the recheck
+            if (a.pairs && live && !recheck) ((int2*)a.pairs)[grow] = make_int2(r1, ERR ? r2 : (j2 == r1 ? j1 : j2));
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(m_empty + lb);   // the sweeps may refill list buffer lb
             TC_T(7);
         }
         if (ERR) {
@@ -1105,7 +1189,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         for (int ph = 0; ph < TC_PHASES; ++ph) atomicAdd(&g_tc_phase_cycles[ph], _tc_acc[ph]);
 #endif
 
-    // teardown: the MMA thread has drained its MMAs and, after an abort, the producer its copies (both bounded)
+    // teardown: the MMA thread has drained its MMAs and, after an abort, the producer its copies
     ptx::tc_fence_before();
     __syncthreads();
     if (warp == MMA_WARP) {
@@ -1116,7 +1200,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
 template <bool ERR, int DT>
 int launch_main(const CUtensorMap& tmap, const TcArgs& P, unsigned grid, size_t smem, cudaStream_t stream) {
-    auto kern = (P.bstages > 0 || P.utiles > 8) ? tc_pass_kernel<ERR, DT, true> : tc_pass_kernel<ERR, DT, false>;
+    auto kern = P.seed ? tc_pass_kernel<ERR, DT, false> : tc_pass_kernel<ERR, DT, true>;
     SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     timer_begin(stream);
     kern<<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
@@ -1160,11 +1244,16 @@ size_t max_smem_optin() {
     return (size_t)v;
 }
 
+// Test hook (somgb_debug_tc_withhold): the next tensor-core pass on this thread withholds one row tile's samples and
+// bounds its protocol waits by `limit` polls; one-shot.
+thread_local int64_t t_withhold_tile = -1;
+thread_local uint32_t t_wait_limit = 0;
+
 }  // namespace
 
 bool tc_shape_ok(int64_t m, int d) {
     if (d != 4 && d != 8 && d != 16 && d != 32) return false;
-    if (m <= 0 || m > (int64_t)MAX_U * TN) return false;   // the per-half candidate summary covers MAX_U column tiles
+    if (m <= 0 || m > (int64_t)MAX_U * TN) return false;   // a list entry names its chunk in a byte
     return tc_shape(m, d).smem <= SMEM_LIMIT;
 }
 
@@ -1175,7 +1264,8 @@ bool tc_device_ok(int64_t m, int d) {
 bool tc_supported(int64_t n, int64_t m, int d, int algo) {
     if (algo == SOMGB_ALGO_FP32) return false;
     if (!tc_shape_ok(m, d)) return false;
-    if (algo == SOMGB_ALGO_AUTO && n * m < ((int64_t)1 << 22)) return false;   // small passes: K0 has no prep cost
+    // AUTO: small passes (no prep cost on CUDA cores) and maps of fewer than 32 units stay on K0
+    if (algo == SOMGB_ALGO_AUTO && (n * m < ((int64_t)1 << 22) || m < 32)) return false;
     return device_is_sm103() && encode_fn() != nullptr && max_smem_optin() >= tc_shape(m, d).smem;
 }
 
@@ -1204,14 +1294,26 @@ int read_device_status(unsigned int* status, bool clear, cudaStream_t stream) {
     return SOMGB_OK;
 }
 
+void tc_debug_withhold(int64_t row_tile, uint32_t wait_limit) {
+    t_withhold_tile = row_tile;
+    t_wait_limit = wait_limit;
+}
+
 size_t tc_workspace_bytes(int64_t n, int64_t m, int d) { return tc_ws_layout(n, m, d, nullptr, nullptr); }
 
 int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t stream) {
-    if (((uintptr_t)a.x) % 16 || ((uintptr_t)a.w) % 16 || ((a.outs & OUT_ERR) && ((uintptr_t)a.topo) % 8))
-        return set_error(SOMGB_ERR_INVALID, "tensor-core pass needs 16-byte aligned x and w, 8-byte aligned topo");
+    if (((uintptr_t)a.x) % 16 || ((uintptr_t)a.w) % 16 || ((a.outs & OUT_ERR) && ((uintptr_t)a.topo) % 8) ||
+        ((uintptr_t)a.pairs) % 8)
+        return set_error(SOMGB_ERR_INVALID,
+                         "tensor-core pass needs 16-byte aligned x and w, 8-byte aligned topo and pairs");
     const TcShape s = tc_shape(a.m, a.d);
     TcWs W;
     if (tc_ws_layout(a.n, a.m, a.d, &W, ws) > ws_bytes) return set_error(SOMGB_ERR_WORKSPACE, "tc workspace too small");
+    const bool err = (a.outs & OUT_ERR) != 0;
+
+    TcArgs P{};
+    tc_error_coefficients(a.d, &P.alpha, &P.beta);
+    P.kthr = nextafterf((float)(2.0 / (1.0 - (double)P.beta)), INFINITY);
 
     // unit operand
     tc_center_kernel<<<1, CENTER_THREADS, 0, stream>>>(a.w, a.m, a.d, W.center);
@@ -1219,6 +1321,18 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     tc_prep_b_kernel<<<(unsigned)ceil_div(s.mpad, 128), 128, 0, stream>>>(a.w, a.m, a.d, s.kpad, s.mpad, W.center,
                                                                           W.b);
     SOMGB_LAUNCH_CHECK();
+    // seed bounds from the rows' best units under an earlier map
+    const bool seeded = a.pairs && a.pairs_in;
+    if (seeded) {
+        const unsigned g = (unsigned)ceil_div(a.n, 256);
+        switch (a.d) {
+            case 4: tc_seed_kernel<4><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
+            case 8: tc_seed_kernel<8><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
+            case 16: tc_seed_kernel<16><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
+            default: tc_seed_kernel<32><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
+        }
+        SOMGB_LAUNCH_CHECK();
+    }
 
     // sample tensor map: rows of d float32, boxes of 128 rows
     CUtensorMap tmap;
@@ -1231,22 +1345,23 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) return set_error(SOMGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
-    TcArgs P{};
     P.a = a;
     P.b = W.b;
     P.center = W.center;
     P.rows = W.rows;
     P.row_count = a.recheck_count;
+    P.seed = seeded ? W.seed : nullptr;   // without seeds: the two-sweep form
     P.kpad = s.kpad;
     P.utiles = s.utiles;
-    tc_error_coefficients(a.d, &P.alpha, &P.beta);
     P.off_a = s.off_a;
     P.off_x = s.off_x;
-    P.off_mask = s.off_mask;
-    P.off_sum = s.off_sum;
-    P.off_flag = s.off_flag;
-    P.off_rlist = s.off_rlist;
+    P.off_lw = s.off_lw;
+    P.off_lm = s.off_lm;
     P.off_part = s.off_part;
+    P.off_row = s.off_row;
+    P.off_lc = s.off_lc;
+    P.off_cnt = s.off_cnt;
+    P.off_flag = s.off_flag;
     P.off_w = s.off_w;
     P.off_center = s.off_center;
     P.off_bar = s.off_bar;
@@ -1255,13 +1370,17 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     P.b_bytes = (uint32_t)s.b_bytes;
     P.b_tile = (uint32_t)s.b_tile;
     P.bstages = s.bstages;
+    P.wait_limit = t_wait_limit ? t_wait_limit : WAIT_LIMIT;
+    P.withhold_tile = t_withhold_tile;
+    t_withhold_tile = -1;
+    t_wait_limit = 0;
 
     const int64_t tiles = ceil_div(a.n, TM);
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());
     // at least half of an SM's shared memory, so that one CTA (the sole TMEM owner) runs per SM
     const size_t smem = std::max<size_t>(s.smem, 120 * 1024);
     int st = SOMGB_OK;
-    if (a.outs & OUT_ERR) {
+    if (err) {
         switch (a.d) {
             case 4: st = launch_main<true, 4>(tmap, P, grid, smem, stream); break;
             case 8: st = launch_main<true, 8>(tmap, P, grid, smem, stream); break;
@@ -1280,7 +1399,7 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     }
     if (st) return st;
     // rows the tensor-core pass could not decide: the exact CUDA-core pass over the listed rows (it must not count
-    // into the list length it reads)
+    // into the list length it reads; it writes those rows' pairs)
     PassArgs b = a;
     b.recheck_count = nullptr;
     return launch_k0_pass(b, stream, W.rows, a.recheck_count);

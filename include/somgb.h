@@ -44,8 +44,8 @@ typedef struct CUstream_st* somgb_stream_t; /* == cudaStream_t; NULL = legacy de
 /* distance-search algorithms */
 #define SOMGB_ALGO_FP32 0       /* CUDA cores: float32 direct differences, margin-gated float64 recheck */
 #define SOMGB_ALGO_TC 1         /* tcgen05 split-FP16 distance GEMM, margin-gated recheck (D in {4, 8, 16, 32},
-                                   M <= 4096; somgb_algo_supported tells) */
-#define SOMGB_ALGO_AUTO 2       /* TC where its shape limits allow and N*M >= 2^22, FP32 otherwise */
+                                   M <= 16384; somgb_algo_supported tells) */
+#define SOMGB_ALGO_AUTO 2       /* TC where its shape limits allow, N*M >= 2^22 and M >= 32; FP32 otherwise */
 
 /* workspace query operations */
 #define SOMGB_OP_FIND_BMUS 0
@@ -70,6 +70,21 @@ int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream);
  * incomplete. Sticky until read with clear != 0.
  */
 int somgb_device_status(unsigned int* status, int clear, somgb_stream_t stream);
+
+/*
+ * The status word of the last pass that used workspace `ws` (synchronises `stream`): non-zero when a bounded
+ * device-side wait of that pass gave up (its outputs are then incomplete). Each pass clears its workspace's word when
+ * it starts, so concurrent calls with their own workspaces each see their own failures. clear != 0 zeroes it.
+ */
+int somgb_workspace_status(const void* ws, unsigned int* status, int clear, somgb_stream_t stream);
+
+/*
+ * Test hook for the bounded waits: the next tensor-core pass on the calling thread never loads the samples of its
+ * row tile `row_tile` and bounds its waits by `wait_limit` polls (about 1 us each), so that the wait for those samples
+ * runs out: that pass returns early with its status word and the device status word set, and the rows it did not
+ * decide keep whatever the outputs held. One-shot; no product call sets it.
+ */
+int somgb_debug_tc_withhold(int64_t row_tile, unsigned int wait_limit);
 
 /* 1 if `algo` can run a pass of these sizes on the current device, else 0. */
 int somgb_algo_supported(int algo, int64_t n, int64_t m, int d);
@@ -158,6 +173,22 @@ int somgb_train_epoch_pass_f64(const double* x, const double* rho, int64_t n, in
 int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
                          int64_t m, double penalty, int algo, int32_t* bmu_out, double* err3, void* ws,
                          size_t ws_bytes, somgb_stream_t stream);
+/*
+ * somgb_train_bmu_pass with seeds: the same outputs (bmu_out and err3 as there; either may be NULL, not both), and
+ * `pairs` (n x 2 int32, 8-byte aligned): on output each row's best two units under `w` (-1 where the pass did not rank
+ * them; the plain FP32 form leaves pairs unchanged); on input, when pairs_in != 0, the same under an earlier map (-1
+ * when unknown), else ignored (the first pass of a training). A row's two units under the previous epoch's map bound
+ * its best distances under this one from above, which lets the tensor-core pass build its candidate lists in one
+ * sweep instead of two; any unit gives a valid bound, so results never depend on the pairs' contents, only the time
+ * does. Replaces the BMU half of _train_step1_epoch_kernel/_train_step2_xpu (algo/som_batch.py:94-150, 509-540),
+ * whose training loop re-runs the search every epoch on the previous epoch's update of the same map
+ * (som_batch.py:285-363), and its compute_errors pass (som_batch.py:363) when bmu_out is NULL. Workspace:
+ * SOMGB_OP_FIND_BMUS sizing.
+ */
+int somgb_train_bmu_pass_seeded(const float* x, const double* rho, int64_t n, int d, const float* w,
+                                const float* topo, int64_t m, double penalty, int algo, int32_t* bmu_out,
+                                double* err3, int32_t* pairs, int pairs_in, void* ws, size_t ws_bytes,
+                                somgb_stream_t stream);
 int somgb_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, somgb_stream_t stream);
 int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
                      const float* bounds, double* S, double* c, somgb_stream_t stream);

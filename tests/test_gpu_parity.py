@@ -60,7 +60,7 @@ def _skip_unsupported_tc(native, algo, n, m, d, call):
 
 SHAPES = [(1, 1, 3, 50), (1, 2, 4, 300), (4, 4, 4, 25_000), (10, 10, 4, 20_000), (8, 9, 7, 5000),
           (32, 32, 16, 40_000), (16, 16, 17, 8000), (8, 16, 32, 10_000), (5, 7, 64, 3000), (4, 5, 100, 2000),
-          (64, 64, 16, 6000), (3, 3, 1, 500)]
+          (64, 64, 16, 6000), (80, 80, 32, 5000), (3, 3, 1, 500)]
 
 
 @pytest.mark.parametrize('algo', ALGOS)
@@ -415,14 +415,17 @@ TC_STRESS = [
     ('uniform', 32, 8, 16, 60_000),
     ('duplicates', 8, 10, 10, 50_000),
     # maps whose unit operand streams through shared memory (64x64 at D = 8 and 16: rings of 4 column tiles; D = 32:
-    # 2 tiles; 32x64 at D = 16: 8 streamed tiles), more than 8 column tiles with a resident operand (64x64 at D = 4),
-    # and 9 column tiles (48x48)
+    # 3 tiles), more than 8 column tiles with a resident operand (64x64 at D = 4), and 9 column tiles (48x48)
     ('large-streamed', 16, 64, 64, 30_000),
     ('large-streamed', 32, 64, 64, 20_000),
     ('large-streamed', 8, 64, 64, 30_000),
     ('large-streamed', 16, 32, 64, 30_000),
     ('large-streamed', 4, 64, 64, 30_000),
     ('large-streamed', 16, 48, 48, 30_000),
+    # more than 16 column tiles: the 80x80 grids of the mixed-training configuration (25 tiles) and 128x128 (64)
+    ('large-streamed', 16, 80, 80, 30_000),
+    ('large-streamed', 32, 80, 80, 20_000),
+    ('large-streamed', 8, 128, 128, 10_000),
 ]
 
 
