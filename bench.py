@@ -251,9 +251,6 @@ class EpochRunner:
         self.S = torch.empty((self.M, self.D), dtype=torch.float64, device=device)
         self.c = torch.empty(self.M, dtype=torch.float64, device=device)
         self.bmu = torch.empty(self.N, dtype=torch.int32, device=device)
-        # each row's best two units from the previous epoch (seeds of the tensor-core search), as SOM_Batch.train
-        # keeps them for a resident catalogue; written by the first epoch, read from the second on
-        self.pairs = torch.full((self.N, 2), -1, dtype=torch.int32, device=device)
         # per-feature bounds of the fixed-point sums: a property of the resident catalogue, computed once
         self.bounds = torch.zeros(self.D + 1, dtype=torch.float32, device=device)
         native.call('somgb_feature_bounds', xd.data_ptr(), None, self.N, self.D, self.bounds.data_ptr(),
@@ -276,9 +273,9 @@ class EpochRunner:
         self.c.zero_()
         if timer is not None:
             nat.call('somgb_set_kernel_timer', timer[0].cuda_event, timer[1].cuda_event)
-        nat.call('somgb_train_bmu_pass_seeded', self.xd.data_ptr(), None, self.N, self.D, self.wcur.data_ptr(),
+        nat.call('somgb_train_bmu_pass', self.xd.data_ptr(), None, self.N, self.D, self.wcur.data_ptr(),
                  self.topo.data_ptr(), self.M, self.penalty, self.algo, self.bmu.data_ptr(), err_slot.data_ptr(),
-                 self.pairs.data_ptr(), 1 if self.epoch > 0 else 0, self.wsp, self.wsb, s)
+                 self.wsp, self.wsb, s)
         if timer is not None:
             nat.call('somgb_set_kernel_timer', None, None)
         if phases is not None:

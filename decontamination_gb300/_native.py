@@ -45,7 +45,6 @@ SIGNATURES = {
     'somgb_device_status': [P, I32, P],
     'somgb_set_kernel_timer': [P, P],
     'somgb_train_bmu_pass': [P, P, I64, I32, P, P, I64, D, I32, P, P, P, SZ, P],
-    'somgb_train_bmu_pass_seeded': [P, P, I64, I32, P, P, I64, D, I32, P, P, P, I32, P, SZ, P],
     'somgb_workspace_status': [P, P, I32, P],
     'somgb_debug_tc_withhold': [I64, ctypes.c_uint],
     'somgb_accumulate': [P, P, P, I64, I32, I64, P, P, P, P],

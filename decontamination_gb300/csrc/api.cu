@@ -142,7 +142,6 @@ int run_pass(PassArgs a, int algo, const Workspace& ws, bool tc, cudaStream_t st
     if (algo == SOMGB_ALGO_TC)
         return set_error(SOMGB_ERR_UNSUPPORTED, "tensor-core path unsupported for n=%lld m=%lld d=%d on this device",
                          (long long)a.n, (long long)a.m, a.d);
-    a.pairs = nullptr;   // the plain FP32 form neither uses nor updates seeds
     return launch_k0_pass(a, stream);
 }
 
@@ -298,26 +297,6 @@ int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, co
     a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.topo = topo; a.penalty = penalty;
     a.err3 = err3; a.train_bmu = bmu_out;
     a.outs = OUT_TRAIN | (err3 ? OUT_ERR : 0);
-    return run_pass(a, algo, W, tc, (cudaStream_t)stream);
-}
-
-int somgb_train_bmu_pass_seeded(const float* x, const double* rho, int64_t n, int d, const float* w,
-                                const float* topo, int64_t m, double penalty, int algo, int32_t* bmu_out,
-                                double* err3, int32_t* pairs, int pairs_in, void* ws, size_t ws_bytes,
-                                somgb_stream_t stream) {
-    if (int s = check_common(x, n, d, w, m, algo)) return s;
-    if (!bmu_out && !err3) return set_error(SOMGB_ERR_INVALID, "bmu_out and err3 are both NULL");
-    if (err3 && !topo) return set_error(SOMGB_ERR_INVALID, "topo is NULL");
-    if (n > 0 && !pairs) return set_error(SOMGB_ERR_INVALID, "pairs is NULL");
-    if (((uintptr_t)pairs) % 8) return set_error(SOMGB_ERR_INVALID, "pairs must be 8-byte aligned");
-    Workspace W;
-    bool tc = false;
-    if (int s = carve(ws, ws_bytes, SOMGB_OP_FIND_BMUS, n, m, d, algo, &W, &tc)) return s;
-    if (n == 0) return SOMGB_OK;
-    PassArgs a{};
-    a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.topo = topo; a.penalty = penalty;
-    a.err3 = err3; a.train_bmu = bmu_out; a.pairs = pairs; a.pairs_in = pairs_in != 0;
-    a.outs = (bmu_out ? OUT_TRAIN : 0) | (err3 ? OUT_ERR : 0);
     return run_pass(a, algo, W, tc, (cudaStream_t)stream);
 }
 

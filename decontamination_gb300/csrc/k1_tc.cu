@@ -23,32 +23,27 @@
 // + gamma, m being the best (second-best) s~ of the row; thr is non-decreasing in m, so any upper bound of m gives a
 // threshold that keeps every such unit.
 //
-// Epilogue. Each sweep warp reads its rows' s~ in 32-column chunks and keeps, per row, the running minimum (for the
-// error sums, the two smallest 8-unit group minima: an upper bound of the second-best s~). When a row of the warp can
-// have a candidate in a chunk (chunk minimum at or under its threshold), the warp builds the chunk's candidate bit
-// masks and every row with a non-zero mask appends (mask word, chunk minimum, chunk) to its own short list. Two forms:
-//   seeded passes (one sweep): the threshold starts at thr of the row's seed (an upper bound of m from the units that
-//     were best under an earlier map, tc_seed_kernel) and falls with the chunks swept; a chunk's mask is built
-//     against the threshold known before it and built again, against the one that takes the chunk in, only where
-//     that fell by more than a small slack (a loose or missing seed);
-//   passes without seeds (two sweeps, every MMA issued twice): the first sweep finds each row's bounds, the two
-//     column halves combine them into the final threshold, the second sweep builds the lists against it.
-// A full list first drops the entries whose chunk minimum is above the current threshold. The resolvers take each
-// row's entries whose chunk minimum is at or under the row's final threshold (both halves and the seed combined),
-// evaluate those candidates on CUDA cores with float32 differences (the reference's terms) and rank them; ranks
-// within float32 rounding of each other are decided by compensated float32 sums and, failing that, by the
-// reference's float64 sum. Rows with more than CAPR candidates, a full list, non-finite features or overflowing
+// Epilogue: two sweeps per row tile (every MMA is issued twice; the tensor pipe has the slack). Sweep 1 reads each
+// row's s~ in 32-column chunks and keeps the smallest value (for the error sums, the two smallest 8-unit group
+// minima: an upper bound of the second-best s~); the two column halves combine theirs into the row's threshold.
+// Sweep 2 reads the same values again: where a row of the warp can have a candidate in a chunk (chunk minimum at or
+// under its threshold), the warp builds the chunk's candidate bit masks, a branch-free subtraction and shift of the
+// sign bit per value, and every row with a non-zero mask appends (mask word, chunk) to its own short list. The
+// resolvers evaluate each row's candidates on CUDA cores with float32 differences (the reference's terms) and rank
+// them; ranks within float32 rounding of each other are decided by compensated float32 sums and, failing that, by
+// the reference's float64 sum. Rows with more than CAPR candidates, a full list, non-finite features or overflowing
 // distances go to an exact per-row recheck.
 //
-// Pipeline (one persistent CTA per SM, 576 threads, every hand-off an mbarrier):
-//   warp 17     TMA producer: the unit operand B (resident: one bulk copy; else a ring of column tiles in the MMAs'
-//               order), sample tiles (2-D tiled TMA, 2-stage ring);
-//   warp 16     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
+// Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
+//   warp 13     TMA producer: the unit operand B (resident: one bulk copy; else a ring of column tiles in the MMAs'
+//               order, twice per row tile), sample tiles (2-D tiled TMA, 2-stage ring);
+//   warp 12     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
 //   warps 0-7   converters (FP32 tile -> centred split-FP16 A tile) and sweeps; warp e reads TMEM lanes
-//               32(e&3).. and column half e>>2 and writes its rows' candidate lists (two list buffers);
-//   warps 8-15  resolvers in two groups of four, group g taking the row tiles t with t % 2 == g (list buffer g):
-//               thread r of the group's warp q decides row 32q+r: candidates' distances from the unit rows (shared
-//               memory when they fit, else L2), ranking, decision, outputs.
+//               32(e&3).. and column half e>>2 and writes its rows' candidate lists (two list buffers, so the sweeps
+//               of row tile t+1 do not wait for the resolvers of row tile t);
+//   warps 8-11  resolvers: thread r of warp 8+q decides row 32q+r of a row tile while the sweeps run the next one:
+//               candidates' distances from the unit rows (shared memory when they fit, else L2), ranking, decision,
+//               outputs.
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
@@ -101,8 +96,9 @@ static_assert(28 + 2 * BMAX <= NBARS, "mbarrier slots");
 static_assert(4 * MAX_U <= 256, "chunk ids are bytes");
 constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
-constexpr int RES_GROUP = 4;               // resolver warps per row tile (one thread per row)
-constexpr int RES_WARPS = 2 * RES_GROUP;   // two groups, alternate row tiles (each owns one list buffer)
+constexpr int RES_GROUP = 4;    // resolver warps per row tile (one thread per row)
+constexpr int RES_GROUPS = 1;   // groups of resolvers taking the row tiles in turn (1 or 2; list buffers: 2)
+constexpr int RES_WARPS = RES_GROUPS * RES_GROUP;
 constexpr int MMA_WARP = SWEEP_WARPS + RES_WARPS;
 constexpr int TMA_WARP = MMA_WARP + 1;
 constexpr int NUM_THREADS = (TMA_WARP + 1) * 32;
@@ -143,8 +139,8 @@ struct TcShape {
     int utiles = 0;
     int bstages = 0;   // 0: the whole unit operand resident in shared memory; else a ring of this many column tiles
     size_t b_bytes = 0, b_tile = 0, a_bytes = 0, x_bytes = 0;
-    size_t off_a = 0, off_x = 0, off_lw = 0, off_lm = 0, off_part = 0, off_row = 0, off_lc = 0, off_cnt = 0,
-           off_flag = 0, off_center = 0, off_bar = 0, off_w = 0, smem = 0;
+    size_t off_a = 0, off_x = 0, off_lw = 0, off_part = 0, off_thr = 0, off_lc = 0, off_cnt = 0, off_flag = 0,
+           off_center = 0, off_bar = 0, off_w = 0, smem = 0;
 };
 
 // Layout after a unit-operand region of `bregion` bytes; returns the end offset (before the unit rows).
@@ -154,16 +150,14 @@ size_t tc_layout(TcShape& s, size_t bregion) {
     off += 2 * align_up(s.a_bytes, 1024);
     s.off_x = off;
     off += XSTAGES * s.x_bytes;
-    // candidate lists, [buffer][half][entry][row]: mask words, chunk minima, chunk ids; per buffer, half and row the
-    // (a1, a2) of the half and the entry count; per buffer and row |x'|^2, the seed bound and the recheck flag
+    // candidate lists, [buffer][half][entry][row]: mask words and chunk ids; per buffer, half and row the half's
+    // bounds (a1, a2) and the entry count; per buffer and row the final threshold and the recheck flag
     s.off_lw = off;
-    off += (size_t)2 * HALVES * CAP * TM * 4;
-    s.off_lm = off;
     off += (size_t)2 * HALVES * CAP * TM * 4;
     s.off_part = off;
     off += (size_t)2 * HALVES * TM * 8;
-    s.off_row = off;
-    off += (size_t)2 * TM * 8;
+    s.off_thr = off;
+    off += (size_t)2 * TM * 4;
     s.off_lc = off;
     off += (size_t)2 * HALVES * CAP * TM;
     s.off_cnt = off;
@@ -205,12 +199,11 @@ TcShape tc_shape(int64_t m, int d) {
     return s;   // does not fit (smem > SMEM_LIMIT): refused by tc_shape_ok
 }
 
-// Scratch: [B operand | centre (d floats) and scale | recheck row list (n int32) | seed bounds (n floats)]
+// Scratch: [B operand | centre (d floats) and scale | recheck row list (n int32)]
 struct TcWs {
     uint8_t* b = nullptr;
     float* center = nullptr;
     int32_t* rows = nullptr;
-    float* seed = nullptr;
 };
 
 size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
@@ -222,14 +215,11 @@ size_t tc_ws_layout(int64_t n, int64_t m, int d, TcWs* out, void* base) {
     off += align_up((size_t)(d + 1) * 4, 256);   // centre and scale
     size_t orow = off;
     off += align_up((size_t)std::max<int64_t>(n, 1) * 4, 256);
-    size_t oseed = off;
-    off += align_up((size_t)std::max<int64_t>(n, 1) * 4, 256);
     if (out && base) {
         uint8_t* p = (uint8_t*)base;
         out->b = p + ob;
         out->center = (float*)(p + oc);
         out->rows = (int32_t*)(p + orow);
-        out->seed = (float*)(p + oseed);
     }
     return off;
 }
@@ -395,53 +385,6 @@ __global__ void tc_prep_b_kernel(const float* __restrict__ w, int64_t m, int d, 
     put(qc + 1, (float)(qs - (double)__half2float(qh)));
 }
 
-// Seed bounds for a pass whose rows' best units under an earlier map are known (pairs[2i], pairs[2i+1]; -1 or out of
-// range when not). For ERR passes the bound covers the second-best s~: both units valid and distinct, the larger of
-// their bounds (two distinct units lie at or under it); otherwise the bound of the first unit covers the best s~.
-// With d' = |x' - w'_b|^2 and |x'|^2 evaluated in float32 (relative error below eps = (D + 4) 2^-23 each), the GEMM
-// value of unit b satisfies s~_b <= d'(1 + eps)(1 + beta) - |x'|^2 (1 - eps) + alpha |x'|^2 (1 + eps) + gamma, and the
-// float32 evaluation of that expression is covered by a further 2^-20 (d' + |x'|^2). Any unit gives a valid bound,
-// so a stale or wrong pair only loosens the search, never changes a result. +inf where no bound is known.
-template <int DT>
-__global__ void tc_seed_kernel(const float* __restrict__ x, int64_t n, const float* __restrict__ w, int64_t m,
-                               const float* __restrict__ center, const int32_t* __restrict__ pairs, int need_two,
-                               float alpha, float beta, float* __restrict__ seed) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int2 pr = __ldg((const int2*)pairs + i);
-    const bool ok1 = pr.x >= 0 && pr.x < m;
-    const bool ok2 = pr.y >= 0 && pr.y < m && pr.y != pr.x;
-    if (!ok1 || (need_two && !ok2)) {
-        seed[i] = INFINITY;
-        return;
-    }
-    const float scale = center[DT];
-    const float* xr = x + i * DT;
-    const float* w1 = w + (int64_t)pr.x * DT;
-    const float* w2 = w + (int64_t)(need_two ? pr.y : pr.x) * DT;
-    float xn = 0.0f, d1 = 0.0f, d2 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < DT; ++k) {
-        const float ck = center[k];
-        const float xp = (__ldg(xr + k) - ck) * scale;
-        xn = fmaf(xp, xp, xn);
-        const float t1 = xp - (__ldg(w1 + k) - ck) * scale;
-        d1 = fmaf(t1, t1, d1);
-        const float t2 = xp - (__ldg(w2 + k) - ck) * scale;
-        d2 = fmaf(t2, t2, d2);
-    }
-    const float dd = fmaxf(d1, d2);
-    if (!(dd < 1.0e30f) || !(xn < 1.0e30f)) {
-        seed[i] = INFINITY;
-        return;
-    }
-    const float eps = (float)(DT + 4) * 1.1920929e-7f;   // (D + 4) 2^-23
-    const float up = 1.0f + eps;
-    const float ub = dd * up * (1.0f + beta) - xn * (1.0f - eps) + alpha * xn * up + GAMMA +
-                     9.5367432e-7f * (dd + xn);   // 2^-20 (d' + |x'|^2)
-    seed[i] = ub;
-}
-
 // ---------------------------------------------------------------------------------------------------------------------
 // main pass
 // ---------------------------------------------------------------------------------------------------------------------
@@ -452,12 +395,11 @@ struct TcArgs {
     const float* center;
     int32_t* rows;
     unsigned long long* row_count;
-    const float* seed;       // per-row seed bounds, or NULL (the two-sweep form)
     int kpad;
     int utiles;
     float alpha, beta, kthr;   // kthr = 2 / (1 - beta), rounded up
-    size_t off_a, off_x, off_lw, off_lm, off_part, off_row, off_lc, off_cnt, off_flag, off_center, off_bar, off_w,
-        a_stride, x_stride;
+    size_t off_a, off_x, off_lw, off_part, off_thr, off_lc, off_cnt, off_flag, off_center, off_bar, off_w, a_stride,
+        x_stride;
     uint32_t b_bytes;
     uint32_t b_tile;         // bytes of one column tile of the unit operand
     int bstages;             // 0: resident unit operand; else the ring depth
@@ -528,30 +470,19 @@ __device__ __forceinline__ float min8(const uint32_t (&v)[32], int b) {
     return fmin3(fmin3(f(0), f(1), f(2)), fmin3(f(3), f(4), f(5)), fminf(f(6), f(7)));
 }
 
-// One sweep warp's row: its running state over the chunks of its column half.
-struct RowSweep {
-    float a1, a2;     // smallest and second-smallest group minimum (ERR) / the running minimum (a1)
-    float thr;        // running threshold (never rises)
-    int cnt;          // list entries
-    bool ovf;         // more chunks with candidates than CAP
-};
-
 // The tensor-core pass. ERR: the error sums (second BMU ranked too); the bound of the second-best s~ is the
-// second-smallest 8-unit group minimum. TWO (passes without seeds): every column tile is computed twice, the first
-// sweep finds each row's final threshold and the second builds the candidate lists against it; otherwise (seeded
-// passes) one sweep builds them against the running threshold of the seed and the chunks already swept.
-template <bool ERR, int DT, bool TWO>
+// second-smallest 8-unit group minimum.
+template <bool ERR, int DT>
 __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs P) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
     uint32_t* sLw = (uint32_t*)(smem + P.off_lw);   // [2][HALVES][CAP][TM] mask words: bit 31-i = column 32c+i
-    float* sLm = (float*)(smem + P.off_lm);         // [2][HALVES][CAP][TM] the chunk's minimum s~
     uint8_t* sLc = smem + P.off_lc;                 // [2][HALVES][CAP][TM] chunk id u * 4 + c
     uint8_t* sCnt = smem + P.off_cnt;               // [2][HALVES][TM] entries; bit 7: the list overflowed
     float2* sPart = (float2*)(smem + P.off_part);   // [2][HALVES][TM] (a1, a2) of the half
-    float2* sRow = (float2*)(smem + P.off_row);     // [2][TM] (|x'|^2, seed bound)
+    float* sThr = (float*)(smem + P.off_thr);       // [2][TM] the row's threshold
     uint8_t* sFlag = smem + P.off_flag;             // [2][TM] the row goes to the exact recheck
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
@@ -564,7 +495,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint64_t* m_full = bars + 15;   // [2]: the sweeps have written the candidate lists of a row tile
     uint64_t* m_empty = bars + 17;  // [2]: the resolvers are done with them
     uint64_t* drain = bars + 19;
-    uint64_t* p_full = bars + 20;   // [2][4] two-sweep form: both halves of a lane quarter have published (a1, a2)
+    uint64_t* p_full = bars + 20;   // [2][4] both halves of a lane quarter have published (a1, a2)
     uint64_t* bs_full = bars + 28;  // [BMAX]: a column tile of the unit operand has landed (streamed operand)
     uint64_t* bs_empty = bars + 28 + BMAX; // [BMAX]: the MMAs reading it have completed
     __shared__ uint32_t tmem_base_s;
@@ -574,7 +505,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int d = DT;
     constexpr int kpad = k_width(DT);
-    constexpr int SWEEPS = TWO ? 2 : 1;
+    constexpr int SWEEPS = 2;
     const int U = P.utiles;
     const uint32_t lim = P.wait_limit;
     const int64_t num_tiles = (a.n + TM - 1) / TM;
@@ -766,12 +697,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         const uint32_t lane_base = (uint32_t)(q * 32) << 16;
 
         // centred, scaled split-FP16 A row of `row`: this thread writes the 16-byte chunks kc = h, h + 2, ... of
-        // kpad / 8; returns |x'|^2 (infinite when a coordinate is not finite or outside the FP16 split's range) and
-        // the row's seed bound (+inf when there is none)
-        auto convert = [&](int64_t it, float& xn_out, float& seed_out) -> bool {
+        // kpad / 8; returns |x'|^2 (infinite when a coordinate is not finite or outside the FP16 split's range)
+        auto convert = [&](int64_t it, float& xn_out) -> bool {
             const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
-            const int64_t grow = (blockIdx.x + it * gridDim.x) * TM + row;
-            seed_out = (P.seed && grow < a.n) ? __ldg(P.seed + grow) : INFINITY;   // used one row tile later
             if (it >= 2 && !wwait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
             if (!wwait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
             const float4* xs4 = (const float4*)(smem + P.off_x + s3 * P.x_stride) + row * (DT / 4);
@@ -875,135 +803,94 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         };
 
         int64_t gcons = 0;   // TMEM tiles consumed
-        float xn_next = 0.0f, seed_next = INFINITY;
-        bool ok = n_my > 0 ? convert(0, xn_next, seed_next) : true;
+        float xn_next = 0.0f;
+        bool ok = n_my > 0 ? convert(0, xn_next) : true;
         for (int64_t it = 0; ok && it < n_my && !waborted(); ++it) {
-            const float xn = xn_next, seedub = seed_next;
+            const float xn = xn_next;
             const int lb = (int)(it & 1);
             TC_T0();
-            if (it + 1 < n_my && !(ok = convert(it + 1, xn_next, seed_next))) break;
+            if (it + 1 < n_my && !(ok = convert(it + 1, xn_next))) break;
             TC_T(4);
-            // the resolvers are done with buffer lb (row tile it - 2): its lists, and in the two-sweep form the half
-            // exchange below, may be rewritten
+            // the resolvers are done with buffer lb (row tile it - 2): its lists and the half exchange below may be
+            // rewritten
             if (it >= 2 && !wwait(m_empty + lb, (uint32_t)(((it >> 1) - 1) & 1))) { fail(512u); break; }
             TC_T(5);
-            const bool flagged = !(xn < HUGE_S);
-            const float axg = fmaf(P.alpha, xn, GAMMA);
-            RowSweep rs;
-            rs.a1 = INFINITY;
-            rs.a2 = INFINITY;
-            rs.thr = flagged ? -INFINITY : thr_of(seedub, xn, axg, P.beta, P.kthr);
-            rs.cnt = 0;
-            rs.ovf = false;
-            if constexpr (TWO) {
-                // ---- sweep 1: the row's bounds over this half's columns ----------------------------------------
-                for (int u = 0; u < U && ok; ++u, ++gcons) {
-                    const int buf = (int)(gcons & 1);
-                    if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
-                    TC_T(0);
-                    ptx::tc_fence_after();
-                    stream_tile(buf, [&](int, const uint32_t (&r)[32]) { chunk_min(r, rs.a1, rs.a2); });
-                    TC_T(1);
-                }
-                if (!ok) break;
-                // both halves' bounds: the row's final threshold
-                sPart[(lb * HALVES + h) * TM + row] = make_float2(rs.a1, rs.a2);
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
-                if (!wwait(p_full + lb * 4 + q, (uint32_t)((it >> 1) & 1))) { fail(2048u); break; }
-                const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
-                const float M1 = fminf(p0.x, p1.x);
-                const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
-                rs.thr = fminf(rs.thr, thr_of(ERR ? M2 : M1, xn, axg, P.beta, P.kthr));
-            }
-            const size_t lbase = (size_t)((lb * HALVES + h) * CAP) * TM + row;
-            uint32_t* lw = sLw + lbase;
-            float* lm = sLm + lbase;
-            uint8_t* lc = sLc + lbase;
-            float thr_up = nextafterf(rs.thr, INFINITY);
-            // A chunk's candidate mask word, built only when a row of the warp can have a candidate there: first
-            // against the threshold known before the chunk (so that it does not wait for the chunk's own minimum), and
-            // again against `t`, the threshold that takes the chunk in, where that fell by more than `slack` (a loose
-            // or missing seed: the chunk holds a new minimum far under the old threshold).
-            const float slack = 2.0f * P.kthr * axg;
-            auto candidates = [&](int u, int c, const uint32_t (&r)[32], float cm, float t) {
-                if (__any_sync(0xffffffffu, cm <= rs.thr)) {
-                    uint32_t mw = sign_mask32(r, thr_up);
-                    if (__any_sync(0xffffffffu, mw != 0u && t < rs.thr - slack))
-                        mw = sign_mask32(r, nextafterf(t, INFINITY));
-                    if (mw != 0u) {
-                        if (rs.cnt == CAP) {   // full: drop the entries a lower threshold has ruled out
-                            int k = 0;
-                            for (int e = 0; e < CAP; ++e) {
-                                const float cme = lm[e * TM];
-                                if (cme <= t) {
-                                    if (k != e) {
-                                        lw[k * TM] = lw[e * TM];
-                                        lm[k * TM] = cme;
-                                        lc[k * TM] = lc[e * TM];
-                                    }
-                                    ++k;
-                                }
-                            }
-                            rs.cnt = k;
-                        }
-                        if (rs.cnt < CAP) {
-                            lw[rs.cnt * TM] = mw;
-                            lm[rs.cnt * TM] = cm;
-                            lc[rs.cnt * TM] = (uint8_t)(u * 4 + c);
-                            ++rs.cnt;
-                        } else {
-                            rs.ovf = true;
-                        }
-                    }
-                }
-            };
+            // ---- sweep 1: the row's bounds over this half's columns ------------------------------------------------
+            float a1 = INFINITY, a2 = INFINITY;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons & 1);
                 if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
                 TC_T(0);
                 ptx::tc_fence_after();
-                if constexpr (TWO) {
-                    // ---- sweep 2: candidate lists against the final threshold -----------------------------------
-                    stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
-                        candidates(u, c, r, fminf(min16<0>(r), min16<16>(r)), rs.thr);
-                    });
-                } else {
-                    // ---- the one sweep: lists against the running threshold, which then takes the chunk in ------
-                    stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
-                        const float cm = chunk_min(r, rs.a1, rs.a2);
-                        const float t = fminf(rs.thr, thr_of(ERR ? rs.a2 : rs.a1, xn, axg, P.beta, P.kthr));
-                        candidates(u, c, r, cm, t);
-                        if (t < rs.thr) {
-                            rs.thr = t;
-                            thr_up = nextafterf(t, INFINITY);
-                        }
-                    });
-                }
+                stream_tile(buf, [&](int, const uint32_t (&r)[32]) { chunk_min(r, a1, a2); });
                 TC_T(1);
             }
             if (!ok) break;
-            if constexpr (!TWO) sPart[(lb * HALVES + h) * TM + row] = make_float2(rs.a1, rs.a2);
-            sCnt[(lb * HALVES + h) * TM + row] = (uint8_t)(rs.cnt | (rs.ovf ? 0x80 : 0));
+            // both halves' bounds: the row's threshold. ERR: M2 is the second smallest 8-unit group minimum, an upper
+            // bound of the second smallest s~ (two groups have a unit at or below it), so the threshold derived from it
+            // keeps every possible second BMU.
+            sPart[(lb * HALVES + h) * TM + row] = make_float2(a1, a2);
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
+            if (!wwait(p_full + lb * 4 + q, (uint32_t)((it >> 1) & 1))) { fail(2048u); break; }
+            const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
+            const float M1 = fminf(p0.x, p1.x);
+            const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
+            const float mref = ERR ? M2 : M1;
+            const bool flagged = !(xn < HUGE_S) || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
+            const float thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
+            // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
+            // floats never rounds to zero), so each value costs one subtraction and one shift of its sign bit
+            const float thr_up = nextafterf(thr, INFINITY);
+            // ---- sweep 2: the candidate lists -----------------------------------------------------------------------
+            const size_t lbase = (size_t)((lb * HALVES + h) * CAP) * TM + row;
+            uint32_t* lw = sLw + lbase;
+            uint8_t* lc = sLc + lbase;
+            int cnt = 0;
+            bool ovf = false;
+            for (int u = 0; u < U && ok; ++u, ++gcons) {
+                const int buf = (int)(gcons & 1);
+                if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
+                TC_T(0);
+                ptx::tc_fence_after();
+                stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                    // the chunk's masks only when a row of the warp has a candidate in it
+                    if (__any_sync(0xffffffffu, fminf(min16<0>(r), min16<16>(r)) <= thr)) {
+                        const uint32_t mw = sign_mask32(r, thr_up);
+                        if (mw != 0u) {
+                            if (cnt < CAP) {
+                                lw[cnt * TM] = mw;
+                                lc[cnt * TM] = (uint8_t)(u * 4 + c);
+                                ++cnt;
+                            } else {
+                                ovf = true;
+                            }
+                        }
+                    }
+                });
+                TC_T(1);
+            }
+            if (!ok) break;
+            sCnt[(lb * HALVES + h) * TM + row] = (uint8_t)(cnt | (ovf ? 0x80 : 0));
             if (h == 0) {
-                sRow[lb * TM + row] = make_float2(xn, seedub);
+                sThr[lb * TM + row] = thr;
                 sFlag[lb * TM + row] = flagged ? 1 : 0;
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(m_full + lb);
         }
     } else if (warp < SWEEP_WARPS + RES_WARPS) {
-        // ------------------------------ resolvers (warps 8..15): group g takes the row tiles it with it % 2 == g ------
-        // (list buffer g) while the sweeps run the next ones; thread r of the group's warp q owns row 32q + r: float32
-        // distances of its candidates, the decision, the outputs
+        // ------------------------------ resolvers: group g takes the row tiles it with it % RES_GROUPS == g ---------
+        // (list buffer it % 2) while the sweeps run the next ones; thread r of the group's warp q owns row 32q + r:
+        // float32 distances of its candidates, the decision, the outputs
         const int grp = (warp - SWEEP_WARPS) / RES_GROUP, q = (warp - SWEEP_WARPS) % RES_GROUP;
         const int row = q * 32 + lane;
         const float g32 = (float)(d + 2) * 5.9604645e-8f;
         const float fac = 1.0f + 8.0f * g32;
         DFAcc e0, e1, e2;
         const float* wrows = P.off_w ? (const float*)(smem + P.off_w) : a.w;   // unit rows: shared memory or L2
-        for (int64_t it = grp; it < n_my && !waborted(); it += 2) {
-            const int lb = grp;
+        for (int64_t it = grp; it < n_my && !waborted(); it += RES_GROUPS) {
+            const int lb = (int)(it & 1);
             TC_T0();
             if (!wwait(m_full + lb, (uint32_t)((it >> 1) & 1))) { fail(1024u); break; }
             TC_T(6);
@@ -1018,15 +905,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const float4 t = __ldg((const float4*)xg + k4);
                 xr[4 * k4] = t.x; xr[4 * k4 + 1] = t.y; xr[4 * k4 + 2] = t.z; xr[4 * k4 + 3] = t.w;
             }
-            // the row's final threshold from both halves' bounds and its seed
-            const float2 rw = sRow[lb * TM + row];
-            const float xn = rw.x;
-            const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
-            const float M1 = fminf(p0.x, p1.x);
-            const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
-            const float mref = fminf(ERR ? M2 : M1, rw.y);
-            const bool flagged = sFlag[lb * TM + row] != 0 || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
-            const float thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
+            const bool flagged = sFlag[lb * TM + row] != 0;
             const uint8_t c0 = sCnt[(lb * HALVES + 0) * TM + row], c1 = sCnt[(lb * HALVES + 1) * TM + row];
             const bool ovf = ((c0 | c1) & 0x80) != 0;
             const int n0 = c0 & 0x7f, nwc = n0 + (c1 & 0x7f);
@@ -1040,9 +919,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 return (ch >> 2) * TN + (wi >= n0 ? 128 : 0) + (ch & 3) * 32 + 31;
             };
             // The candidates, one per lane and iteration (the next entry fetched in the same iteration), each one's
-            // float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found. Entries
-            // whose chunk minimum is above the final threshold hold no candidate and are skipped. A row with more than
-            // CAPR candidates stops there and goes to the exact recheck.
+            // float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found. A row with
+            // more than CAPR candidates stops there and goes to the exact recheck.
             int cnt = 0;
             float f1 = INFINITY, f2 = INFINITY, f3 = INFINITY;
             int32_t j1 = -1, j2 = -1, j3 = -1;
@@ -1062,7 +940,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     const bool need = word == 0u;
                     if (need && wi < nwc) {
                         const size_t ix = entry(wi);
-                        word = sLm[ix] <= thr ? sLw[ix] : 0u;
+                        word = sLw[ix];
                         jtop = entry_top(wi, ix);
                     }
                     wi += need ? 1 : 0;
@@ -1080,7 +958,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             auto for_each_cand = [&](auto&& f) {
                 for (int wi = 0; wi < nwc; ++wi) {
                     const size_t ix = entry(wi);
-                    if (!(sLm[ix] <= thr)) continue;
                     uint32_t word = sLw[ix];
                     const int jt = entry_top(wi, ix);
                     while (word) {
@@ -1092,7 +969,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             };
             TC_T(9);
             const bool recheck = live && (flagged || ovf || cnt == 0 || cnt > CAPR);
-            int32_t r1 = -1, r2 = -1;
             if (recheck) {
                 const unsigned long long slotq = atomicAdd(P.row_count, 1ull);
                 P.rows[slotq] = (int32_t)grow;
@@ -1108,6 +984,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const bool gap12 = j2 < 0 || !(f2 <= c1lim);
                 const bool separated = ERR ? (gap12 && (j3 < 0 || !(f3 <= c2lim))) : gap12;
                 const float climit = ERR ? c2lim : c1lim;
+                int32_t r1, r2;
                 float2 tr1 = make_float2(0.0f, 0.0f), tr2 = tr1;
                 DFloat rd1{0.0f, 0.0f};
                 if (separated) {
@@ -1163,9 +1040,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 TC_T(10);
                 emit_sample32(a, grow, rho_v, r1, r2, rd1, tr1, tr2, e0, e1, e2);
             }
-            // the row's best two units for the next pass's seeds (for BMU-only passes the second is the float32
-            // runner-up among the candidates: any unit gives a valid seed); rechecked rows are written by the recheck
-            if (a.pairs && live && !recheck) ((int2*)a.pairs)[grow] = make_int2(r1, ERR ? r2 : (j2 == r1 ? j1 : j2));
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(m_empty + lb);   // the sweeps may refill list buffer lb
             TC_T(7);
@@ -1200,7 +1074,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
 
 template <bool ERR, int DT>
 int launch_main(const CUtensorMap& tmap, const TcArgs& P, unsigned grid, size_t smem, cudaStream_t stream) {
-    auto kern = P.seed ? tc_pass_kernel<ERR, DT, false> : tc_pass_kernel<ERR, DT, true>;
+    auto kern = tc_pass_kernel<ERR, DT>;
     SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     timer_begin(stream);
     kern<<<grid, NUM_THREADS, smem, stream>>>(tmap, P);
@@ -1302,10 +1176,8 @@ void tc_debug_withhold(int64_t row_tile, uint32_t wait_limit) {
 size_t tc_workspace_bytes(int64_t n, int64_t m, int d) { return tc_ws_layout(n, m, d, nullptr, nullptr); }
 
 int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t stream) {
-    if (((uintptr_t)a.x) % 16 || ((uintptr_t)a.w) % 16 || ((a.outs & OUT_ERR) && ((uintptr_t)a.topo) % 8) ||
-        ((uintptr_t)a.pairs) % 8)
-        return set_error(SOMGB_ERR_INVALID,
-                         "tensor-core pass needs 16-byte aligned x and w, 8-byte aligned topo and pairs");
+    if (((uintptr_t)a.x) % 16 || ((uintptr_t)a.w) % 16 || ((a.outs & OUT_ERR) && ((uintptr_t)a.topo) % 8))
+        return set_error(SOMGB_ERR_INVALID, "tensor-core pass needs 16-byte aligned x and w, 8-byte aligned topo");
     const TcShape s = tc_shape(a.m, a.d);
     TcWs W;
     if (tc_ws_layout(a.n, a.m, a.d, &W, ws) > ws_bytes) return set_error(SOMGB_ERR_WORKSPACE, "tc workspace too small");
@@ -1321,19 +1193,6 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     tc_prep_b_kernel<<<(unsigned)ceil_div(s.mpad, 128), 128, 0, stream>>>(a.w, a.m, a.d, s.kpad, s.mpad, W.center,
                                                                           W.b);
     SOMGB_LAUNCH_CHECK();
-    // seed bounds from the rows' best units under an earlier map
-    const bool seeded = a.pairs && a.pairs_in;
-    if (seeded) {
-        const unsigned g = (unsigned)ceil_div(a.n, 256);
-        switch (a.d) {
-            case 4: tc_seed_kernel<4><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
-            case 8: tc_seed_kernel<8><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
-            case 16: tc_seed_kernel<16><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
-            default: tc_seed_kernel<32><<<g, 256, 0, stream>>>(a.x, a.n, a.w, a.m, W.center, a.pairs, err, P.alpha, P.beta, W.seed); break;
-        }
-        SOMGB_LAUNCH_CHECK();
-    }
-
     // sample tensor map: rows of d float32, boxes of 128 rows
     CUtensorMap tmap;
     cuuint64_t gdim[2] = {(cuuint64_t)a.d, (cuuint64_t)a.n};
@@ -1350,15 +1209,13 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     P.center = W.center;
     P.rows = W.rows;
     P.row_count = a.recheck_count;
-    P.seed = seeded ? W.seed : nullptr;   // without seeds: the two-sweep form
     P.kpad = s.kpad;
     P.utiles = s.utiles;
     P.off_a = s.off_a;
     P.off_x = s.off_x;
     P.off_lw = s.off_lw;
-    P.off_lm = s.off_lm;
     P.off_part = s.off_part;
-    P.off_row = s.off_row;
+    P.off_thr = s.off_thr;
     P.off_lc = s.off_lc;
     P.off_cnt = s.off_cnt;
     P.off_flag = s.off_flag;
@@ -1399,7 +1256,7 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     }
     if (st) return st;
     // rows the tensor-core pass could not decide: the exact CUDA-core pass over the listed rows (it must not count
-    // into the list length it reads; it writes those rows' pairs)
+    // into the list length it reads)
     PassArgs b = a;
     b.recheck_count = nullptr;
     return launch_k0_pass(b, stream, W.rows, a.recheck_count);

@@ -27,9 +27,6 @@ struct PassArgs {
     double* err3;          // OUT_ERR (3)
     int32_t* train_bmu;    // OUT_TRAIN (n)
     unsigned long long* recheck_count;  // optional: samples that took the exact path
-    int32_t* pairs;        // optional (tensor-core pass), n x 2: in (when pairs_in), each row's best two units under
-                           // an earlier map (seeds; -1 = unknown); out, under this map (-1 where not ranked)
-    int pairs_in;          // pairs holds seeds on input
     unsigned int* status;  // optional: this call's status word (bounded waits that gave up), besides the global one
     int outs;
 };
@@ -52,7 +49,6 @@ __device__ __forceinline__ void emit_sample(const PassArgs& a, int64_t i, const 
         float r32 = (float)rho;
         a.train_bmu[i] = (r32 > 0.0f && r.i1 >= 0) ? r.i1 : -1;
     }
-    if (a.pairs) ((int2*)a.pairs)[i] = make_int2(r.i1, r.i2);   // the tensor-core pass's recheck: next pass's seeds
     if ((outs & OUT_ERR) && rho > 0.0 && r.i1 >= 0 && r.i2 >= 0 && r.i1 != r.i2) {
         e0 += rho * sqrt(r.d1);
         if (topo_sqdist(a.topo, r.i1, r.i2) > a.penalty) e1 += rho;

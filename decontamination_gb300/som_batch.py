@@ -85,11 +85,10 @@ class SOM_Batch(SOM_Abstract):
         return xc, rc, bounds
 
     def _chunk_source(self, dataset, dataset_weights, device):
-        """Chunks for the epoch loop, as (x, rho, bounds, pieces, pairs). Arrays are uploaded once and reused by every
-        epoch: the first epoch gets them with the row pieces of their upload (its passes overlap the copy, and the
-        bounds are accumulated piece by piece), later epochs whole (pieces None, bounds complete). A resident chunk
-        also keeps each row's best two units from the previous pass (`pairs`), which seed the next pass's search.
-        Generator datasets are uploaded every epoch, as the reference does, without seeds."""
+        """Chunks for the epoch loop, as (x, rho, bounds, pieces). Arrays are uploaded once and reused by every epoch:
+        the first epoch gets them with the row pieces of their upload (its passes overlap the copy, and the bounds
+        are accumulated piece by piece), later epochs whole (pieces None, bounds complete). Generator datasets are
+        uploaded every epoch, as the reference does."""
         if (dataset is None or is_array(dataset)) and (dataset_weights is None or is_array(dataset_weights)):
             resident = []
 
@@ -97,13 +96,11 @@ class SOM_Batch(SOM_Abstract):
                 for xr, rr in raw_chunks(dataset, dataset_weights):
                     xd, rd, pieces = device_pieces(xr, rr, self._dtype, device)
                     bounds = None if self._is_f64 else torch.zeros(self._dim + 1, dtype=torch.float32, device=device)
-                    pairs = None if self._is_f64 else torch.full((_device.rows(xd), 2), -1, dtype=torch.int32,
-                                                                 device=device)
-                    resident.append((xd, rd, bounds, None, pairs))
-                    yield xd, rd, bounds, pieces, pairs
+                    resident.append((xd, rd, bounds, None))
+                    yield xd, rd, bounds, pieces
 
             return lambda: first() if not resident else iter(resident)
-        return lambda: ((*self._with_bounds(xc, rc, device), None, None)
+        return lambda: ((*self._with_bounds(xc, rc, device), None)
                         for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device))
 
     def _bmu_buffer(self, n, device):
@@ -112,11 +109,9 @@ class SOM_Batch(SOM_Abstract):
             buf = self._bmu_buf = torch.empty(max(n, 1), dtype=torch.int32, device=device)
         return buf
 
-    def _piece_pass(self, xd, rd, a, b, last, with_errors, w, topo, err, e, device, pairs=None):
+    def _piece_pass(self, xd, rd, a, b, last, with_errors, w, topo, err, e, device):
         """Rows a..b of a resident chunk: the training pass (BMUs; error sums of the previous epoch's map when e > 0)
-        or, after the last epoch, the error pass. Float64 maps train in one call per chunk (_accumulate). With
-        `pairs` (the chunk's best two units per row, written by every pass) the passes after the first are seeded by
-        the previous one's."""
+        or, after the last epoch, the error pass. Float64 maps train in one call per chunk (_accumulate)."""
         M, D = self._m * self._n, self._dim
         xc, rc = xd[a:b], (None if rd is None else rd[a:b])
         n = b - a
@@ -126,11 +121,6 @@ class SOM_Batch(SOM_Abstract):
             if self._is_f64:
                 _native.call('somgb_compute_errors_f64', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
                              topo.data_ptr(), M, self._penalty, err.data_ptr(), _device.stream())
-            elif pairs is not None:
-                wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, n, M, D, self._algo, device)
-                _native.call('somgb_train_bmu_pass_seeded', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
-                             topo.data_ptr(), M, self._penalty, self._algo, None, err.data_ptr(),
-                             pairs[a:b].data_ptr(), 1 if e > 0 else 0, wsp, wsb, _device.stream())
             else:
                 wsp, wsb = self._ws.for_op(_native.OP_ERRORS, n, M, D, self._algo, device)
                 _native.call('somgb_compute_errors', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
@@ -141,14 +131,9 @@ class SOM_Batch(SOM_Abstract):
             return
         bmu = self._bmu_buffer(_device.rows(xd), device)[a:b]
         wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, n, M, D, self._algo, device)
-        err_p = _device.ptr(err if e > 0 else None)
-        if pairs is not None:
-            _native.call('somgb_train_bmu_pass_seeded', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
-                         topo.data_ptr(), M, self._penalty, self._algo, bmu.data_ptr(), err_p,
-                         pairs[a:b].data_ptr(), 1 if e > 0 else 0, wsp, wsb, _device.stream())
-        else:
-            _native.call('somgb_train_bmu_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(),
-                         M, self._penalty, self._algo, bmu.data_ptr(), err_p, wsp, wsb, _device.stream())
+        _native.call('somgb_train_bmu_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(), M,
+                     self._penalty, self._algo, bmu.data_ptr(), _device.ptr(err if e > 0 else None), wsp, wsb,
+                     _device.stream())
 
     def _accumulate(self, xd, rd, bounds, S, c, w, topo, err):
         """The per-BMU sums of a whole chunk after its BMU passes (float64 maps: the fused float64 epoch pass, with
@@ -225,7 +210,7 @@ class SOM_Batch(SOM_Abstract):
             c.zero_()
             err = errs[e] if with_errors else None
             last = e == n_epochs
-            for xd, rd, bounds, pieces, pairs in chunks():
+            for xd, rd, bounds, pieces in chunks():
                 if pieces is None:
                     pieces = [(0, _device.rows(xd))]
                 elif bounds is not None:
@@ -233,12 +218,12 @@ class SOM_Batch(SOM_Abstract):
                     for a, b in pieces:
                         _native.call('somgb_feature_bounds', xd[a:b].data_ptr(), _device.ptr(rd[a:b] if rd is not None
                                      else None), b - a, D, bounds.data_ptr(), _device.stream())
-                        self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device, pairs)
+                        self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
                     if not last:
                         self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
                     continue
                 for a, b in pieces:
-                    self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device, pairs)
+                    self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
                 if not last:
                     self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
             if check_stop and e > 0 and with_errors:

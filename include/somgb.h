@@ -173,22 +173,6 @@ int somgb_train_epoch_pass_f64(const double* x, const double* rho, int64_t n, in
 int somgb_train_bmu_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
                          int64_t m, double penalty, int algo, int32_t* bmu_out, double* err3, void* ws,
                          size_t ws_bytes, somgb_stream_t stream);
-/*
- * somgb_train_bmu_pass with seeds: the same outputs (bmu_out and err3 as there; either may be NULL, not both), and
- * `pairs` (n x 2 int32, 8-byte aligned): on output each row's best two units under `w` (-1 where the pass did not rank
- * them; the plain FP32 form leaves pairs unchanged); on input, when pairs_in != 0, the same under an earlier map (-1
- * when unknown), else ignored (the first pass of a training). A row's two units under the previous epoch's map bound
- * its best distances under this one from above, which lets the tensor-core pass build its candidate lists in one
- * sweep instead of two; any unit gives a valid bound, so results never depend on the pairs' contents, only the time
- * does. Replaces the BMU half of _train_step1_epoch_kernel/_train_step2_xpu (algo/som_batch.py:94-150, 509-540),
- * whose training loop re-runs the search every epoch on the previous epoch's update of the same map
- * (som_batch.py:285-363), and its compute_errors pass (som_batch.py:363) when bmu_out is NULL. Workspace:
- * SOMGB_OP_FIND_BMUS sizing.
- */
-int somgb_train_bmu_pass_seeded(const float* x, const double* rho, int64_t n, int d, const float* w,
-                                const float* topo, int64_t m, double penalty, int algo, int32_t* bmu_out,
-                                double* err3, int32_t* pairs, int pairs_in, void* ws, size_t ws_bytes,
-                                somgb_stream_t stream);
 int somgb_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, somgb_stream_t stream);
 int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
                      const float* bounds, double* S, double* c, somgb_stream_t stream);

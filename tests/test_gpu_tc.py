@@ -1,0 +1,99 @@
+"""GPU tests of the tensor-core pass's training entry point on large maps and of its bounded waits (C ABI).
+
+Maps above 4096 units (80x80, as in the mixed-training configuration, and 128x128) take the tensor-core path, and the
+training pass must give the oracle's BMUs and error sums. A row tile whose samples are withheld (the test hook) makes a
+bounded wait run out: the pass reports it in its own workspace's status word and in the device status word instead of
+hanging, and the next call is exact again.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from decontamination_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+ERR_RTOL = 1e-9
+
+
+def _ws(native, op, n, m, d, algo, device):
+    nbytes = native.workspace_bytes(op, n, m, d, algo)
+    buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+    return buf, buf.data_ptr() + (-buf.data_ptr()) % 256, nbytes
+
+
+@pytest.mark.parametrize('m,n,d,N,topology', [(80, 80, 16, 30_000, 'square'), (80, 80, 32, 20_000, 'hexagonal'),
+                                               (128, 128, 8, 10_000, 'square'), (64, 64, 16, 40_000, 'square')])
+def test_training_pass_on_large_maps(cuda, native, oracle, m, n, d, N, topology):
+    rng = np.random.default_rng(m * 7 + d)
+    M = m * n
+    x = synthetic.correlated_lognormal(N, d, 5)
+    w = x[rng.integers(0, N, M)] * (1 + 0.02 * rng.standard_normal((M, d))).astype(np.float32)
+    topo = oracle.topography(m, n, topology)
+    pen = 2.0 if topology == 'square' else 1.0
+    assert native.lib().somgb_algo_supported(native.ALGO_TC, N, M, d), 'must take the tensor-core path'
+    xd, wd, td = (torch.from_numpy(np.ascontiguousarray(a)).to(cuda) for a in (x, w, topo))
+    s = torch.cuda.current_stream().cuda_stream
+    bmu = torch.full((N,), -7, dtype=torch.int32, device=cuda)
+    err = torch.zeros(3, dtype=torch.float64, device=cuda)
+    buf, wsp, nbytes = _ws(native, native.OP_FIND_BMUS, N, M, d, native.ALGO_TC, cuda)
+    native.call('somgb_train_bmu_pass', xd.data_ptr(), None, N, d, wd.data_ptr(), td.data_ptr(), M, pen,
+                native.ALGO_TC, bmu.data_ptr(), err.data_ptr(), wsp, nbytes, s)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bmu.cpu().numpy(), oracle.find_bmus(w, x, 'numba'))
+    np.testing.assert_allclose(err.cpu().numpy(), oracle.compute_errors_raw(w, topo, x, None, pen, 'numba'),
+                               rtol=ERR_RTOL)
+    st = ctypes.c_uint(1)
+    native.call('somgb_workspace_status', wsp, ctypes.addressof(st), 0, s)
+    assert st.value == 0
+
+
+def test_bounded_wait_runs_out_and_the_next_call_is_exact(cuda, native):
+    """The producer never loads one row tile's samples (test hook, short wait limit): the pass returns with its
+    status set instead of hanging, and a normal call afterwards gives exactly the BMUs of a normal call before."""
+    rng = np.random.default_rng(13)
+    N, M, d = 200_000, 1024, 16
+    x = synthetic.correlated_lognormal(N, d, 8)
+    w = x[rng.integers(0, N, M)].copy()
+    xd, wd = torch.from_numpy(x).to(cuda), torch.from_numpy(w).to(cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    buf, wsp, nbytes = _ws(native, native.OP_FIND_BMUS, N, M, d, native.ALGO_TC, cuda)
+    buf2, wsp2, _ = _ws(native, native.OP_FIND_BMUS, N, M, d, native.ALGO_TC, cuda)
+    st = ctypes.c_uint(0)
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    assert st.value == 0
+
+    def find(ws_ptr):
+        out = torch.full((N,), -7, dtype=torch.int32, device=cuda)
+        native.call('somgb_find_bmus', xd.data_ptr(), N, d, wd.data_ptr(), M, native.ALGO_TC, out.data_ptr(), ws_ptr,
+                    nbytes, s)
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
+
+    before = find(wsp)
+    native.call('somgb_workspace_status', wsp, ctypes.addressof(st), 0, s)
+    assert st.value == 0
+    native.call('somgb_debug_tc_withhold', 5, 20_000)
+    find(wsp)                                          # returns early on the GPU; the C call itself succeeds
+    native.call('somgb_workspace_status', wsp, ctypes.addressof(st), 0, s)
+    assert st.value != 0, 'the call whose wait ran out reports it in its own workspace'
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    assert st.value != 0
+    native.call('somgb_device_status', ctypes.addressof(st), 0, s)
+    assert st.value == 0, 'reading with clear resets the device status'
+    after = find(wsp2)                                 # the hook is one-shot
+    assert np.array_equal(after, before)
+    native.call('somgb_workspace_status', wsp2, ctypes.addressof(st), 0, s)
+    assert st.value == 0
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    assert st.value == 0
+
+
+def test_debug_hook_arguments_are_checked(native):
+    with pytest.raises(native.SomgbError):
+        native.call('somgb_debug_tc_withhold', -1, 100)
+    with pytest.raises(native.SomgbError):
+        native.call('somgb_debug_tc_withhold', 0, 0)
