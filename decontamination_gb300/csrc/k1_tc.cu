@@ -4,7 +4,7 @@
 // w' = (w - c) S are centred on the mean unit c (the centring shrinks every error term below) and scaled by a power
 // of two S that puts the largest unit coordinate in [2^5, 2^6) (samples up to 512 times farther out stay in FP16
 // range; the scaling is exact in float32). One GEMM per
-// 128-sample row tile and 256-unit column tile produces s~_j in TMEM:
+// 128-sample row tile and TN-unit column tile produces s~_j in TMEM:
 //   A row (sample)  = [ x'_hi | x'_lo | x'_hi | 2^11 | 2^11 | 0 ... ]             (FP16, K padded to a multiple of 16)
 //   B row (unit j)  = [ -2w'_hi | -2w'_hi | -2w'_lo | q_hi | q_lo | 0 ... ] with q_hi + q_lo = 2^-11 |w'_j|^2
 // so that sum_k A.B = -2 (x_hi w_hi + x_lo w_hi + x_hi w_lo) + |w'|^2 ~ s_j, accumulated in FP32. (For D a multiple
@@ -37,7 +37,7 @@
 // Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
 //   warp 13     TMA producer: the unit operand B (resident: one bulk copy; else a ring of column tiles in the MMAs'
 //               order, twice per row tile), sample tiles (2-D tiled TMA, 2-stage ring);
-//   warp 12     TMEM allocator and MMA issuer (one thread), two 256-column TMEM accumulators;
+//   warp 12     TMEM allocator and MMA issuer (one thread), NACC TMEM accumulators of TN columns each;
 //   warps 0-7   converters (FP32 tile -> centred split-FP16 A tile) and sweeps; warp e reads TMEM lanes
 //               32(e&3).. and column half e>>2 and writes its rows' candidate lists (two list buffers, so the sweeps
 //               of row tile t+1 do not wait for the resolvers of row tile t);
@@ -85,15 +85,19 @@ namespace {
 
 constexpr int TM = 128;           // samples per row tile (MMA M)
 constexpr int TN = 256;           // units per column tile (MMA N)
-constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning 128 of 256 columns
+constexpr int NACC = 512 / TN;    // TMEM accumulators (512 columns), so the MMAs run up to NACC - 1 tiles ahead
+constexpr int HW = TN / 2;        // columns of a tile per sweep warp (two column halves)
+constexpr int CPW = HW / 32;      // 32-column chunks per tile and sweep warp
+constexpr int HALVES = 2;         // sweep warps per TMEM lane quarter, each owning half of a tile's columns
 constexpr int CAPR = 24;          // candidates a resolver ranks per row
 constexpr int CAP = 4;            // candidate-list entries per row and column half
 constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
-constexpr int MAX_U = 64;         // column tiles per row tile (a list entry names its chunk, 4 per tile and half, in a byte)
-constexpr int NBARS = 40;         // mbarrier slots
-constexpr int BMAX = 4;           // deepest ring of streamed unit-operand tiles (slots 28 .. 28 + 2 BMAX - 1)
-static_assert(28 + 2 * BMAX <= NBARS, "mbarrier slots");
-static_assert(4 * MAX_U <= 256, "chunk ids are bytes");
+constexpr int MAX_U = 16384 / TN; // column tiles per row tile (a list entry names its chunk, CPW per tile and half, in a byte)
+constexpr int NBARS = 48;         // mbarrier slots
+constexpr int BMAX = 4;           // deepest ring of streamed unit-operand tiles (slots 32 .. 32 + 2 BMAX - 1)
+static_assert(32 + 2 * BMAX <= NBARS, "mbarrier slots");
+static_assert(CPW * MAX_U <= 256, "chunk ids are bytes");
+static_assert(NACC * TN == 512 && CPW * 32 == HW, "TMEM and chunk layout");
 constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
 constexpr int SWEEP_WARPS = 4 * HALVES;
 constexpr int RES_GROUP = 4;    // resolver warps per row tile (one thread per row)
@@ -184,7 +188,7 @@ TcShape tc_shape(int64_t m, int d) {
     // In order of preference: the unit operand resident with the unit rows; a ring of BMAX (down to 2) column tiles
     // streamed from L2 with the unit rows; then the same without the unit rows (the resolvers read them from L2).
     for (int rows = 1; rows >= 0; --rows) {
-        for (int st : {0, BMAX, BMAX - 1, 2}) {
+        for (int st = 0; st == 0 || st >= 2; st = st == 0 ? BMAX : st - 1) {
             s.bstages = st;
             size_t off = tc_layout(s, st == 0 ? s.b_bytes : (size_t)st * align_up(s.b_tile, 1024));
             s.off_w = 0;
@@ -479,7 +483,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint8_t* sB = smem;
     float* sCenter = (float*)(smem + P.off_center);
     uint32_t* sLw = (uint32_t*)(smem + P.off_lw);   // [2][HALVES][CAP][TM] mask words: bit 31-i = column 32c+i
-    uint8_t* sLc = smem + P.off_lc;                 // [2][HALVES][CAP][TM] chunk id u * 4 + c
+    uint8_t* sLc = smem + P.off_lc;                 // [2][HALVES][CAP][TM] chunk id u * CPW + c
     uint8_t* sCnt = smem + P.off_cnt;               // [2][HALVES][TM] entries; bit 7: the list overflowed
     float2* sPart = (float2*)(smem + P.off_part);   // [2][HALVES][TM] (a1, a2) of the half
     float* sThr = (float*)(smem + P.off_thr);       // [2][TM] the row's threshold
@@ -490,14 +494,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint64_t* x_empty = bars + 4;   // [XSTAGES]
     uint64_t* a_full = bars + 7;    // [2]
     uint64_t* a_empty = bars + 9;   // [2]
-    uint64_t* t_full = bars + 11;   // [2]
-    uint64_t* t_empty = bars + 13;  // [2]
-    uint64_t* m_full = bars + 15;   // [2]: the sweeps have written the candidate lists of a row tile
-    uint64_t* m_empty = bars + 17;  // [2]: the resolvers are done with them
-    uint64_t* drain = bars + 19;
-    uint64_t* p_full = bars + 20;   // [2][4] both halves of a lane quarter have published (a1, a2)
-    uint64_t* bs_full = bars + 28;  // [BMAX]: a column tile of the unit operand has landed (streamed operand)
-    uint64_t* bs_empty = bars + 28 + BMAX; // [BMAX]: the MMAs reading it have completed
+    uint64_t* t_full = bars + 11;   // [NACC]: an accumulator holds a computed column tile
+    uint64_t* t_empty = bars + 15;  // [NACC]: the sweeps have read it
+    uint64_t* m_full = bars + 19;   // [2]: the sweeps have written the candidate lists of a row tile
+    uint64_t* m_empty = bars + 21;  // [2]: the resolvers are done with them
+    uint64_t* drain = bars + 23;
+    uint64_t* p_full = bars + 24;   // [2][4] both halves of a lane quarter have published (a1, a2)
+    uint64_t* bs_full = bars + 32;  // [BMAX]: a column tile of the unit operand has landed (streamed operand)
+    uint64_t* bs_empty = bars + 32 + BMAX; // [BMAX]: the MMAs reading it have completed
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_s;
 
@@ -521,11 +525,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             ptx::mbar_init(x_full + s, 1);
             ptx::mbar_init(x_empty + s, SWEEP_WARPS);
         }
+        for (int s = 0; s < NACC; ++s) {
+            ptx::mbar_init(t_full + s, 1);
+            ptx::mbar_init(t_empty + s, SWEEP_WARPS);
+        }
         for (int s = 0; s < 2; ++s) {
             ptx::mbar_init(a_full + s, SWEEP_WARPS);
             ptx::mbar_init(a_empty + s, 1);
-            ptx::mbar_init(t_full + s, 1);
-            ptx::mbar_init(t_empty + s, SWEEP_WARPS);
             ptx::mbar_init(m_full + s, SWEEP_WARPS);
             ptx::mbar_init(m_empty + s, RES_GROUP);
             for (int qq = 0; qq < 4; ++qq) ptx::mbar_init(p_full + s * 4 + qq, HALVES);
@@ -648,9 +654,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 const uint32_t a_addr = ptx::smem_u32(smem + P.off_a + s * P.a_stride);
                 for (int uu = 0; uu < SWEEPS * U; ++uu, ++g) {
                     const int u = uu >= U ? uu - U : uu;
-                    const int buf = (int)(g & 1);
+                    const int buf = (int)(g % NACC);
                     TC_T0();
-                    if (g >= 2 && !ptx::mbar_wait(t_empty + buf, (uint32_t)(((g >> 1) - 1) & 1), lim)) {
+                    if (g >= NACC && !ptx::mbar_wait(t_empty + buf, (uint32_t)((g / NACC - 1) & 1), lim)) {
                         fail(8u);
                         ok = false;
                         break;
@@ -691,7 +697,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         }
     } else if (warp < SWEEP_WARPS) {
         // ------------------------------ converter + sweep (warps 0..7) ----------------------------------------------
-        // warp e: TMEM lane quarter q = e & 3 (rows 32q..32q+31), column half h = e >> 2 (128 of each 256 columns)
+        // warp e: TMEM lane quarter q = e & 3 (rows 32q..32q+31), column half h = e >> 2 (HW of each tile's TN columns)
         const int q = warp & 3, h = warp >> 2;
         const int row = q * 32 + lane;
         const uint32_t lane_base = (uint32_t)(q * 32) << 16;
@@ -764,25 +770,28 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             if (lane == 0) ptx::mbar_arrive(t_empty + buf);
         };
 
-        // This warp's 128 columns of TMEM tile `buf` in four 32-column chunks, software-pipelined: chunk c + 1 is
-        // loading while chunk c is processed (tcgen05.wait::ld waits for every load issued before it, so one load is
-        // in flight at a time). The accumulator is handed back as soon as the last load has landed.
+        // This warp's HW columns of TMEM tile `buf` in CPW 32-column chunks, software-pipelined: chunk c + 1 is loading
+        // while chunk c is processed (tcgen05.wait::ld waits for every load issued before it, so one load is in flight
+        // at a time). The accumulator is handed back as soon as the last load has landed.
         auto stream_tile = [&](int buf, auto&& process) {
-            const uint32_t base = tbase + lane_base + (uint32_t)(buf * TN + h * 128);
+            const uint32_t base = tbase + lane_base + (uint32_t)(buf * TN + h * HW);
             uint32_t ra[32], rb[32];
             ptx::tmem_ld32_raw(base, ra);
             ptx::tmem_wait_ld1(ra);
-            ptx::tmem_ld32_raw(base + 32, rb);
-            process(0, ra);
-            ptx::tmem_wait_ld1(rb);
-            ptx::tmem_ld32_raw(base + 64, ra);
-            process(1, rb);
-            ptx::tmem_wait_ld1(ra);
-            ptx::tmem_ld32_raw(base + 96, rb);
-            process(2, ra);
+#pragma unroll
+            for (int c = 0; c + 2 < CPW; c += 2) {
+                ptx::tmem_ld32_raw(base + 32 * (c + 1), rb);
+                process(c, ra);
+                ptx::tmem_wait_ld1(rb);
+                ptx::tmem_ld32_raw(base + 32 * (c + 2), ra);
+                process(c + 1, rb);
+                ptx::tmem_wait_ld1(ra);
+            }
+            ptx::tmem_ld32_raw(base + 32 * (CPW - 1), rb);
+            process(CPW - 2, ra);
             ptx::tmem_wait_ld1(rb);
             release(buf);
-            process(3, rb);
+            process(CPW - 1, rb);
         };
 
         // the chunk's minimum; for ERR it also folds the chunk's four 8-unit group minima into the running two
@@ -818,8 +827,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             // ---- sweep 1: the row's bounds over this half's columns ------------------------------------------------
             float a1 = INFINITY, a2 = INFINITY;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
-                const int buf = (int)(gcons & 1);
-                if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(64u); ok = false; break; }
+                const int buf = (int)(gcons % NACC);
+                if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) { fail(64u); ok = false; break; }
                 TC_T(0);
                 ptx::tc_fence_after();
                 stream_tile(buf, [&](int, const uint32_t (&r)[32]) { chunk_min(r, a1, a2); });
@@ -849,8 +858,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             int cnt = 0;
             bool ovf = false;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
-                const int buf = (int)(gcons & 1);
-                if (!wwait(t_full + buf, (uint32_t)((gcons >> 1) & 1))) { fail(128u); ok = false; break; }
+                const int buf = (int)(gcons % NACC);
+                if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) { fail(128u); ok = false; break; }
                 TC_T(0);
                 ptx::tc_fence_after();
                 stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
@@ -860,7 +869,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                         if (mw != 0u) {
                             if (cnt < CAP) {
                                 lw[cnt * TM] = mw;
-                                lc[cnt * TM] = (uint8_t)(u * 4 + c);
+                                lc[cnt * TM] = (uint8_t)(u * CPW + c);
                                 ++cnt;
                             } else {
                                 ovf = true;
@@ -916,7 +925,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             };
             auto entry_top = [&](int wi, size_t ix) -> int {   // the unit of bit 0 of the entry's word
                 const int ch = sLc[ix];
-                return (ch >> 2) * TN + (wi >= n0 ? 128 : 0) + (ch & 3) * 32 + 31;
+                return (ch / CPW) * TN + (wi >= n0 ? HW : 0) + (ch % CPW) * 32 + 31;
             };
             // The candidates, one per lane and iteration (the next entry fetched in the same iteration), each one's
             // float32 distance computed and ranked (float32 top-3 in (distance, unit) order) as it is found. A row with
