@@ -1,23 +1,30 @@
 #!/usr/bin/env python3
 """Benchmark of the batch-SOM hot path on GB300: one step = one SOM_Batch training epoch.
 
-Workload (default): hexagonal 32x32 map, D=16 float32 features, N=12,582,912 samples (the HEALPix nside=1024
-pixel count) from the seeded correlated log-normal generator (decontamination_gb300.synthetic, seed 2), weights
-U[-1, 1], sigma0 = 16 with the reference's 1/(1+2e/E) decay over a 20-epoch schedule.
+Workload (default, the shape of the >=10x target): square 64x64 map, D=16 float32 features, N=12,582,912 samples (the
+HEALPix nside=1024 pixel count) from the seeded correlated log-normal generator (decontamination_gb300.synthetic,
+seed 2), weights U[-1, 1], sigma0 = 32 with the reference's 1/(1+2e/E) decay over a 20-epoch schedule.
 
-  value   epochs with the catalogue resident in HBM (805 MB > L2, so no flush is needed): each epoch is one fused
-          BMU + error pass, the per-BMU segmented sums and the neighbourhood update, timed with CUDA events;
-          metric N*M / epoch time in Gsample.unit/s.
-  e2e     the same metric through the public API call a user makes, SOM_Batch.train(X, n_epochs=1) on a pinned
-          host tensor: host->device copy of the catalogue, training pass, error pass and device->host copy of the
-          weights, history and errors every step.
-  fp32_form  the plain FP32 CUDA-core form of the same epoch (the tensor-core path's baseline).
+  value     epochs with the catalogue resident in HBM (805 MB > L2, so no flush is needed): each epoch is one fused
+            BMU + error pass, the per-BMU segmented sums and the neighbourhood update, timed with CUDA events;
+            metric N*M / epoch time in Gsample.unit/s.
+  e2e       the same metric through the public API call a user makes, SOM_Batch.train(X, n_epochs=1) on a pinned
+            host tensor: host->device copy of the catalogue, training pass, error pass and device->host copy of the
+            weights, history and errors every step.
+  fp32_form the plain FP32 CUDA-core form of the same epoch (the tensor-core path's baseline).
+  parity    on the full catalogue after the timed epochs: the BMUs of the tensor-core pass against an independent
+            evaluation (float32 GEMM distances for the three nearest units, then the reference's typing), rows whose
+            two best distances are tied within float32 rounding counted and adjudicated by float64 distances; the
+            trained weights of one more epoch against a float64 evaluation of the same update from the same BMUs.
+  sq64      the 64x64, D = 32 configuration over 50,331,648 rows (HEALPix nside=2048), generated on the device.
+  serve     BMU serving on a resident 64x64, D = 16 map: Poisson arrivals, request sizes log-uniform in [1e3, 1e7].
   cpu_baseline  the reference's CPU formulation (oracle port: per-sample scatter into every unit with float32
-          atomics, then the error pass) on all host cores, on a bounded prefix of the catalogue.
+            atomics, then the error pass) on all host cores, on a bounded prefix of the catalogue.
 
-`--impl reference` times only that CPU formulation (rank 0), each step a bounded sample, and prints its line.
-Under torchrun every rank runs an independent replica (the path is data-parallel; this build keeps one GPU per
-replica and no collective) and value = units processed by all ranks / max time.
+`--impl reference` times only that CPU formulation (rank 0), each step a bounded prefix of the workload, and prints
+its line. `--serve` prints the serving record alone. Under torchrun every rank runs an independent replica (the path is
+data-parallel; this build keeps one GPU per replica and no collective) and value = units processed by all ranks / max
+time.
 """
 
 import argparse
@@ -34,24 +41,25 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = dict(name='hex 32x32 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=16, 20-epoch schedule',
-                m=32, n=32, d=16, N=12_582_912, topology='hexagonal', sigma0=16.0, schedule=20, seed=2)
-# the larger training configuration (square 64x64 map, D = 32, N = 50,331,648 = HEALPix nside 2048), measured with
-# --workload sq64, and the 64x64, D = 16 map over the default catalogue (--workload sq64d16)
-WORKLOADS = {'hex32': WORKLOAD,
-             'sq64': dict(name='square 64x64 SOM, D=32, N=50331648 (HEALPix nside=2048 pixel count), sigma0=32, '
-                               '20-epoch schedule', m=64, n=64, d=32, N=50_331_648, topology='square', sigma0=32.0,
-                          schedule=20, seed=3),
-             # the speed-up target's shape: a 64x64 map with D = 16 over the 12.6 M-row catalogue
-             'sq64d16': dict(name='square 64x64 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=32, '
-                                  '20-epoch schedule', m=64, n=64, d=16, N=12_582_912, topology='square', sigma0=32.0,
-                             schedule=20, seed=2)}
+WORKLOADS = {
+    # the speed-up target's shape: a 64x64 map with D = 16 over the 12.6 M-row catalogue
+    'sq64d16': dict(name='square 64x64 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=32, '
+                         '20-epoch schedule', m=64, n=64, d=16, N=12_582_912, topology='square', sigma0=32.0,
+                    schedule=20, seed=2),
+    # the plain-FP32 training configuration's shape: hexagonal 32x32, D = 16, same catalogue
+    'hex32': dict(name='hex 32x32 SOM, D=16, N=12582912 (HEALPix nside=1024 pixel count), sigma0=16, 20-epoch schedule',
+                  m=32, n=32, d=16, N=12_582_912, topology='hexagonal', sigma0=16.0, schedule=20, seed=2),
+    # the split-precision configuration: square 64x64, D = 32, N = 50,331,648 (HEALPix nside 2048)
+    'sq64': dict(name='square 64x64 SOM, D=32, N=50331648 (HEALPix nside=2048 pixel count), sigma0=32, '
+                      '20-epoch schedule', m=64, n=64, d=32, N=50_331_648, topology='square', sigma0=32.0,
+                 schedule=20, seed=3),
+}
 METRIC = 'SOM epoch Gsample·unit/s'
-# DRAM traffic (bytes read + written) of one tensor-core BMU pass per catalogue row, from an ncu capture of
-# tc_pass_kernel on the 4,194,304-row case of this workload (summary under profiles/). The pass streams every row
-# once (64 B of samples, 4 B of BMU, unit operand from L2), so the traffic of a full launch scales with N.
-K1_DRAM_BYTES_PER_ROW = 67.84
 UNIT = 'Gsample·unit/s'
+# DRAM traffic (bytes read + written) of one tensor-core BMU pass per catalogue row, from ncu captures of tc_pass_kernel
+# on 4,194,304-row cases of each workload (summaries under profiles/). The pass streams every row once (the samples,
+# the BMU, the unit operand from L2), so the traffic of a full launch scales with N.
+K1_DRAM_BYTES_PER_ROW = {}
 
 
 def parse():
@@ -61,16 +69,19 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--algo', default='auto', choices=['auto', 'tc', 'fp32'])
-    ap.add_argument('--workload', default='hex32', choices=sorted(WORKLOADS),
-                    help='hex32: the headline epoch (default); sq64: the 64x64, D = 32 training configuration')
+    ap.add_argument('--workload', default='sq64d16', choices=sorted(WORKLOADS))
     ap.add_argument('--n', type=int, default=None, help='catalogue rows (default: the full workload)')
     ap.add_argument('--skip-cpu', action='store_true')
     ap.add_argument('--skip-e2e', action='store_true')
     ap.add_argument('--skip-fp32', action='store_true')
+    ap.add_argument('--skip-parity', action='store_true')
+    ap.add_argument('--skip-sq64', action='store_true', help='no 64x64, D = 32, 50.3 M-row sub-record')
+    ap.add_argument('--skip-serve', action='store_true', help='no serving sub-record')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
-    ap.add_argument('--serve', action='store_true',
-                    help='BMU-serving latency instead of the epoch: 64x64x16 map, Poisson arrivals, mixed sizes')
-    ap.add_argument('--serve-seconds', type=float, default=5.0, help='arrival window of the serving run')
+    ap.add_argument('--clock-seconds', type=float, default=2.0,
+                    help='the epochs also run this long after the timed ones while the clocks are sampled')
+    ap.add_argument('--serve', action='store_true', help='print the BMU-serving record alone')
+    ap.add_argument('--serve-seconds', type=float, default=10.0, help='arrival window of the serving run')
     ap.add_argument('--serve-rate', type=float, default=200.0, help='mean request arrivals per second')
     return ap.parse_args()
 
@@ -181,9 +192,8 @@ def make_data(N, w):
 # ----------------------------------------------------------------------------------------------------------------------
 
 def cpu_epoch_rate(x, w0, w, seconds, threads=0):
-    """Times reference-formulation epochs (scatter with float32 atomics + error pass) on a prefix of x.
-
-    Returns (Gsample.unit/s, samples used, threads)."""
+    """Times one reference-formulation epoch (scatter with float32 atomics + error pass) on a prefix of x sized to
+    take about `seconds`. Returns (Gsample.unit/s, prefix rows, threads, seconds measured)."""
     from oracle import somref
     M, D = w['m'] * w['n'], w['d']
     topo = somref.topography(w['m'], w['n'], w['topology'])
@@ -210,27 +220,37 @@ def cpu_epoch_rate(x, w0, w, seconds, threads=0):
 
 
 def reference_arm(args, ws, rank):
+    """The reference's CPU formulation on rank 0: each step one epoch over a prefix of the workload's catalogue; the
+    line reports the measured time of those steps (the prefix rows are named in `config`)."""
     w = WORKLOADS[args.workload]
     if rank != 0:
         return
     x, w0 = make_data(min(args.n or w['N'], 400_000), w)
-    rates = []
-    info = None
+    M = w['m'] * w['n']
+    rates, secs, rows = [], [], None
+    nt = None
+    t_start = time.perf_counter()
     for step in range(args.warmup + args.steps):
-        r, ns, nt, dt = cpu_epoch_rate(x, w0, w, seconds=4.0)
+        r, ns, nt, dt = cpu_epoch_rate(x, w0, w, seconds=2.0)
         if step >= args.warmup:
             rates.append(r)
-            info = (ns, nt)
+            secs.append(dt)
+            rows = ns
+    wall = time.perf_counter() - t_start
     value = statistics.median(rates)
+    ms = statistics.median(secs) * 1e3
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': args.gpus, 'steps': args.steps,
-        'warmup': args.warmup, 'ms_per_step': w['N'] * w['m'] * w['n'] / (value * 1e9) * 1e3,
-        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-        'config': {'workload': w['name'], 'formulation': 'reference CPU epoch (per-sample scatter, float32 atomics, '
-                                                        'error pass), oracle port in C++/OpenMP'},
-        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': info[1], 'kind': 'port',
-                         'sample': f'first {info[0]} samples of the workload, 1 epoch + error pass per step'},
+        'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32', 'data': 'synthetic',
+        'config': {'workload': w['name'], 'rows_per_step': rows, 'units': M,
+                   'formulation': 'reference CPU epoch (per-sample scatter into every unit with float32 atomics, '
+                                  'then the error pass) as the oracle port in C++/OpenMP; numba, which the reference '
+                                  'compiles it with, is not installed'},
+        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': nt, 'kind': 'port',
+                         'sample': f'first {rows} rows of the workload per step (one epoch and its error pass)'},
         'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'consistency': {'steps_wall_s': wall, 'steps_x_ms_s': (args.warmup + args.steps) * ms * 1e-3},
     }
     print(json.dumps(line), flush=True)
 
@@ -246,7 +266,7 @@ class EpochRunner:
         self.t, self.nat, self.xd, self.topo, self.w, self.dev = torch, native, xd, topo, w, device
         self.M, self.D, self.N = w['m'] * w['n'], w['d'], int(xd.shape[0])
         self.algo = native.ALGOS[algo]
-        self.wcur = torch.from_numpy(w0).to(device)
+        self.wcur = (torch.from_numpy(w0) if isinstance(w0, np.ndarray) else w0).to(device).contiguous()
         self.wnext = torch.empty_like(self.wcur)
         self.S = torch.empty((self.M, self.D), dtype=torch.float64, device=device)
         self.c = torch.empty(self.M, dtype=torch.float64, device=device)
@@ -263,6 +283,10 @@ class EpochRunner:
         nb = int(native.lib().somgb_neighbourhood_grid_workspace_bytes(w['m'], w['n'], self.D))
         self.upd_ws = torch.empty(nb, dtype=torch.uint8, device=device)
         self.epoch = 0
+
+    def sigma(self):
+        e = self.epoch % self.w['schedule']
+        return max(float(np.float32(self.w['sigma0'])) / (1.0 + 2.0 * e / self.w['schedule']), 1e-12)
 
     def step(self, err_slot, timer=None, phases=None):
         t, nat = self.t, self.nat
@@ -284,18 +308,23 @@ class EpochRunner:
                  self.bounds.data_ptr(), self.S.data_ptr(), self.c.data_ptr(), s)
         if phases is not None:
             phases[2].record()
-        e = self.epoch % self.w['schedule']
-        sigma = float(np.float32(self.w['sigma0'])) / (1.0 + 2.0 * e / self.w['schedule'])
         nat.call('somgb_neighbourhood_update_grid', self.S.data_ptr(), self.c.data_ptr(), self.topo.data_ptr(),
-                 self.w['m'], self.w['n'], self.D, max(sigma, 1e-12), self.wnext.data_ptr(), None, None,
+                 self.w['m'], self.w['n'], self.D, self.sigma(), self.wnext.data_ptr(), None, None,
                  self.upd_ws.data_ptr(), self.upd_ws.numel(), s)
         if phases is not None:
             phases[3].record()
         self.wcur, self.wnext = self.wnext, self.wcur
         self.epoch += 1
 
+    def rechecks(self):
+        v = np.zeros(1, dtype=np.int64)
+        self.nat.call('somgb_last_recheck_count', v.ctypes.data, self.t.cuda.current_stream().cuda_stream)
+        return int(v[0])
 
-def time_epochs(torch, runner, warmup, steps):
+
+def time_epochs(torch, runner, warmup, steps, sustain_s=0.0):
+    """W warm-up epochs, then exactly `steps` epochs between two events (each dominant kernel timed too); then, untimed,
+    the same epochs for `sustain_s` seconds more (a window for the clock samples), and one epoch with phase events."""
     errs = torch.zeros((warmup + steps, 3), dtype=torch.float64, device=runner.dev)
     for i in range(warmup):
         runner.step(errs[i])
@@ -313,16 +342,167 @@ def time_epochs(torch, runner, warmup, steps):
     stop.record()
     torch.cuda.synchronize()
     launches = runner.nat.lib().somgb_kernel_launches() - launches0
+    rechecks = runner.rechecks()
     total_ms = start.elapsed_time(stop)
     kernel_ms = [a.elapsed_time(b) for a, b in kt]
-    # one more (untimed) epoch with events between its phases, for the breakdown
-    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     extra = torch.zeros(3, dtype=torch.float64, device=runner.dev)
+    t_end = time.perf_counter() + sustain_s
+    while time.perf_counter() < t_end:
+        runner.step(extra)
+        torch.cuda.synchronize()
+    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     runner.step(extra, phases=ph)
     torch.cuda.synchronize()
     phases = {'bmu_pass_ms': ph[0].elapsed_time(ph[1]), 'accumulate_ms': ph[1].elapsed_time(ph[2]),
               'neighbourhood_update_ms': ph[2].elapsed_time(ph[3])}
-    return total_ms, kernel_ms, launches, errs.cpu().numpy(), phases
+    return total_ms, kernel_ms, launches, errs.cpu().numpy(), phases, rechecks
+
+
+def find_bmus(torch, native, xd, w, algo):
+    N, D = xd.shape
+    M = w.shape[0]
+    out = torch.empty(N, dtype=torch.int32, device=xd.device)
+    nb = native.workspace_bytes(native.OP_FIND_BMUS, N, M, D, native.ALGOS[algo])
+    wsb = torch.empty(nb + 256, dtype=torch.uint8, device=xd.device)
+    native.call('somgb_find_bmus', xd.data_ptr(), N, D, w.data_ptr(), M, native.ALGOS[algo], out.data_ptr(),
+                wsb.data_ptr() + (-wsb.data_ptr()) % 256, nb, torch.cuda.current_stream().cuda_stream)
+    del wsb
+    return out
+
+
+def bmu_check(torch, xd, w, bmu, train=False, chunk=1 << 16):
+    """BMUs of the tensor-core pass on every row against an independent evaluation: float32 GEMM distances find each
+    row's three nearest units, whose distances are then taken in the reference's typing (float32 differences and
+    squares, float64 sum) and ranked by (distance, unit). Rows whose two best reference distances lie within the
+    float32 rounding bound 2 (D + 2) 2^-24 of each other are near-ties: counted, and adjudicated by float64 distances
+    over every unit. A row whose GEMM three do not contain its BMU is scanned in full as well. `train`: BMUs of
+    training semantics (-1 for a row without a valid unit)."""
+    N, D = xd.shape
+    tol = 2.0 * (D + 2) * 2.0 ** -24
+    wd = w.double()
+    wn = (w * w).sum(1)
+    mism = ties = tie_agree = tie_differ = scanned = 0
+    for a in range(0, N, chunk):
+        x = xd[a:a + chunk]
+        dist = (x * x).sum(1, keepdim=True) - 2.0 * (x @ w.T) + wn[None, :]
+        top = torch.topk(dist, 3, dim=1, largest=False).indices                      # (b, 3)
+        t = w[top] - x[:, None, :]                                                    # float32 differences
+        dref = (t * t).double().sum(-1)                                               # float32 squares, float64 sum
+        dref = torch.where(torch.isnan(dref), torch.full_like(dref, float('inf')), dref)
+        order = torch.argsort(top, dim=1)                                            # unit order, then stable by value
+        top = torch.gather(top, 1, order)
+        dref = torch.gather(dref, 1, order)
+        srt = torch.argsort(dref, dim=1, stable=True)
+        d_sorted = torch.gather(dref, 1, srt)
+        b_ref = torch.gather(top, 1, srt)[:, 0].to(torch.int32)
+        b = bmu[a:a + chunk]
+        near = (d_sorted[:, 1] - d_sorted[:, 0]) <= tol * d_sorted[:, 0]
+        in_top = (top == b[:, None].long()).any(1)
+        full = near | ~in_top | ~torch.isfinite(d_sorted[:, 0])
+        ok = (b == b_ref) | full
+        if train:
+            ok = ok | (b < 0)
+        mism += int((~ok).sum().item())
+        idx = torch.nonzero(full & (b >= 0) if train else full).flatten()
+        scanned += int(idx.numel())
+        for k in range(0, int(idx.numel()), 256):
+            # float64 distances over every unit (the adjudication) and the reference-typed argmin (full scan)
+            ii = idx[k:k + 256]
+            xs = x[ii]
+            d64 = ((wd[None, :, :] - xs.double()[:, None, :]) ** 2).sum(-1)
+            b64 = torch.argmin(torch.nan_to_num(d64, nan=float('inf')), dim=1).to(torch.int32)
+            t32 = w[None, :, :] - xs[:, None, :]
+            dr = (t32 * t32).double().sum(-1)
+            b_full = torch.argmin(torch.nan_to_num(dr, nan=float('inf')), dim=1).to(torch.int32)
+            bb = b[ii]
+            mism += int((bb != b_full).sum().item())
+            nt = near[ii]
+            ties += int(nt.sum().item())
+            tie_agree += int(((bb == b64) & nt).sum().item())
+            tie_differ += int(((bb != b64) & nt).sum().item())
+    return {'rows': int(N), 'mismatches_vs_reference_typing': mism, 'near_ties': ties, 'near_tie_tol_rel': tol,
+            'near_ties_fp64_agrees': tie_agree, 'near_ties_fp64_differs': tie_differ, 'rows_scanned_in_full': scanned,
+            'how': 'float32 GEMM top-3 per row, then the reference typing (float32 squares, float64 sum) and '
+                   '(distance, unit) order; near-ties and rows outside the top-3 scanned over every unit; near-ties '
+                   'adjudicated by float64 distances'}
+
+
+def weights_check(torch, runner):
+    """One more epoch of the runner, then its new weights against a float64 evaluation of the same update: the per-BMU
+    sums S, c of the epoch's own BMUs in float64, num = H S and den = H c with the reference's neighbourhood factor
+    h_jb = exp(-|t_j - t_b|^2 / (2 sigma^2)) (|t_j - t_b|^2 typed as the reference: float32 differences and squares,
+    float64 sum), w = num / den where den > 1e-12."""
+    sigma = runner.sigma()
+    extra = torch.zeros(3, dtype=torch.float64, device=runner.dev)
+    runner.step(extra)
+    torch.cuda.synchronize()
+    w32 = runner.wcur.double()
+    keep = runner.bmu >= 0
+    b = runner.bmu[keep].long()
+    S = torch.zeros((runner.M, runner.D), dtype=torch.float64, device=runner.dev)
+    S.index_add_(0, b, runner.xd[keep].double())
+    c = torch.bincount(b, minlength=runner.M).double()
+    s_rel = float(((runner.S - S).abs().max() / S.abs().max().clamp_min(1e-300)).item())
+    t = runner.topo
+    d = t[:, None, :] - t[None, :, :]
+    d2 = (d * d).double().sum(-1)
+    H = torch.exp(-d2 / (2.0 * sigma * sigma))
+    num = H @ S
+    den = H @ c
+    w64 = torch.where(den[:, None] > 1e-12, num / den[:, None], torch.zeros_like(num))
+    rel = (w32 - w64).abs() / w64.abs().clamp_min(1e-30)
+    rel = torch.where(w64 == 0, (w32 - w64).abs(), rel)
+    return {'max_rel': float(rel.max().item()), 'rms_rel': float(rel.pow(2).mean().sqrt().item()),
+            'sums_max_rel': s_rel, 'epoch_sigma': sigma, 'rows': runner.N,
+            'against': 'a float64 evaluation of the same epoch update (float64 per-BMU sums of the same BMUs, '
+                       'pairwise Gaussian contraction, divide)'}
+
+
+def fp32_roofline(N, M, D, ms, clocks):
+    """The plain FP32 form's BMU pass against the nominal FP32 FMA rate of the part (SMs x 128 lanes x 2 flops at the
+    sampled maximum SM clock): algorithmic 2 N M D flops of direct differences."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clocks or {}).get('sm_max_mhz') or 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    ach = 2.0 * N * M * D / (ms * 1e-3) / 1e12
+    return {'achieved': ach, 'peak': peak, 'unit': 'TFLOP/s', 'frac': ach / peak,
+            'peak_source': f'nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 flops x {mhz:.0f} MHz'}
+
+
+def sq64_record(torch, native, device, args):
+    """The 64x64, D = 32 configuration over 50.3 M rows, catalogue generated on the device: tensor-core epochs, the
+    plain FP32 form's epochs, the recheck rate and BMU mismatches between the two forms on the final map."""
+    import decontamination_gb300 as dg
+    from decontamination_gb300 import synthetic
+    w = WORKLOADS['sq64']
+    M, D, N = w['m'] * w['n'], w['d'], w['N']
+    xd = synthetic.correlated_lognormal_device(N, D, w['seed'], device)
+    w0 = synthetic.uniform_weights(M, D, w['seed'])
+    topo = torch.from_numpy(dg.SOM_Batch(w['m'], w['n'], D, topology=w['topology'])._topography).to(device)
+    out = {'workload': w['name'], 'N': N, 'M': M, 'D': D,
+           'data': 'synthetic on the device (the correlated log-normal recipe, torch generator)'}
+    r = EpochRunner(torch, native, xd, w0, topo, w, 'auto', device)
+    total, kms, _, _, ph, rc = time_epochs(torch, r, 2, 3)
+    out.update({'value': N * M / (total / 3 * 1e-3) / 1e9, 'ms_per_step': total / 3, 'bmu_kernel_ms':
+                statistics.mean(kms), 'phases': ph, 'recheck_rows_last_epoch': rc, 'recheck_rate': rc / N})
+    wfin = r.wcur.clone()
+    del r
+    torch.cuda.empty_cache()
+    if not args.skip_fp32:
+        r32 = EpochRunner(torch, native, xd, w0, topo, w, 'fp32', device)
+        t32, k32, _, _, _, _ = time_epochs(torch, r32, 1, 2)
+        del r32
+        out['fp32_form'] = {'value': N * M / (t32 / 2 * 1e-3) / 1e9, 'ms_per_step': t32 / 2,
+                            'bmu_kernel_ms': statistics.mean(k32)}
+        out['speedup_vs_fp32_form'] = out['fp32_form']['ms_per_step'] / out['ms_per_step']
+        b_tc = find_bmus(torch, native, xd, wfin, 'tc')
+        b_32 = find_bmus(torch, native, xd, wfin, 'fp32')
+        out['bmu_mismatches_vs_fp32_form'] = int((b_tc != b_32).sum().item())
+        del b_tc, b_32
+    del xd
+    torch.cuda.empty_cache()
+    return out
 
 
 def gpu_arm(args, ws, rank, local):
@@ -333,6 +513,7 @@ def gpu_arm(args, ws, rank, local):
 
     gbuild.build()
     torch.cuda.set_device(local)
+    torch.backends.cuda.matmul.allow_tf32 = False
     device = torch.device('cuda', local)
     if ws > 1:
         dist.init_process_group('nccl', device_id=device)
@@ -356,13 +537,13 @@ def gpu_arm(args, ws, rank, local):
         args.algo != 'fp32' else 'fp32'
     barrier()
     with ClockSampler(gpu_bus_id(torch, device)) as clk:
-        total_ms, kernel_ms, launches, errs, phases = time_epochs(torch, runner, args.warmup, args.steps)
+        total_ms, kernel_ms, launches, errs, phases, rechecks = time_epochs(torch, runner, args.warmup, args.steps,
+                                                                            args.clock_seconds)
     barrier()
     clocks = clk.summary()
+    clocks['window'] = f'the {args.steps} timed epochs and {args.clock_seconds:.1f} s more of the same epochs'
     ms_per_step = slowest_rank(total_ms, ws, device) / args.steps
     value = whole_job_rate(ws, N, M, ms_per_step)
-    rechecks = np.zeros(1, dtype=np.int64)
-    _native.call('somgb_last_recheck_count', rechecks.ctypes.data, torch.cuda.current_stream().cuda_stream)
 
     # roofline of the dominant kernel (the BMU pass): algorithmic 2*N*M*D flops per launch
     peaks, peak_kind = measured_peaks()
@@ -370,17 +551,18 @@ def gpu_arm(args, ws, rank, local):
     flops = 2.0 * N * M * D
     achieved_tflops = flops / (k_ms * 1e-3) / 1e12
     peak = peaks.get('bf16_tflops_sustained', peaks.get('bf16_tflops'))
+    traffic = K1_DRAM_BYTES_PER_ROW.get(args.workload)
     roofline = {'bound': 'tensor', 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
                 'frac': achieved_tflops / peak,
-                'traffic': K1_DRAM_BYTES_PER_ROW * N if used_algo == 'tc' else None,
+                'traffic': traffic * N if (traffic and used_algo == 'tc') else None,
                 'kernel': 'BMU pass (%s)' % ('tcgen05 split-FP16' if used_algo == 'tc' else 'FP32 CUDA cores'),
                 'kernel_ms': k_ms, 'kernel_share': k_ms * args.steps / total_ms,
                 'peak_source': f'{peak_kind} bf16_tflops_sustained (dense FP16 and BF16 share the rate)',
                 'hbm_bytes_algorithmic': N * D * 4 + N * 4,
                 'hbm_frac': (N * D * 4 + N * 4) / (k_ms * 1e-3) / 1e9 / peaks.get('hbm_gbs', 6800.0)}
     if used_algo == 'tc':
-        # what the tensor pipe actually executes: two sweeps (the second recomputes the MMAs) of the split-FP16
-        # contraction over the padded map, K = 16 x K-steps (lo.hi, hi.lo, hi.hi blocks and the |w|^2 step)
+        # what the tensor pipe executes: two sweeps (the second recomputes the MMAs) of the split-FP16 contraction over
+        # the padded map, K = 16 x K-steps (lo.hi, hi.lo, hi.hi blocks and the |w|^2 step)
         k_steps = 3 * (D // 16) + 1 if D % 16 == 0 else (3 * D + 2 + 15) // 16
         m_pad = (M + 255) // 256 * 256
         executed = 2 * 2.0 * N * m_pad * (16 * k_steps) / (k_ms * 1e-3) / 1e12
@@ -395,50 +577,34 @@ def gpu_arm(args, ws, rank, local):
                    'l2': f'catalogue {N * D * 4 / 1e6:.0f} MB > 129 MB L2 per epoch; no flush',
                    'parallelism': f'replicas x{ws}'},
         'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clocks, 'phases': phases,
-        'recheck_last_epoch': int(rechecks[0]),
+        'recheck_last_epoch': rechecks,
         'qe_last': float(errs[-1][0] / errs[-1][2]) if errs[-1][2] > 0 else None,
     }
 
     # --- plain FP32 form of the same epoch ------------------------------------------------------------------------------
     if not args.skip_fp32 and used_algo == 'tc':
         r32 = EpochRunner(torch, _native, xd, w0, topo, w, 'fp32', device)
-        t32, k32, _, _, ph32 = time_epochs(torch, r32, min(args.warmup, 3), max(3, args.steps // 4))
         n32 = max(3, args.steps // 4)
+        t32, k32, _, _, ph32, _ = time_epochs(torch, r32, min(args.warmup, 3), n32)
+        del r32
         out['fp32_form'] = {'value': N * M / (t32 / n32 * 1e-3) / 1e9, 'ms_per_step': t32 / n32,
-                            'bmu_kernel_ms': statistics.mean(k32), 'phases': ph32}
+                            'bmu_kernel_ms': statistics.mean(k32), 'phases': ph32,
+                            'roofline': fp32_roofline(N, M, D, statistics.mean(k32), clocks)}
         out['speedup_vs_fp32_form'] = out['fp32_form']['ms_per_step'] / ms_per_step
         # matched BMUs: both forms on the tensor-core run's final map, every row of the catalogue
-        b_tc = torch.empty(N, dtype=torch.int32, device=device)
-        b_32 = torch.empty(N, dtype=torch.int32, device=device)
-        for algo_name, dst in (('tc', b_tc), ('fp32', b_32)):
-            nb = _native.workspace_bytes(_native.OP_FIND_BMUS, N, M, D, _native.ALGOS[algo_name])
-            wsb = torch.empty(nb + 256, dtype=torch.uint8, device=device)
-            _native.call('somgb_find_bmus', xd.data_ptr(), N, D, runner.wcur.data_ptr(), M, _native.ALGOS[algo_name],
-                         dst.data_ptr(), wsb.data_ptr() + (-wsb.data_ptr()) % 256, nb,
-                         torch.cuda.current_stream().cuda_stream)
-            del wsb
+        b_tc = find_bmus(torch, _native, xd, runner.wcur, 'tc')
+        b_32 = find_bmus(torch, _native, xd, runner.wcur, 'fp32')
         out['fp32_form']['bmu_mismatches'] = int((b_tc != b_32).sum().item())
         out['fp32_form']['bmu_rows_compared'] = N
         del b_tc, b_32
 
-    # --- trained weights against the same training on a float64 map (this library's float64 path): the difference
-    #     includes the two typings' different BMUs at near-ties, so it bounds, not measures, the float32 path's error ---
-    if not args.skip_fp32:
-        sub = min(N, 200_000)
-        e_w = 3
-        errs64 = {}
-        maps = {}
-        for dt_ in (np.float32, np.float64):
-            som_ = dg.SOM_Batch(w['m'], w['n'], D, dtype=dt_, topology=w['topology'], sigma=w['sigma0'])
-            som_.bmu_algo = args.algo
-            som_._weights[...] = w0.astype(dt_)
-            som_.train(x[:sub].astype(dt_), n_epochs=e_w, use_best_epoch=False)
-            maps[dt_] = som_.weights.reshape(-1, D).astype(np.float64)
-        rel = np.abs(maps[np.float32] - maps[np.float64]) / np.maximum(np.abs(maps[np.float64]), 1e-6)
-        out['weights_vs_fp64'] = {'max_rel': float(rel.max()), 'rms_rel': float(np.sqrt(np.mean(rel ** 2))),
-                                  'rows': sub, 'epochs': e_w,
-                                  'against': 'the same training on a float64 map (float64 distances, so BMUs at '
-                                             'near-ties can differ from the float32 typing)'}
+    # --- parity at full size: BMUs against an independent evaluation, weights against float64 ---------------------------
+    if not args.skip_parity:
+        b = find_bmus(torch, _native, xd, runner.wcur, args.algo)
+        out['parity'] = {'bmu': bmu_check(torch, xd, runner.wcur, b)}
+        del b
+        out['parity']['weights'] = weights_check(torch, runner)
+        torch.cuda.empty_cache()
 
     # --- end to end through the public API ------------------------------------------------------------------------------
     if not args.skip_e2e:
@@ -460,12 +626,23 @@ def gpu_arm(args, ws, rank, local):
                       'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3,
                       'call': 'SOM_Batch.train(pinned host tensor, n_epochs=1): upload, training pass, error pass, '
                               'weights/history/errors back to the host'}
+        del som
+
+    del runner, xd
+    torch.cuda.empty_cache()
+    # --- the 64x64, D = 32 configuration (rank 0, one GPU) ---------------------------------------------------------------
+    if not args.skip_sq64 and rank == 0 and ws == 1 and args.n is None:
+        out['sq64'] = sq64_record(torch, _native, device, args)
+
+    # --- BMU serving (rank 0, one GPU) ----------------------------------------------------------------------------------
+    if not args.skip_serve and rank == 0 and ws == 1:
+        out['serve'] = serve_record(args)
 
     # --- CPU baseline (rank 0, N=1) -------------------------------------------------------------------------------------
     if not args.skip_cpu and rank == 0 and ws == 1:
         r, ns, nt, dt = cpu_epoch_rate(x, w0, w, seconds=args.cpu_seconds)
         out['cpu_baseline'] = {'value': r, 'unit': UNIT, 'cores': nt, 'kind': 'port',
-                               'sample': f'first {ns} samples of the workload, one reference-formulation epoch '
+                               'sample': f'first {ns} rows of the workload, one reference-formulation epoch '
                                          f'(scatter + float32 atomics) and its error pass, {dt:.1f} s'}
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -482,7 +659,7 @@ SERVE = dict(name='BMU serving: square 64x64 map (M = 4096), D = 16, Poisson arr
                   'in [1e3, 1e7] rows', m=64, n=64, d=16, seed=4, pool=10_000_000, lo=1_000, hi=10_000_000)
 
 
-def serve_arm(args):
+def serve_record(args):
     """Requests arrive as a Poisson process and are submitted to SomServer as slices of a pinned host catalogue;
     latency is submit to result on the host. The map is trained once (3 epochs on 500k rows) before the clock runs."""
     import threading
@@ -530,20 +707,22 @@ def serve_arm(args):
     lat = np.asarray(srv.latencies('bmu')[3:]) * 1e3
     rows = int(sizes.sum())
     wall = t_end - t0
-    out = {
-        'metric': 'BMU-serve latency p99', 'value': float(np.percentile(lat, 99)), 'unit': 'ms',
-        'higher_is_better': False, 'n_gpus': 1, 'p50_ms': float(np.percentile(lat, 50)),
-        'p99_ms': float(np.percentile(lat, 99)), 'mean_ms': float(lat.mean()), 'requests': n_req,
-        'rows': rows, 'wall_s': wall,
+    return {
+        'workload': s['name'], 'p50_ms': float(np.percentile(lat, 50)), 'p99_ms': float(np.percentile(lat, 99)),
+        'mean_ms': float(lat.mean()), 'requests': n_req, 'rows': rows, 'wall_s': wall,
         'throughput': {'value': rows * M / wall / 1e9, 'unit': UNIT},
         'offered': {'requests_per_s': args.serve_rate, 'sample_units_per_s': rows * M / args.serve_seconds / 1e9,
-                    'unit': UNIT},
-        'passes': len(srv.batch_sizes()), 'dtype': 'f16x3-split/f32acc' if algo_used == 'tc' else 'f32',
+                    'unit': UNIT, 'window_s': args.serve_seconds},
+        'passes': len(srv.batch_sizes()), 'algo': algo_used, 'workers': srv.workers, 'max_batch_rows': 1 << 20,
+        'returns': 'int32 BMUs + M-bin activation histogram per request',
         'data': 'synthetic (seeded 5-component Gaussian mixture, D = 16); requests are slices of a pinned 1e7-row '
-                'catalogue', 'config': {'workload': s['name'], 'algo': algo_used, 'rate': args.serve_rate,
-                                         'window_s': args.serve_seconds, 'max_batch_rows': 1 << 20,
-                                         'workers': srv.workers, 'returns': 'int32 BMUs + M-bin activation histogram'},
-    }
+                'catalogue'}
+
+
+def serve_arm(args):
+    r = serve_record(args)
+    out = {'metric': 'BMU-serve latency p99', 'value': r['p99_ms'], 'unit': 'ms', 'higher_is_better': False,
+           'n_gpus': 1, **r}
     print(json.dumps(out), flush=True)
 
 

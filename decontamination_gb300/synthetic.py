@@ -70,3 +70,24 @@ def correlated_lognormal(n, d, seed, scale=0.3, outlier_frac=0.02, outlier_scale
 
 def uniform_weights(m, d, seed, low=-1.0, high=1.0):
     return np.random.default_rng([seed, 3]).uniform(low, high, size=(m, d)).astype(np.float32)
+
+
+def correlated_lognormal_device(n, d, seed, device, scale=0.3, outlier_frac=0.02, outlier_scale=10.0,
+                                chunk=1 << 22):
+    """The recipe of ``correlated_lognormal`` generated on the device (a torch float32 tensor), for catalogues too
+    large to generate and copy from the host in a benchmark's time: the same correlation factor L, the same
+    log-normal transform and outlier fraction, with torch's seeded generator in place of numpy's streams (so the
+    values differ from ``correlated_lognormal``'s, the distribution does not)."""
+    import torch
+    L = torch.from_numpy(correlation_cholesky(d, seed).T.copy()).to(device=device, dtype=torch.float32)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed) * 1000003 + 17)
+    out = torch.empty((n, d), dtype=torch.float32, device=device)
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        z = torch.randn((e - s, d), generator=g, device=device, dtype=torch.float32) @ L
+        x = torch.exp(scale * z)
+        mask = torch.rand(e - s, generator=g, device=device) < outlier_frac
+        x[mask] *= outlier_scale
+        out[s:e] = x
+    return out
