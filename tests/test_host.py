@@ -80,6 +80,99 @@ def test_hdf5_round_trip(tmp_path):
     assert np.array_equal(other.weights, som.weights)
 
 
+class _FakeH5:
+    """A stand-in for the h5py module (absent here): File objects over an in-memory store that records groups,
+    attributes and datasets the way h5py returns them (numbers as numpy scalars, arrays as arrays)."""
+
+    files = {}
+
+    class Group(dict):
+        def __init__(self):
+            super().__init__()
+            self.attrs = _FakeH5.Attrs()
+
+        def create_group(self, name, track_order=None):
+            g = _FakeH5.Group()
+            self[name] = g
+            return g
+
+        def create_dataset(self, name, data, shape, dtype):
+            arr = np.array(data, dtype=dtype).reshape(shape)
+            self[name] = arr
+            return arr
+
+    class Attrs(dict):
+        def __setitem__(self, k, v):
+            if isinstance(v, bool):
+                v = np.bool_(v)
+            elif isinstance(v, (int, np.integer)):
+                v = np.int64(v)
+            elif isinstance(v, (float, np.floating)):
+                v = np.float64(v)
+            super().__setitem__(k, v)
+
+    class File:
+        def __init__(self, filename, mode='r'):
+            if mode == 'w':
+                _FakeH5.files[filename] = _FakeH5.Group()
+            self.root = _FakeH5.files[filename]
+
+        def __enter__(self):
+            return self.root
+
+        def __exit__(self, *exc):
+            return False
+
+
+@pytest.fixture
+def fake_h5py(monkeypatch):
+    import sys
+    import types
+    mod = types.ModuleType('h5py')
+    mod.File = _FakeH5.File
+    monkeypatch.setitem(sys.modules, 'h5py', mod)
+    _FakeH5.files.clear()
+    return _FakeH5
+
+
+def test_hdf5_layout_and_round_trip_without_h5py(fake_h5py):
+    """The reference's HDF5 layout (algo/som_abstract.py:188-319, algo/som_batch.py:75-81, algo/som_pca.py:78-84):
+    one group 'model' whose attributes are the header fields and whose datasets are the weights and error
+    histories; saving and loading gives the same model back."""
+    som = dg.SOM_Batch(3, 4, 2, topology='square', sigma=1.5)
+    som.init_rand(2)
+    som._n_epochs = 7
+    som._quantization_errors = np.array([0.5, 0.25])
+    som._topographic_errors = np.array([0.1, 0.05])
+    som.save('som.h5')
+    g = fake_h5py.files['som.h5']['model']
+    assert set(g.attrs) == {'mode', 'sigma', 'n_epochs', 'n_vectors', 'm', 'n', 'dim', 'topology'}
+    assert set(g) == {'weights', 'quantization_errors', 'topographic_errors'}
+    assert g.attrs['mode'] == 'batch' and g.attrs['topology'] == 'square' and g.attrs['m'] == 3
+    assert g['weights'].dtype == np.float32 and g['weights'].shape == som._weights.shape
+    other = dg.SOM_Batch(1, 1, 1)
+    other.load('som.h5')
+    assert (other.m, other.n, other.dim, other.topology, other.sigma) == (3, 4, 2, 'square', 1.5)
+    assert other._n_epochs == 7 and other._n_vectors == 0
+    assert np.array_equal(other.weights, som.weights)
+    # every dataset comes back in the map's dtype, as the reference casts it (algo/som_abstract.py:307-309)
+    assert other.quantization_errors.dtype == np.float32
+    assert np.array_equal(other.quantization_errors, som.quantization_errors.astype(np.float32))
+    assert np.array_equal(other.topographic_errors, som.topographic_errors.astype(np.float32))
+    assert other._topography.shape == (12, 2)          # rebuilt for the loaded grid
+
+    pca = dg.SOM_PCA(4, 5, 3, topology='hexagonal')
+    pca.init_rand(3)
+    pca.save('pca.h5')
+    g = fake_h5py.files['pca.h5']['model']
+    assert set(g.attrs) == {'mode', 'scale_by_variance', 'apply_cdf', 'cdf_gain', 'm', 'n', 'dim', 'topology'}
+    assert g.attrs['mode'] == 'pca'
+    back = dg.SOM_PCA(1, 1, 2)
+    back.load('pca.h5')
+    assert (back.m, back.n, back.dim, back.topology) == (4, 5, 3, 'hexagonal')
+    assert np.array_equal(back.weights, pca.weights)
+
+
 @pytest.mark.parametrize('n', [2 * _dataset.PIECE_ROWS, 2 * _dataset.PIECE_ROWS + 7, 3 * _dataset.PIECE_ROWS - 1,
                                12_582_912, 12_582_912 + 13, 50_331_648, 7 * _dataset.PIECE_ROWS + 1])
 def test_piece_edges_cover_the_chunk(n):
