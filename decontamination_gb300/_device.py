@@ -48,6 +48,7 @@ class Workspace:
 
     def __init__(self):
         self._buf = None
+        self._off = 0
 
     def get(self, nbytes, device=None):
         device = device or require_cuda()
@@ -55,11 +56,38 @@ class Workspace:
         if self._buf is None or self._buf.numel() < nbytes or self._buf.device != device:
             self._buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
         base = self._buf.data_ptr()
-        off = (-base) % 256
-        return base + off, self._buf.numel() - off
+        self._off = (-base) % 256
+        return base + self._off, self._buf.numel() - self._off
 
     def for_op(self, op, n, m, d, algo, device=None):
         return self.get(_native.workspace_bytes(op, n, m, d, algo), device)
+
+    def status_word(self):
+        """The status word of the last pass that used this workspace (a one-element int32 device tensor; non-zero
+        when a bounded device-side wait of that pass gave up). Each pass clears it when it starts."""
+        return self._buf[self._off + 8:self._off + 12].view(torch.int32)
+
+    def note_status(self, acc):
+        """ORs the last pass's status word into `acc` on the device, in stream order (no synchronisation)."""
+        if self._buf is not None:
+            acc.bitwise_or_(self.status_word())
+
+
+class StatusCheck:
+    """The status words of every pass of one API call, OR-ed on the device and checked once at its end, so that a
+    wait that gave up in this call fails this call and no other (concurrent calls use their own workspaces)."""
+
+    def __init__(self, device):
+        self.acc = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def note(self, ws):
+        ws.note_status(self.acc)
+
+    def check(self):
+        v = int(self.acc.item())
+        if v:
+            raise _native.SomgbError(_native.SOMGB_ERR_TIMEOUT,
+                                     f'a device-side wait gave up (status {v:#x}); results are incomplete')
 
 
 def rows(x):

@@ -152,6 +152,9 @@ class GpuExecutor:
                 hh = ob[n * 4 + (-(n * 4)) % 8:][:nh * M * 8].view(torch.float64).view(nh, M)
                 hh.copy_(hd[:nh], non_blocking=True)
         sl.stream.synchronize()
+        if n and int(entry['ws'][slot].status_word().item()):
+            # a bounded wait of this pass gave up: this batch fails, and no other (the word is this workspace's)
+            raise nat.SomgbError(nat.SOMGB_ERR_TIMEOUT, 'a device-side wait gave up; the pass returned early')
         res = oh.numpy().copy()
         hres = hh.numpy().copy() if nh else None
         parts, r, k = [], 0, 0

@@ -226,15 +226,6 @@ class SOM_Abstract(object):
         _native.call('somgb_last_recheck_count', cnt.ctypes.data, _device.stream())
         self._last_recheck_count = int(cnt[0])
 
-    @staticmethod
-    def _check_device():
-        """Raises if a bounded device-side wait gave up during the calls since the last check."""
-        st = ctypes.c_uint(0)
-        _native.call('somgb_device_status', ctypes.addressof(st), 1, _device.stream())
-        if st.value:
-            raise _native.SomgbError(_native.SOMGB_ERR_TIMEOUT,
-                                     f'a device-side wait gave up (status {st.value:#x}); results are incomplete')
-
     # -- projection calls -------------------------------------------------------------------------------------------------
 
     def compute_errors(self, dataset, dataset_weights=None, show_progress_bar: bool = False, enable_gpu: bool = True,
@@ -247,6 +238,7 @@ class SOM_Abstract(object):
         w = self._device_weights()
         topo = self._device_topography()
         M, D = self._m * self._n, self._dim
+        status = _device.StatusCheck(device)
         for xc, rc in iterate_pieces(dataset, dataset_weights, self._dtype, device):
             n = _device.rows(xc)
             if self._is_f64:
@@ -257,8 +249,9 @@ class SOM_Abstract(object):
                 _native.call('somgb_compute_errors', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
                              topo.data_ptr(), M, self._penalty, self._algo, out.data_ptr(), wsp, wsb,
                              _device.stream())
+                status.note(self._ws)
         o = out.cpu().numpy()
-        self._check_device()
+        status.check()
         return (o[0] / o[2], o[1] / o[2]) if o[2] > 0.0 else (np.nan, np.nan)
 
     def get_activation_map(self, dataset, dataset_weights=None, show_progress_bar: bool = False,
@@ -268,6 +261,7 @@ class SOM_Abstract(object):
         M, D = self._m * self._n, self._dim
         hist = torch.zeros(M, dtype=torch.float64, device=device)
         w = self._device_weights()
+        status = _device.StatusCheck(device)
         for xc, rc in iterate_pieces(dataset, dataset_weights, self._dtype, device):
             n = _device.rows(xc)
             if self._is_f64:
@@ -277,8 +271,9 @@ class SOM_Abstract(object):
                 wsp, wsb = self._ws.for_op(_native.OP_COUNT_BMUS, n, M, D, self._algo, device)
                 _native.call('somgb_count_bmus', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), M, self._algo,
                              hist.data_ptr(), wsp, wsb, _device.stream())
+                status.note(self._ws)
         h = hist.cpu().numpy()
-        self._check_device()
+        status.check()
         return h.astype(self._dtype).reshape((self._m, self._n))
 
     def get_footprint_maps(self, dataset, dataset_weights=None) -> typing.Tuple[np.ndarray, np.ndarray, np.ndarray]:
@@ -294,6 +289,7 @@ class SOM_Abstract(object):
         hist_w = torch.zeros(M, dtype=torch.float64, device=device)
         hist_c = torch.zeros(M, dtype=torch.float64, device=device)
         w = self._device_weights()
+        status = _device.StatusCheck(device)
         for a, b in pieces:
             xp, op = x[a:b], winners[a:b]
             rp = None if rho is None else rho[a:b]
@@ -305,10 +301,11 @@ class SOM_Abstract(object):
                 _native.call('somgb_footprint_maps', xp.data_ptr(), _device.ptr(rp), b - a, D, w.data_ptr(), M,
                              self._algo, op.data_ptr(), hist_w.data_ptr(), hist_c.data_ptr(), wsp, wsb,
                              _device.stream())
+                status.note(self._ws)
         cat = hist_w.cpu().numpy().astype(self._dtype).reshape((self._m, self._n))
         foot = hist_c.cpu().numpy().astype(self._dtype).reshape((self._m, self._n))
         res = winners.cpu().numpy()
-        self._check_device()
+        status.check()
         return cat, foot, res
 
     def get_winners(self, dataset, enable_gpu: bool = True,
@@ -319,6 +316,7 @@ class SOM_Abstract(object):
         x, _, pieces = device_pieces(dataset, None, self._dtype, device)
         out = torch.empty(_device.rows(x), dtype=torch.int32, device=device)
         w = self._device_weights()
+        status = _device.StatusCheck(device)
         for a, b in pieces:
             xp, op = x[a:b], out[a:b]
             if self._is_f64:
@@ -328,8 +326,9 @@ class SOM_Abstract(object):
                 wsp, wsb = self._ws.for_op(_native.OP_FIND_BMUS, b - a, M, D, self._algo, device)
                 _native.call('somgb_find_bmus', xp.data_ptr(), b - a, D, w.data_ptr(), M, self._algo, op.data_ptr(),
                              wsp, wsb, _device.stream())
+                status.note(self._ws)
         if not self._is_f64:
             self._record_recheck()
         res = out.cpu().numpy()
-        self._check_device()
+        status.check()
         return res

@@ -115,6 +115,7 @@ class SOM_Batch(SOM_Abstract):
         M, D = self._m * self._n, self._dim
         xc, rc = xd[a:b], (None if rd is None else rd[a:b])
         n = b - a
+        status = self._status
         if last:
             if not with_errors:
                 return
@@ -126,6 +127,7 @@ class SOM_Batch(SOM_Abstract):
                 _native.call('somgb_compute_errors', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(),
                              topo.data_ptr(), M, self._penalty, self._algo, err.data_ptr(), wsp, wsb,
                              _device.stream())
+                status.note(self._ws)
             return
         if self._is_f64:
             return
@@ -134,6 +136,7 @@ class SOM_Batch(SOM_Abstract):
         _native.call('somgb_train_bmu_pass', xc.data_ptr(), _device.ptr(rc), n, D, w.data_ptr(), topo.data_ptr(), M,
                      self._penalty, self._algo, bmu.data_ptr(), _device.ptr(err if e > 0 else None), wsp, wsb,
                      _device.stream())
+        status.note(self._ws)
 
     def _accumulate(self, xd, rd, bounds, S, c, w, topo, err):
         """The per-BMU sums of a whole chunk after its BMU passes (float64 maps: the fused float64 epoch pass, with
@@ -197,6 +200,7 @@ class SOM_Batch(SOM_Abstract):
         with_errors = M >= 2   # compute_errors returns (nan, nan) below two units (som_abstract.py:547-549)
 
         chunks = self._chunk_source(dataset, dataset_weights, device)
+        self._status = _device.StatusCheck(device)
         topo = self._device_topography()
         w = self._device_weights()
         history = torch.empty((n_epochs, M, D), dtype=td, device=device)
@@ -247,7 +251,7 @@ class SOM_Batch(SOM_Abstract):
             for e in range(done):
                 self._quantization_errors[e], self._topographic_errors[e] = self._errors_of(eh[e + 1])
         self._weights[:] = history[done - 1].cpu().numpy() if done > 0 else self._weights
-        self._check_device()
+        self._status.check()
 
     def _train_vectors(self, dataset, dataset_weights, n_vectors):
         device = _device.require_cuda()

@@ -97,3 +97,31 @@ def test_debug_hook_arguments_are_checked(native):
         native.call('somgb_debug_tc_withhold', -1, 100)
     with pytest.raises(native.SomgbError):
         native.call('somgb_debug_tc_withhold', 0, 0)
+
+
+def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
+    """The serving executor and the API methods read the status word of their own workspace: the pass whose wait ran
+    out raises, the same request on the other worker's slot and the next calls give the normal results."""
+    import decontamination_gb300 as dg
+    from decontamination_gb300.serve import GpuExecutor
+    rng = np.random.default_rng(14)
+    N, d = 200_000, 16
+    x = synthetic.correlated_lognormal(N, d, 9)
+    som = dg.SOM_Batch(32, 32, d, topology='square')
+    som._weights[...] = x[rng.integers(0, N, 1024)].reshape(som._weights.shape)
+    som.bmu_algo = 'tc'
+    ex = GpuExecutor(workers=2)
+    entry = ex.load(som)
+    want = ex.run_bmu(entry, [x], slot=1)[0]
+    native.call('somgb_debug_tc_withhold', 3, 20_000)
+    with pytest.raises(native.SomgbError) as ei:
+        ex.run_bmu(entry, [x], slot=0)
+    assert ei.value.status == native.SOMGB_ERR_TIMEOUT
+    assert np.array_equal(ex.run_bmu(entry, [x], slot=1)[0], want)
+    assert np.array_equal(ex.run_bmu(entry, [x], slot=0)[0], want)
+    native.call('somgb_debug_tc_withhold', 2, 20_000)
+    with pytest.raises(native.SomgbError):
+        som.get_winners(x)
+    assert np.array_equal(som.get_winners(x), want)
+    st = ctypes.c_uint(0)
+    native.call('somgb_device_status', ctypes.addressof(st), 1, torch.cuda.current_stream().cuda_stream)

@@ -123,6 +123,26 @@ def test_a_failing_request_fails_alone():
     assert 'bmu' in srv.stats() and srv.stats()['bmu']['count'] == 2
 
 
+def test_a_device_timeout_fails_only_its_own_request():
+    """An executor pass whose device-side wait ran out raises a timeout status (the executor reads its own
+    workspace's status word): that request's future gets the error, the others their results."""
+    from decontamination_gb300 import _native
+
+    class TimingOut(FakeExecutor):
+        def run_bmu(self, entry, xs, slot=0, hist=None):
+            if any(np.asarray(x)[0, 0] == 13 for x in xs):
+                raise _native.SomgbError(_native.SOMGB_ERR_TIMEOUT, 'a device-side wait gave up')
+            return super().run_bmu(entry, xs, slot, hist)
+
+    with SomServer(executor=TimingOut(), max_batch_rows=10, workers=1) as srv:
+        mid = srv.add_map('m')
+        futs = [srv.submit_bmu(mid, _req(v)) for v in (1, 13, 2)]
+        assert np.all(futs[0].result(5) == 1) and np.all(futs[2].result(5) == 2)
+        with pytest.raises(_native.SomgbError) as ei:
+            futs[1].result(5)
+        assert ei.value.status == _native.SOMGB_ERR_TIMEOUT
+
+
 def test_other_kinds_training_and_stats():
     ex = FakeExecutor()
     with SomServer(ex) as srv:
