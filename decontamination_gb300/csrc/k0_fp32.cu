@@ -375,8 +375,10 @@ __global__ void __launch_bounds__(K0_THREADS) k0_rows_block_kernel(PassArgs a, c
 
 template <int DMAX>
 int launch_rows(const PassArgs& a, const int32_t* rows, const unsigned long long* count, cudaStream_t stream) {
-    // the list length is known on the device only: both kernels launch and the one whose range it is in runs
-    const long long split = (long long)num_sms() * K0_THREADS;   // one 128-row turn per SM
+    // the list length is known on the device only: both kernels launch and the one whose range it is in runs. Above
+    // a thousand rows the block form wins: its rows share each unit tile through shared memory, where a warp per row
+    // reads the whole map from L2 for every row.
+    const long long split = 1024;
     const dim3 grid((unsigned)(4 * num_sms())), bgrid((unsigned)(2 * num_sms()));
     if (a.outs & OUT_ERR) {
         k0_rows_kernel<DMAX, true><<<grid, KR_THREADS, 0, stream>>>(a, rows, count, split - 1);

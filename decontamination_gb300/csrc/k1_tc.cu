@@ -293,51 +293,56 @@ void tc_error_coefficients(int d, float* alpha, float* beta) {
 // ---------------------------------------------------------------------------------------------------------------------
 
 // Mean of the finite unit rows, per feature, in float64; then center[d] = the power-of-two scale S that puts the
-// largest |w - c| coordinate of those rows in [2^5, 2^6). One CTA: warps stride over units, lanes over features
-// (d <= 64: two per lane), so every row is read once, coalesced, per pass.
+// largest |w - c| coordinate of those rows in [2^5, 2^6). One CTA, three coalesced passes over the m x d values
+// (d divides the block, so thread t always holds feature t % d): rows with a non-finite value are marked in a shared
+// bitmap, then the finite rows are summed per feature (each thread its own float64 sum, combined per feature), then
+// their largest scaled deviation is taken. Any centre keeps the pass exact (the error bound holds for every centre);
+// a central one keeps the bound tight.
 constexpr int CENTER_THREADS = 1024;
+constexpr int CENTER_MAXM = 16384;   // the largest map of the tensor-core pass (rows of the shared bitmap)
 __global__ void __launch_bounds__(CENTER_THREADS) tc_center_kernel(const float* __restrict__ w, int64_t m, int d,
                                                                    float* __restrict__ center) {
-    constexpr int NW = CENTER_THREADS / 32;
-    __shared__ double part[NW][64];
-    __shared__ unsigned long long cnt_w[NW];
-    __shared__ unsigned int maxbits_s;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool k0 = lane < d, k1 = lane + 32 < d;
-    if (threadIdx.x == 0) maxbits_s = 0u;
-    double s0 = 0.0, s1 = 0.0;
-    unsigned long long c = 0;
-    for (int64_t j = warp; j < m; j += NW) {
-        const float v0 = k0 ? w[j * d + lane] : 0.0f, v1 = k1 ? w[j * d + lane + 32] : 0.0f;
-        if (__all_sync(0xffffffffu, isfinite(v0) && isfinite(v1))) {
-            s0 += (double)v0;
-            s1 += (double)v1;
-            ++c;
-        }
+    __shared__ uint32_t bad[CENTER_MAXM / 32];
+    __shared__ double part[CENTER_THREADS];
+    __shared__ unsigned int nvalid_s, maxbits_s;
+    const int tid = threadIdx.x;
+    const int total = (int)m * d;   // m <= CENTER_MAXM (tc_shape_ok)
+    for (int i = tid; i < CENTER_MAXM / 32; i += CENTER_THREADS) bad[i] = 0u;
+    if (tid == 0) {
+        nvalid_s = 0u;
+        maxbits_s = 0u;
     }
-    part[warp][lane] = s0;
-    part[warp][lane + 32] = s1;
-    if (lane == 0) cnt_w[warp] = c;
     __syncthreads();
-    unsigned long long cnt = 0;
-    for (int q = 0; q < NW; ++q) cnt += cnt_w[q];
-    for (int k = threadIdx.x; k < d; k += CENTER_THREADS) {
+    for (int idx = tid; idx < total; idx += CENTER_THREADS)
+        if (!isfinite(__ldg(w + idx))) atomicOr(&bad[(idx / d) >> 5], 1u << ((idx / d) & 31));
+    __syncthreads();
+    unsigned int nv = 0;
+    for (int j = tid; j < (int)m; j += CENTER_THREADS) nv += ((bad[j >> 5] >> (j & 31)) & 1u) ? 0u : 1u;
+    atomicAdd(&nvalid_s, nv);
+    double s = 0.0;
+    for (int idx = tid; idx < total; idx += CENTER_THREADS) {
+        const int j = idx / d;
+        if (!((bad[j >> 5] >> (j & 31)) & 1u)) s += (double)__ldg(w + idx);
+    }
+    part[tid] = s;
+    __syncthreads();
+    const unsigned int cnt = nvalid_s;
+    for (int k = tid; k < d; k += CENTER_THREADS) {
         double t = 0.0;
-        for (int q = 0; q < NW; ++q) t += part[q][k];
+        for (int q = k; q < CENTER_THREADS; q += d) t += part[q];
         center[k] = cnt ? (float)(t / (double)cnt) : 0.0f;
     }
     __syncthreads();
-    const float c0 = k0 ? center[lane] : 0.0f, c1 = k1 ? center[lane + 32] : 0.0f;
+    const float ck = center[tid % d];   // this thread's feature
     unsigned int mx = 0u;
-    for (int64_t j = warp; j < m; j += NW) {
-        const float v0 = k0 ? w[j * d + lane] : 0.0f, v1 = k1 ? w[j * d + lane + 32] : 0.0f;
-        if (__all_sync(0xffffffffu, isfinite(v0) && isfinite(v1)))
-            mx = max(mx, max(__float_as_uint(fabsf(v0 - c0)), __float_as_uint(fabsf(v1 - c1))));
+    for (int idx = tid; idx < total; idx += CENTER_THREADS) {
+        const int j = idx / d;
+        if (!((bad[j >> 5] >> (j & 31)) & 1u)) mx = max(mx, __float_as_uint(fabsf(__ldg(w + idx) - ck)));
     }
     mx = __reduce_max_sync(0xffffffffu, mx);
-    if (lane == 0 && mx) atomicMax(&maxbits_s, mx);
+    if ((tid & 31) == 0 && mx) atomicMax(&maxbits_s, mx);
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         const float mxf = __uint_as_float(maxbits_s);
         int e = 0;
         if (mxf > 0.0f && isfinite(mxf)) frexpf(mxf, &e);   // mx < 2^e
@@ -1137,6 +1142,7 @@ thread_local uint32_t t_wait_limit = 0;
 bool tc_shape_ok(int64_t m, int d) {
     if (d != 4 && d != 8 && d != 16 && d != 32) return false;
     if (m <= 0 || m > (int64_t)MAX_U * TN) return false;   // a list entry names its chunk in a byte
+    static_assert(MAX_U * TN <= CENTER_MAXM, "the centre kernel's bitmap covers every map of the pass");
     return tc_shape(m, d).smem <= SMEM_LIMIT;
 }
 
