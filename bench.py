@@ -83,6 +83,10 @@ def parse():
     ap.add_argument('--serve', action='store_true', help='print the BMU-serving record alone')
     ap.add_argument('--serve-seconds', type=float, default=10.0, help='arrival window of the serving run')
     ap.add_argument('--serve-rate', type=float, default=200.0, help='mean request arrivals per second')
+    ap.add_argument('--serve-train', action='store_true',
+                    help='mixed-training serving: a stream of training jobs of mixed grids, D and sizes')
+    ap.add_argument('--jobs', type=int, default=500, help='training jobs of --serve-train')
+    ap.add_argument('--train-algos', default='auto,fp32', help='distance searches compared by --serve-train')
     return ap.parse_args()
 
 
@@ -726,12 +730,92 @@ def serve_arm(args):
     print(json.dumps(out), flush=True)
 
 
+MIXED = dict(name='mixed-training serving: grids uniform in {8x8, 16x16, 32x32, 48x48, 80x80}, square or hexagonal, '
+                  'D in {4, 8, 16, 32}, N log-uniform in [1e4, 5e6], 5-component Gaussian mixture or correlated '
+                  'log-normal, 10-30 epochs, weights U[-1, 1]', grids=(8, 16, 32, 48, 80), dims=(4, 8, 16, 32),
+             lo=10_000, hi=5_000_000, seed=5)
+
+
+def mixed_jobs(n_jobs):
+    """The seeded job list of the mixed-training workload (one dict per job)."""
+    c = MIXED
+    rng = np.random.default_rng(c['seed'])
+    jobs = []
+    for i in range(n_jobs):
+        g = int(rng.choice(c['grids']))
+        jobs.append(dict(m=g, n=g, topology=str(rng.choice(['square', 'hexagonal'])), d=int(rng.choice(c['dims'])),
+                         N=int(np.exp(rng.uniform(np.log(c['lo']), np.log(c['hi'])))),
+                         gen=str(rng.choice(['mixture', 'lognormal'])), epochs=int(rng.integers(10, 31)),
+                         seed=1000 + i))
+    return jobs
+
+
+def serve_train_record(args, algo):
+    """All jobs are submitted to SomServer as they are generated (each catalogue made on the device, then handed to
+    the server), trained on its two training streams under its device-memory admission; completion latency is from
+    submission to the trained map on the host."""
+    import torch
+    import decontamination_gb300 as dg
+    from decontamination_gb300 import synthetic
+    from decontamination_gb300.serve import SomServer
+    device = torch.device('cuda', torch.cuda.current_device())
+    jobs = mixed_jobs(args.jobs)
+    futs, work = [], 0
+    with SomServer(train_workers=2) as srv:
+        # warm-up: one small job of every D (library state, workspaces)
+        for d in MIXED['dims']:
+            som = dg.SOM_Batch(8, 8, d, topology='square')
+            som.bmu_algo = algo
+            srv.submit_train(som, synthetic.gaussian_mixture_device(20_000, d, 1, device), n_epochs=2).result()
+        n_warm = len(srv.latencies('train'))
+        t0 = time.perf_counter()
+        for j in jobs:
+            gen = synthetic.gaussian_mixture_device if j['gen'] == 'mixture' else \
+                synthetic.correlated_lognormal_device
+            x = gen(j['N'], j['d'], j['seed'], device)
+            torch.cuda.current_stream().synchronize()
+            som = dg.SOM_Batch(j['m'], j['n'], j['d'], topology=j['topology'])
+            som._weights[...] = synthetic.uniform_weights(j['m'] * j['n'], j['d'], j['seed']).reshape(
+                som._weights.shape)
+            som.bmu_algo = algo
+            futs.append(srv.submit_train(som, x, n_epochs=j['epochs'], use_best_epoch=False))
+            work += j['N'] * j['m'] * j['n'] * j['epochs']
+            del x
+        for f in futs:
+            f.result()
+        wall = time.perf_counter() - t0
+        lat = np.asarray(srv.latencies('train')[n_warm:]) * 1e3
+    return {'algo': algo, 'jobs': len(jobs), 'jobs_per_s': len(jobs) / wall, 'wall_s': wall,
+            'p50_ms': float(np.percentile(lat, 50)), 'p99_ms': float(np.percentile(lat, 99)),
+            'epoch_sample_units_per_s': {'value': work / wall / 1e9, 'unit': UNIT}}
+
+
+def serve_train_arm(args):
+    from decontamination_gb300 import build as gbuild
+    gbuild.build()
+    recs = [serve_train_record(args, a.strip()) for a in args.train_algos.split(',') if a.strip()]
+    jobs = mixed_jobs(args.jobs)
+    out = {'metric': 'mixed-training serving jobs/s', 'value': recs[0]['jobs_per_s'], 'unit': 'jobs/s',
+           'higher_is_better': True, 'n_gpus': 1, 'workload': MIXED['name'], 'runs': recs,
+           'jobs': {'count': len(jobs), 'rows_total': int(sum(j['N'] for j in jobs)),
+                    'tensor_core_shapes': int(sum(1 for j in jobs if j['m'] * j['n'] >= 32)),
+                    'sample_unit_epochs': float(sum(j['N'] * j['m'] * j['n'] * j['epochs'] for j in jobs))},
+           'data': 'synthetic, generated on the device per job (seeded)'}
+    if len(recs) > 1:
+        out['speedup_vs_' + recs[1]['algo']] = recs[0]['jobs_per_s'] / recs[1]['jobs_per_s']
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
     if args.serve:
         if rank == 0:
             serve_arm(args)
+        return
+    if args.serve_train:
+        if rank == 0:
+            serve_train_arm(args)
         return
     if args.impl == 'reference':
         reference_arm(args, ws, rank)

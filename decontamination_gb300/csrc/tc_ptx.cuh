@@ -46,12 +46,19 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t pari
         : "memory");
     return ok != 0;
 }
+// Suspend-time hint of the bounded waits, in nanoseconds (0: plain polling with try_wait).
+#ifndef SOMGB_WAIT_HINT_NS
+#define SOMGB_WAIT_HINT_NS 1000
+#endif
+
 // Waits until phase `parity` of `bar` has completed; false after `limit` polls of at most ~1 us each (a second or
 // more at the default limit; shorter only if the hardware ignores the hint, still far above any legitimate wait).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 22)) {
     if (mbar_try_wait(bar, parity)) return true;
-    for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
+    for (uint32_t i = 0; i < limit; ++i) {
+        if (SOMGB_WAIT_HINT_NS > 0 ? mbar_try_wait_sleep(bar, parity, SOMGB_WAIT_HINT_NS) : mbar_try_wait(bar, parity))
+            return true;
+    }
     return false;
 }
 

@@ -91,3 +91,15 @@ def correlated_lognormal_device(n, d, seed, device, scale=0.3, outlier_frac=0.02
         x[mask] *= outlier_scale
         out[s:e] = x
     return out
+
+
+def gaussian_mixture_device(n, d, seed, device, k=5, spread=3.0, sigma=0.5):
+    """The recipe of ``gaussian_mixture`` generated on the device (torch's seeded generator; same means, values
+    differ from the host generator's)."""
+    import torch
+    means = torch.from_numpy(np.random.default_rng(seed).uniform(-spread, spread, size=(k, d))).to(
+        device=device, dtype=torch.float32)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed) * 1000003 + 29)
+    idx = torch.randint(0, k, (n,), generator=g, device=device)
+    return (means[idx] + sigma * torch.randn((n, d), generator=g, device=device)).contiguous()
