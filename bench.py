@@ -59,7 +59,8 @@ UNIT = 'Gsample·unit/s'
 # DRAM traffic (bytes read + written) of one tensor-core BMU pass per catalogue row, from ncu captures of tc_pass_kernel
 # on 4,194,304-row cases of each workload (summaries under profiles/). The pass streams every row once (the samples,
 # the BMU, the unit operand from L2), so the traffic of a full launch scales with N.
-K1_DRAM_BYTES_PER_ROW = {}
+K1_DRAM_BYTES_PER_ROW = {'sq64d16': (269.468672e6 + 15.487488e6) / 4_194_304,
+                         'hex32': (268.734208e6 + 15.436032e6) / 4_194_304}
 
 
 def parse():
@@ -559,6 +560,8 @@ def gpu_arm(args, ws, rank, local):
     roofline = {'bound': 'tensor', 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
                 'frac': achieved_tflops / peak,
                 'traffic': traffic * N if (traffic and used_algo == 'tc') else None,
+                'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4,194,304-row case of this '
+                                  'workload, scaled by rows' if traffic else None,
                 'kernel': 'BMU pass (%s)' % ('tcgen05 split-FP16' if used_algo == 'tc' else 'FP32 CUDA cores'),
                 'kernel_ms': k_ms, 'kernel_share': k_ms * args.steps / total_ms,
                 'peak_source': f'{peak_kind} bf16_tflops_sustained (dense FP16 and BF16 share the rate)',
@@ -798,7 +801,8 @@ def serve_train_arm(args):
     out = {'metric': 'mixed-training serving jobs/s', 'value': recs[0]['jobs_per_s'], 'unit': 'jobs/s',
            'higher_is_better': True, 'n_gpus': 1, 'workload': MIXED['name'], 'runs': recs,
            'jobs': {'count': len(jobs), 'rows_total': int(sum(j['N'] for j in jobs)),
-                    'tensor_core_shapes': int(sum(1 for j in jobs if j['m'] * j['n'] >= 32)),
+                    'tensor_core_jobs': int(sum(1 for j in jobs if j['m'] * j['n'] >= 32 and
+                                                j['N'] * j['m'] * j['n'] >= (1 << 22))),
                     'sample_unit_epochs': float(sum(j['N'] * j['m'] * j['n'] * j['epochs'] for j in jobs))},
            'data': 'synthetic, generated on the device per job (seeded)'}
     if len(recs) > 1:
