@@ -110,7 +110,12 @@ constexpr float X_LIMIT = 32768.0f;   // scaled sample coordinates at or above t
 constexpr float Q_COLUMN = 2048.0f;   // A's value in the two q columns (B holds q / 2^11)
 constexpr float GAMMA = 0.00390625f;  // 2^-8: absolute error bound of the FP16 subnormal range, in scaled units
 constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go to the exact recheck
-constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN);
+// Each column tile's MMAs are issued as NSPLIT MMAs of N = TN / NSPLIT, one per column part with its own full and
+// empty barriers (NSPLIT = 2: each sweep half hands its columns back on its own). One MMA of N = 256 per K-step is
+// faster: two of N = 128 read the A tile twice, and the MMAs' shared-memory operand reads set their pace.
+constexpr int NSPLIT = 1;
+static_assert(NSPLIT == 1 || NSPLIT == HALVES, "one accumulator part per sweep half, or one for both");
+constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN / NSPLIT);
 constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded mbarrier wait (each at most about 1 us)
 // K layout of the operands (elements per row, FP16). D a multiple of 16: A = [x_hi | x_lo | q columns],
 // B = [-2w_hi | -2w_lo | q_hi q_lo 0...], and the MMA K-steps pair the blocks (lo.hi, hi.lo, hi.hi, then q), so no
@@ -499,8 +504,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     uint64_t* x_empty = bars + 4;   // [XSTAGES]
     uint64_t* a_full = bars + 7;    // [2]
     uint64_t* a_empty = bars + 9;   // [2]
-    uint64_t* t_full = bars + 11;   // [NACC]: an accumulator holds a computed column tile
-    uint64_t* t_empty = bars + 15;  // [NACC]: the sweeps have read it
+    uint64_t* t_full = bars + 11;   // [NACC][NSPLIT]: a part of an accumulator holds a computed column tile
+    uint64_t* t_empty = bars + 15;  // [NACC][NSPLIT]: the sweeps have read it
     uint64_t* m_full = bars + 19;   // [2]: the sweeps have written the candidate lists of a row tile
     uint64_t* m_empty = bars + 21;  // [2]: the resolvers are done with them
     uint64_t* drain = bars + 23;
@@ -530,9 +535,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             ptx::mbar_init(x_full + s, 1);
             ptx::mbar_init(x_empty + s, SWEEP_WARPS);
         }
-        for (int s = 0; s < NACC; ++s) {
+        static_assert(NACC * NSPLIT <= 4, "barrier slots 11-14 and 15-18");
+        for (int s = 0; s < NACC * NSPLIT; ++s) {
             ptx::mbar_init(t_full + s, 1);
-            ptx::mbar_init(t_empty + s, SWEEP_WARPS);
+            ptx::mbar_init(t_empty + s, SWEEP_WARPS / NSPLIT);
         }
         for (int s = 0; s < 2; ++s) {
             ptx::mbar_init(a_full + s, SWEEP_WARPS);
@@ -661,31 +667,36 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     const int u = uu >= U ? uu - U : uu;
                     const int buf = (int)(g % NACC);
                     TC_T0();
-                    if (g >= NACC && !ptx::mbar_wait(t_empty + buf, (uint32_t)((g / NACC - 1) & 1), lim)) {
-                        fail(8u);
-                        ok = false;
-                        break;
-                    }
-                    TC_T(12);
                     if (BST > 0 && !ptx::mbar_wait(bs_full + bst, bpar, lim)) {
                         fail(8192u);
                         ok = false;
                         break;
                     }
                     TC_T(13);
-                    ptx::tc_fence_after();
-                    const uint32_t dt = tbase + (uint32_t)(buf * TN);
                     const uint32_t bu = BST > 0 ? b_addr + (uint32_t)bst * b_stride
                                                 : b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
+                    for (int pp = 0; pp < NSPLIT; ++pp) {
+                        const int part = buf * NSPLIT + pp;
+                        if (g >= NACC && !ptx::mbar_wait(t_empty + part, (uint32_t)((g / NACC - 1) & 1), lim)) {
+                            fail(8u);
+                            ok = false;
+                            break;
+                        }
+                        TC_T(12);
+                        ptx::tc_fence_after();
+                        const uint32_t dt = tbase + (uint32_t)(buf * TN + pp * (TN / NSPLIT));
+                        const uint32_t bp = bu + (uint32_t)pp * (uint32_t)(TN / NSPLIT / 8) * sbo;
 #pragma unroll
-                    for (int ks = 0; ks < k_steps(DT); ++ks) {
-                        int ka, kb;
-                        k_step_cols(DT, ks, ka, kb);
-                        const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
-                        const uint64_t bd = ptx::smem_desc(bu + (uint32_t)(kb / 8) * 128u, 128, sbo);
-                        ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
+                        for (int ks = 0; ks < k_steps(DT); ++ks) {
+                            int ka, kb;
+                            k_step_cols(DT, ks, ka, kb);
+                            const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
+                            const uint64_t bd = ptx::smem_desc(bp + (uint32_t)(kb / 8) * 128u, 128, sbo);
+                            ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
+                        }
+                        ptx::mma_commit(t_full + part);
                     }
-                    ptx::mma_commit(t_full + buf);
+                    if (!ok) break;
                     if (BST > 0) {
                         ptx::mma_commit(bs_empty + bst);   // the stage is free once these MMAs have completed
                         if (++bst == BST) {
@@ -772,7 +783,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         auto release = [&](int buf) {
             ptx::tc_fence_before();
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(t_empty + buf);
+            if (lane == 0) ptx::mbar_arrive(t_empty + buf * NSPLIT + (NSPLIT > 1 ? h : 0));
         };
 
         // This warp's HW columns of TMEM tile `buf` in CPW 32-column chunks, software-pipelined: chunk c + 1 is loading
@@ -833,7 +844,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             float a1 = INFINITY, a2 = INFINITY;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons % NACC);
-                if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) { fail(64u); ok = false; break; }
+                if (!wwait(t_full + buf * NSPLIT + (NSPLIT > 1 ? h : 0), (uint32_t)((gcons / NACC) & 1))) {
+                    fail(64u);
+                    ok = false;
+                    break;
+                }
                 TC_T(0);
                 ptx::tc_fence_after();
                 stream_tile(buf, [&](int, const uint32_t (&r)[32]) { chunk_min(r, a1, a2); });
@@ -864,7 +879,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             bool ovf = false;
             for (int u = 0; u < U && ok; ++u, ++gcons) {
                 const int buf = (int)(gcons % NACC);
-                if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) { fail(128u); ok = false; break; }
+                if (!wwait(t_full + buf * NSPLIT + (NSPLIT > 1 ? h : 0), (uint32_t)((gcons / NACC) & 1))) {
+                    fail(128u);
+                    ok = false;
+                    break;
+                }
                 TC_T(0);
                 ptx::tc_fence_after();
                 stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
