@@ -287,6 +287,13 @@ class EpochRunner:
         self.penalty = 2.0 if w['topology'] == 'square' else 1.0
         nb = int(native.lib().somgb_neighbourhood_grid_workspace_bytes(w['m'], w['n'], self.D))
         self.upd_ws = torch.empty(nb, dtype=torch.uint8, device=device)
+        # the tensor-core form regroups the catalogue's rows by BMU after each epoch (SOM_Batch.train does the same)
+        self.regroup = self.algo != native.ALGO_FP32 and self.M > 256
+        self.x_pass = xd     # the rows (in their order) of the last pass, which self.bmu refers to
+        if self.regroup:     # two buffers of its own: the caller's catalogue is never written
+            self.bufs = [torch.empty_like(xd), torch.empty_like(xd)]
+            self.sort_ws = torch.empty(int(native.lib().somgb_sort_rows_workspace_bytes(self.M)), dtype=torch.uint8,
+                                       device=device)
         self.epoch = 0
 
     def sigma(self):
@@ -313,6 +320,14 @@ class EpochRunner:
                  self.bounds.data_ptr(), self.S.data_ptr(), self.c.data_ptr(), s)
         if phases is not None:
             phases[2].record()
+        self.x_pass = self.xd
+        if self.regroup:
+            xs = self.bufs[0] if self.bufs[0] is not self.xd else self.bufs[1]
+            nat.call('somgb_sort_rows', self.xd.data_ptr(), None, self.bmu.data_ptr(), self.N, self.D, self.M,
+                     xs.data_ptr(), None, self.sort_ws.data_ptr(), self.sort_ws.numel(), s)
+            self.xd = xs
+        if phases is not None:
+            phases[4].record()
         nat.call('somgb_neighbourhood_update_grid', self.S.data_ptr(), self.c.data_ptr(), self.topo.data_ptr(),
                  self.w['m'], self.w['n'], self.D, self.sigma(), self.wnext.data_ptr(), None, None,
                  self.upd_ws.data_ptr(), self.upd_ws.numel(), s)
@@ -355,11 +370,11 @@ def time_epochs(torch, runner, warmup, steps, sustain_s=0.0):
     while time.perf_counter() < t_end:
         runner.step(extra)
         torch.cuda.synchronize()
-    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ph = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
     runner.step(extra, phases=ph)
     torch.cuda.synchronize()
     phases = {'bmu_pass_ms': ph[0].elapsed_time(ph[1]), 'accumulate_ms': ph[1].elapsed_time(ph[2]),
-              'neighbourhood_update_ms': ph[2].elapsed_time(ph[3])}
+              'regroup_rows_ms': ph[2].elapsed_time(ph[4]), 'neighbourhood_update_ms': ph[4].elapsed_time(ph[3])}
     return total_ms, kernel_ms, launches, errs.cpu().numpy(), phases, rechecks
 
 
@@ -445,7 +460,7 @@ def weights_check(torch, runner):
     keep = runner.bmu >= 0
     b = runner.bmu[keep].long()
     S = torch.zeros((runner.M, runner.D), dtype=torch.float64, device=runner.dev)
-    S.index_add_(0, b, runner.xd[keep].double())
+    S.index_add_(0, b, runner.x_pass[keep].double())
     c = torch.bincount(b, minlength=runner.M).double()
     s_rel = float(((runner.S - S).abs().max() / S.abs().max().clamp_min(1e-300)).item())
     t = runner.topo

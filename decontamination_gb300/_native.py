@@ -55,6 +55,9 @@ SIGNATURES = {
     'somgb_footprint_maps_f64': [P, P, I64, I32, P, I64, P, P, P, P],
     'somgb_bmu_histograms': [P, P, I64, I64, P, P, P],
     'somgb_neighbourhood_grid_workspace_bytes': [I64, I64, I32],
+    'somgb_sort_rows_workspace_bytes': [I64],
+    'somgb_last_sweep2_tiles': [P, P],
+    'somgb_sort_rows': [P, P, P, I64, I32, I64, P, P, P, SZ, P],
     'somgb_neighbourhood_update_grid': [P, P, P, I64, I64, I32, D, P, P, P, P, SZ, P],
     'somgb_neighbourhood_update_grid_f64': [P, P, P, I64, I64, I32, D, P, P, P, P, SZ, P],
     'somgb_weighted_moments_f64': [P, P, I64, I32, P, P],
@@ -76,7 +79,8 @@ SIGNATURES = {
     'somgb_divide_f64': [P, P, I64, I32, P, P],
 }
 _RESTYPES = {'somgb_last_error': SZ, 'somgb_workspace_bytes': SZ, 'somgb_kernel_launches': I64,
-             'somgb_find_bmus_noalloc_scratch_bytes': SZ, 'somgb_neighbourhood_grid_workspace_bytes': SZ}
+             'somgb_find_bmus_noalloc_scratch_bytes': SZ, 'somgb_neighbourhood_grid_workspace_bytes': SZ,
+             'somgb_sort_rows_workspace_bytes': SZ}
 
 
 class SomgbError(RuntimeError):

@@ -18,6 +18,9 @@ int launch_neighbourhood_grid(const double* S, const double* c, const T* topo, i
                               double sigma, T* w_out, double* num, double* den, void* ws, size_t ws_bytes,
                               cudaStream_t stream);
 size_t grid_neighbourhood_workspace(int64_t rows, int64_t cols, int d);
+size_t sort_rows_workspace(int64_t m);
+int launch_sort_rows(const float* x, const double* rho, const int32_t* key, int64_t n, int d, int64_t m,
+                     float* x_out, double* rho_out, void* ws, size_t ws_bytes, cudaStream_t stream);
 int launch_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_w, double* hist_c,
                           cudaStream_t stream);
 template <typename T>
@@ -129,9 +132,10 @@ int check_common(const void* x, int64_t n, int d, const void* w, int64_t m, int 
 }
 
 int run_pass(PassArgs a, int algo, const Workspace& ws, bool tc, cudaStream_t stream) {
-    SOMGB_CUDA_TRY(cudaMemsetAsync(ws.counter, 0, 16, stream));   // recheck counter and status word
+    SOMGB_CUDA_TRY(cudaMemsetAsync(ws.counter, 0, 24, stream));   // recheck counter, status word, sweep-2 tiles
     a.recheck_count = ws.counter;
     a.status = (unsigned int*)(ws.counter + 1);
+    a.sweep2_tiles = ws.counter + 2;
     // the tensor-core pass reads sample and unit rows as float4 and topographic coordinates as float2
     const bool aligned = ((uintptr_t)a.x) % 16 == 0 && ((uintptr_t)a.w) % 16 == 0 &&
                          (!(a.outs & OUT_ERR) || ((uintptr_t)a.topo) % 8 == 0);
@@ -184,6 +188,17 @@ int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream) {
     SOMGB_CUDA_TRY(cudaMemcpyAsync(&v, g_last_counter, sizeof(v), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     SOMGB_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
     *count = (int64_t)v;
+    return SOMGB_OK;
+}
+
+int somgb_last_sweep2_tiles(int64_t* tiles, somgb_stream_t stream) {
+    if (!tiles) return set_error(SOMGB_ERR_INVALID, "tiles is NULL");
+    *tiles = 0;
+    if (!g_last_counter) return SOMGB_OK;
+    unsigned long long v = 0;
+    SOMGB_CUDA_TRY(cudaMemcpyAsync(&v, g_last_counter + 2, sizeof(v), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    SOMGB_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    *tiles = (int64_t)v;
     return SOMGB_OK;
 }
 
@@ -345,6 +360,18 @@ int somgb_neighbourhood_update(const double* S, const double* c, const float* to
     if (!S || !c || !topo || !w_out) return set_error(SOMGB_ERR_INVALID, "NULL argument");
     if (!(sigma > 0.0)) return set_error(SOMGB_ERR_INVALID, "sigma must be > 0");
     return launch_neighbourhood<float>(S, c, topo, m, d, sigma, w_out, num, den, (cudaStream_t)stream);
+}
+
+size_t somgb_sort_rows_workspace_bytes(int64_t m) { return m > 0 ? sort_rows_workspace(m) : 0; }
+
+int somgb_sort_rows(const float* x, const double* rho, const int32_t* key, int64_t n, int d, int64_t m,
+                    float* x_out, double* rho_out, void* ws, size_t ws_bytes, somgb_stream_t stream) {
+    if (n < 0 || m <= 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
+    if (n > 0 && (!x || !key || !x_out)) return set_error(SOMGB_ERR_INVALID, "x/key/x_out is NULL");
+    if (n > 0 && rho && !rho_out) return set_error(SOMGB_ERR_INVALID, "rho_out is NULL");
+    if (n > 0 && x_out == x) return set_error(SOMGB_ERR_INVALID, "x_out must not be x");
+    if (!ws) return set_error(SOMGB_ERR_INVALID, "workspace is NULL");
+    return launch_sort_rows(x, rho, key, n, d, m, x_out, rho_out, ws, ws_bytes, (cudaStream_t)stream);
 }
 
 size_t somgb_neighbourhood_grid_workspace_bytes(int64_t rows, int64_t cols, int d) {

@@ -23,22 +23,29 @@
 // + gamma, m being the best (second-best) s~ of the row; thr is non-decreasing in m, so any upper bound of m gives a
 // threshold that keeps every such unit.
 //
-// Epilogue: two sweeps per row tile (every MMA is issued twice; the tensor pipe has the slack). Sweep 1 reads each
-// row's s~ in 32-column chunks and keeps the smallest value (for the error sums, the two smallest 8-unit group
-// minima: an upper bound of the second-best s~); the two column halves combine theirs into the row's threshold.
-// Sweep 2 reads the same values again: where a row of the warp can have a candidate in a chunk (chunk minimum at or
-// under its threshold), the warp builds the chunk's candidate bit masks, a branch-free subtraction and shift of the
-// sign bit per value, and every row with a non-zero mask appends (mask word, chunk) to its own short list. The
+// Epilogue: two sweeps per row tile. Sweep 1 computes every column tile and reads each row's s~ in 32-column chunks,
+// keeping the smallest value (for the error sums, the two smallest 8-unit group minima: an upper bound of the
+// second-best s~) and each column tile's minimum; the two column halves combine theirs into the row's threshold, and
+// the column tiles where some row of the 128-row tile has a tile minimum at or under its threshold make the tile set
+// of sweep 2. Sweep 2 recomputes only those column tiles (every candidate lies in one; with the rows grouped by their
+// previous BMU, somgb_sort_rows, a tile's rows share a neighbourhood of the map and the set is small): where a row of
+// the warp can have a candidate in a chunk (chunk minimum at or under its threshold), the warp builds the chunk's
+// candidate bit masks, a branch-free subtraction and shift of the sign bit per value, and every row with a non-zero
+// mask appends (mask word, chunk) to its own short list. The MMAs run sweep 1 of row tile k, then sweep 2 of row
+// tile k - 1, so that sweep 2's tile set is known a whole sweep ahead. The
 // resolvers evaluate each row's candidates on CUDA cores with float32 differences (the reference's terms) and rank
 // them; ranks within float32 rounding of each other are decided by compensated float32 sums and, failing that, by
 // the reference's float64 sum. Rows with more than CAPR candidates, a full list, non-finite features or overflowing
 // distances go to an exact per-row recheck.
 //
-// Pipeline (one persistent CTA per SM, 448 threads, every hand-off an mbarrier):
+// Pipeline (one persistent CTA per SM, 480 threads, every hand-off an mbarrier):
 //   warp 13     TMA producer: the unit operand B (resident: one bulk copy; else a ring of column tiles in the MMAs'
-//               order, twice per row tile), sample tiles (2-D tiled TMA, 2-stage ring);
-//   warp 12     TMEM allocator and MMA issuer (one thread), NACC TMEM accumulators of TN columns each;
-//   warps 0-7   converters (FP32 tile -> centred split-FP16 A tile) and sweeps; warp e reads TMEM lanes
+//               order), sample tiles (2-D tiled TMA, one row tile ahead);
+//   warp 12     TMEM allocator; two TMEM accumulators of TN columns each;
+//   warps 12/14 MMA issuers (one thread each): warp 12 the even column tiles (accumulator 0), warp 14 the odd ones
+//               (accumulator 1);
+//   warps 0-7   converters (FP32 tile -> centred split-FP16 A tile, three A stages: two row tiles' MMAs read them
+//               while the next is written) and sweeps; warp e reads TMEM lanes
 //               32(e&3).. and column half e>>2 and writes its rows' candidate lists (two list buffers, so the sweeps
 //               of row tile t+1 do not wait for the resolvers of row tile t);
 //   warps 8-11  resolvers: thread r of warp 8+q decides row 32q+r of a row tile while the sweeps run the next one:
@@ -93,29 +100,29 @@ constexpr int CAPR = 24;          // candidates a resolver ranks per row
 constexpr int CAP = 4;            // candidate-list entries per row and column half
 constexpr size_t SMEM_LIMIT = 227 * 1024;   // opt-in shared memory of one CTA
 constexpr int MAX_U = 16384 / TN; // column tiles per row tile (a list entry names its chunk, CPW per tile and half, in a byte)
-constexpr int NBARS = 48;         // mbarrier slots
+constexpr int NBARS = 56;         // mbarrier slots
+constexpr int ASTAGES = 3;        // A tiles: sweep 1 of row tile k and sweep 2 of k - 1 read two, the converters write a third
 constexpr int BMAX = 4;           // deepest ring of streamed unit-operand tiles (slots 32 .. 32 + 2 BMAX - 1)
-static_assert(32 + 2 * BMAX <= NBARS, "mbarrier slots");
+static_assert(32 + 2 * BMAX <= 40 && 44 + 2 * ASTAGES <= NBARS, "mbarrier slots");
 static_assert(CPW * MAX_U <= 256, "chunk ids are bytes");
 static_assert(NACC * TN == 512 && CPW * 32 == HW, "TMEM and chunk layout");
-constexpr int XSTAGES = 2;   // the converters release a sample tile as soon as they have read it
+constexpr int XSTAGES = 1;   // a sample tile is converted a whole row tile before its MMAs: one stage is ahead enough
 constexpr int SWEEP_WARPS = 4 * HALVES;
 constexpr int RES_GROUP = 4;    // resolver warps per row tile (one thread per row)
 constexpr int RES_GROUPS = 1;   // groups of resolvers taking the row tiles in turn (1 or 2; list buffers: 2)
 constexpr int RES_WARPS = RES_GROUPS * RES_GROUP;
-constexpr int MMA_WARP = SWEEP_WARPS + RES_WARPS;
+constexpr int MMA_WARP = SWEEP_WARPS + RES_WARPS;   // issuer of the tiles of accumulator 0; allocates TMEM
 constexpr int TMA_WARP = MMA_WARP + 1;
-constexpr int NUM_THREADS = (TMA_WARP + 1) * 32;
+constexpr int MMA_WARP2 = TMA_WARP + 1;              // issuer of the tiles of accumulator 1
+constexpr int NUM_THREADS = (MMA_WARP2 + 1) * 32;
 constexpr float X_LIMIT = 32768.0f;   // scaled sample coordinates at or above this go to the exact recheck
 constexpr float Q_COLUMN = 2048.0f;   // A's value in the two q columns (B holds q / 2^11)
 constexpr float GAMMA = 0.00390625f;  // 2^-8: absolute error bound of the FP16 subnormal range, in scaled units
 constexpr float HUGE_S = 1.0e30f; // rows whose best s~ + |x'|^2 reaches this go to the exact recheck
-// Each column tile's MMAs are issued as NSPLIT MMAs of N = TN / NSPLIT, one per column part with its own full and
-// empty barriers (NSPLIT = 2: each sweep half hands its columns back on its own). One MMA of N = 256 per K-step is
-// faster: two of N = 128 read the A tile twice, and the MMAs' shared-memory operand reads set their pace.
-constexpr int NSPLIT = 1;
-static_assert(NSPLIT == 1 || NSPLIT == HALVES, "one accumulator part per sweep half, or one for both");
-constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN / NSPLIT);
+// One MMA of N = TN = 256 per K-step: two of N = 128, each half of the accumulator with its own barriers, were
+// measured slower (they read the A tile twice).
+static_assert(NACC == 2, "one MMA issuer per accumulator (issuer k: column tiles g with g % 2 == k)");
+constexpr uint32_t IDESC = ptx::idesc_f16_f32(TM, TN);
 constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded mbarrier wait (each at most about 1 us)
 // K layout of the operands (elements per row, FP16). D a multiple of 16: A = [x_hi | x_lo | q columns],
 // B = [-2w_hi | -2w_lo | q_hi q_lo 0...], and the MMA K-steps pair the blocks (lo.hi, hi.lo, hi.hi, then q), so no
@@ -149,14 +156,14 @@ struct TcShape {
     int bstages = 0;   // 0: the whole unit operand resident in shared memory; else a ring of this many column tiles
     size_t b_bytes = 0, b_tile = 0, a_bytes = 0, x_bytes = 0;
     size_t off_a = 0, off_x = 0, off_lw = 0, off_part = 0, off_thr = 0, off_lc = 0, off_cnt = 0, off_flag = 0,
-           off_center = 0, off_bar = 0, off_w = 0, smem = 0;
+           off_tmin = 0, off_union = 0, off_center = 0, off_bar = 0, off_w = 0, smem = 0;
 };
 
 // Layout after a unit-operand region of `bregion` bytes; returns the end offset (before the unit rows).
 size_t tc_layout(TcShape& s, size_t bregion) {
     size_t off = align_up(bregion, 1024);
     s.off_a = off;
-    off += 2 * align_up(s.a_bytes, 1024);
+    off += ASTAGES * align_up(s.a_bytes, 1024);
     s.off_x = off;
     off += XSTAGES * s.x_bytes;
     // candidate lists, [buffer][half][entry][row]: mask words and chunk ids; per buffer, half and row the half's
@@ -173,6 +180,12 @@ size_t tc_layout(TcShape& s, size_t bregion) {
     off += (size_t)2 * HALVES * TM;
     s.off_flag = off;
     off += (size_t)2 * TM;
+    // per row, column half and column tile the tile's minimum (FP16), and per list buffer the column tiles with a
+    // candidate, one word per sweep warp
+    s.off_tmin = align_up(off, 16);
+    off = s.off_tmin + (size_t)HALVES * s.utiles * TM * 2;
+    s.off_union = align_up(off, 16);
+    off = s.off_union + (size_t)2 * SWEEP_WARPS * 8;
     s.off_center = align_up(off, 16);
     off = s.off_center + align_up((size_t)(s.d + 1) * 4, 16);
     s.off_bar = align_up(off, 8);
@@ -412,8 +425,8 @@ struct TcArgs {
     int kpad;
     int utiles;
     float alpha, beta, kthr;   // kthr = 2 / (1 - beta), rounded up
-    size_t off_a, off_x, off_lw, off_part, off_thr, off_lc, off_cnt, off_flag, off_center, off_bar, off_w, a_stride,
-        x_stride;
+    size_t off_a, off_x, off_lw, off_part, off_thr, off_lc, off_cnt, off_flag, off_tmin, off_union, off_center,
+        off_bar, off_w, a_stride, x_stride;
     uint32_t b_bytes;
     uint32_t b_tile;         // bytes of one column tile of the unit operand
     int bstages;             // 0: resident unit operand; else the ring depth
@@ -498,17 +511,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     float2* sPart = (float2*)(smem + P.off_part);   // [2][HALVES][TM] (a1, a2) of the half
     float* sThr = (float*)(smem + P.off_thr);       // [2][TM] the row's threshold
     uint8_t* sFlag = smem + P.off_flag;             // [2][TM] the row goes to the exact recheck
+    __half* sTmin = (__half*)(smem + P.off_tmin);   // [HALVES][U][TM] tile minimum of s~ + |x'|^2, rounded down
+    uint64_t* sUnion = (uint64_t*)(smem + P.off_union);   // [2][SWEEP_WARPS] column tiles with a candidate
     uint64_t* bars = (uint64_t*)(smem + P.off_bar);
     uint64_t* b_full = bars + 0;
     uint64_t* x_full = bars + 1;    // [XSTAGES]
     uint64_t* x_empty = bars + 4;   // [XSTAGES]
-    uint64_t* a_full = bars + 7;    // [2]
-    uint64_t* a_empty = bars + 9;   // [2]
-    uint64_t* t_full = bars + 11;   // [NACC][NSPLIT]: a part of an accumulator holds a computed column tile
-    uint64_t* t_empty = bars + 15;  // [NACC][NSPLIT]: the sweeps have read it
+    uint64_t* a_full = bars + 44;   // [ASTAGES]
+    uint64_t* a_empty = bars + 47;  // [ASTAGES]
+    uint64_t* t_full = bars + 11;   // [NACC]: an accumulator holds a computed column tile
+    uint64_t* t_empty = bars + 15;  // [NACC]: the sweeps have read it
     uint64_t* m_full = bars + 19;   // [2]: the sweeps have written the candidate lists of a row tile
     uint64_t* m_empty = bars + 21;  // [2]: the resolvers are done with them
-    uint64_t* drain = bars + 23;
+    uint64_t* drain = bars + 40;    // [NACC]: every MMA of one issuer has completed
+    uint64_t* u_full = bars + 42;   // [2]: every sweep warp has published its column tiles with a candidate
     uint64_t* p_full = bars + 24;   // [2][4] both halves of a lane quarter have published (a1, a2)
     uint64_t* bs_full = bars + 32;  // [BMAX]: a column tile of the unit operand has landed (streamed operand)
     uint64_t* bs_empty = bars + 32 + BMAX; // [BMAX]: the MMAs reading it have completed
@@ -519,7 +535,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr int d = DT;
     constexpr int kpad = k_width(DT);
-    constexpr int SWEEPS = 2;
     const int U = P.utiles;
     const uint32_t lim = P.wait_limit;
     const int64_t num_tiles = (a.n + TM - 1) / TM;
@@ -535,19 +550,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             ptx::mbar_init(x_full + s, 1);
             ptx::mbar_init(x_empty + s, SWEEP_WARPS);
         }
-        static_assert(NACC * NSPLIT <= 4, "barrier slots 11-14 and 15-18");
-        for (int s = 0; s < NACC * NSPLIT; ++s) {
+        static_assert(NACC <= 4, "barrier slots 11-14 and 15-18");
+        for (int s = 0; s < NACC; ++s) {
             ptx::mbar_init(t_full + s, 1);
-            ptx::mbar_init(t_empty + s, SWEEP_WARPS / NSPLIT);
+            ptx::mbar_init(t_empty + s, SWEEP_WARPS);
         }
         for (int s = 0; s < 2; ++s) {
-            ptx::mbar_init(a_full + s, SWEEP_WARPS);
-            ptx::mbar_init(a_empty + s, 1);
             ptx::mbar_init(m_full + s, SWEEP_WARPS);
             ptx::mbar_init(m_empty + s, RES_GROUP);
+            ptx::mbar_init(u_full + s, SWEEP_WARPS);
             for (int qq = 0; qq < 4; ++qq) ptx::mbar_init(p_full + s * 4 + qq, HALVES);
         }
-        ptx::mbar_init(drain, 1);
+        for (int s = 0; s < NACC; ++s) ptx::mbar_init(drain + s, 1);
+        for (int s = 0; s < ASTAGES; ++s) {
+            ptx::mbar_init(a_full + s, SWEEP_WARPS);
+            ptx::mbar_init(a_empty + s, NACC);   // a commit from each issuer
+        }
         ptx::fence_mbar_init();
         abort_s = 0;
     }
@@ -578,6 +596,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         return __all_sync(0xffffffffu, ptx::mbar_wait(bar, parity, lim));
     };
     auto waborted = [&]() -> bool { return __any_sync(0xffffffffu, *abort_v != 0); };
+    // the column tiles of sweep 2 of the row tiles with list buffer lb (after their u_full phase)
+    auto union_of = [&](int lb) -> uint64_t {
+        uint64_t un = 0;
+#pragma unroll
+        for (int k = 0; k < SWEEP_WARPS; ++k) un |= sUnion[lb * SWEEP_WARPS + k];
+        return un;
+    };
 #ifdef SOMGB_TC_PHASE_TIMING
     unsigned long long _tc_acc[TC_PHASES] = {};
     long long _tc_t0 = 0;
@@ -617,24 +642,35 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             if (BST == 0) {
                 for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) ok = issue_x(it);
             } else {
-                // sample tiles one row tile ahead of the unit-operand tiles, which go in the MMAs' order
-                for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
-                    while (ok && issued < n_my && issued <= it + 1) ok = issue_x(issued);
-                    for (int uu = 0; ok && uu < SWEEPS * U && !*abort_v; ++uu, ++kb) {
-                        const int u = uu >= U ? uu - U : uu;
-                        const int st = (int)(kb % BSTD);
-                        if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BSTD - 1) & 1), lim)) {
-                            fail(4096u);
-                            ok = false;
-                            break;
-                        }
-                        ptx::mbar_arrive_expect_tx(bs_full + st, P.b_tile);
-                        const uint8_t* src = P.b + (size_t)u * P.b_tile;
-                        for (uint32_t off = 0; off < P.b_tile; off += 32768u) {
-                            const uint32_t len = P.b_tile - off < 32768u ? P.b_tile - off : 32768u;
-                            ptx::bulk_g2s(sB + (size_t)st * b_stride + off, src + off, len, bs_full + st);
-                        }
+                // sample tiles one row tile ahead of the unit-operand tiles, which go in the MMAs' order: every
+                // column tile for sweep 1, then those with a candidate for sweep 2, once the sweeps have published them
+                auto stream_b = [&](int u) -> bool {
+                    const int st = (int)(kb % BSTD);
+                    if (kb >= BST && !ptx::mbar_wait(bs_empty + st, (uint32_t)((kb / BSTD - 1) & 1), lim)) {
+                        fail(4096u);
+                        return false;
                     }
+                    ptx::mbar_arrive_expect_tx(bs_full + st, P.b_tile);
+                    const uint8_t* src = P.b + (size_t)u * P.b_tile;
+                    for (uint32_t off = 0; off < P.b_tile; off += 32768u) {
+                        const uint32_t len = P.b_tile - off < 32768u ? P.b_tile - off : 32768u;
+                        ptx::bulk_g2s(sB + (size_t)st * b_stride + off, src + off, len, bs_full + st);
+                    }
+                    ++kb;
+                    return true;
+                };
+                for (int64_t k = 0; ok && k <= n_my && !*abort_v; ++k) {   // phase k: sweep 1 of k, sweep 2 of k - 1
+                    while (ok && issued < n_my && issued <= k + 1) ok = issue_x(issued);
+                    for (int u = 0; ok && k < n_my && u < U && !*abort_v; ++u) ok = stream_b(u);
+                    if (!ok || *abort_v || k == 0) continue;
+                    const int64_t j = k - 1;
+                    if (!ptx::mbar_wait(u_full + (j & 1), (uint32_t)((j >> 1) & 1), lim)) {
+                        fail(32768u);
+                        ok = false;
+                        break;
+                    }
+                    for (uint64_t rest = union_of((int)(j & 1)); ok && rest != 0 && !*abort_v; rest &= rest - 1)
+                        ok = stream_b(__ffsll((long long)rest) - 1);
                 }
             }
             if (*abort_v || !ok) {
@@ -647,7 +683,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     ptx::mbar_wait(bs_full + (int)(k % BSTD), (uint32_t)((k / BSTD) & 1));
             }
         }
-    } else if (warp == MMA_WARP) {
+    } else if (warp == MMA_WARP || warp == MMA_WARP2) {
+        // Two issuers, one per accumulator: issuer k issues the MMAs of the column tiles g with g % NACC == k, so the
+        // waits for one accumulator never hold up the other's MMAs.
+        const int ik = warp == MMA_WARP ? 0 : 1;
         if (lane == 0 && n_my > 0) {
             const int BST = P.bstages;
             bool ok = BST > 0 || ptx::mbar_wait(b_full, 0, lim);
@@ -656,60 +695,88 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             const uint32_t b_addr = ptx::smem_u32(sB);
             const uint32_t b_stride = (P.b_tile + 1023u) & ~1023u;
             int64_t g = 0;
-            int bst = 0;              // ring stage of the next streamed column tile, and the parity of its use
+            int bst = 0;              // ring stage of column tile g, and the parity of its use
             uint32_t bpar = 0;
-            for (int64_t it = 0; ok && it < n_my && !*abort_v; ++it) {
-                const int s = (int)(it & 1);
-                if (!ptx::mbar_wait(a_full + s, (uint32_t)((it >> 1) & 1), lim)) { fail(4u); break; }
+            // column tile g, unit tile u: its MMAs when it is this issuer's
+            auto tile = [&](uint32_t a_addr, int u) -> bool {
+                const int cur_bst = bst;
+                const uint32_t cur_bpar = bpar;
+                if (BST > 0 && ++bst == BST) {
+                    bst = 0;
+                    bpar ^= 1u;
+                }
+                const int64_t gg = g++;
+                if ((int)(gg & (NACC - 1)) != ik) return true;
+                const int buf = ik;
+                TC_T0();
+                // The unit-operand tile and the accumulator. With an even ring depth the stage's previous use,
+                // column tile g - BST, was issued by this thread after its own wait, so that phase has completed
+                // and the parity names this use: the tile is waited for first, off the critical path (the
+                // accumulator is the wait that ends last). With an odd depth the previous use belongs to the
+                // other issuer; the accumulator comes first, and once the sweeps have released tile g - NACC every
+                // tile before it has completed its MMAs, so that use is over.
+                const bool b_first = (BST & 1) == 0;
+                if (b_first && BST > 0 && !ptx::mbar_wait(bs_full + cur_bst, cur_bpar, lim)) {
+                    fail(8192u);
+                    return false;
+                }
+                TC_T(13);
+                if (gg >= NACC && !ptx::mbar_wait(t_empty + buf, (uint32_t)((gg / NACC - 1) & 1), lim)) {
+                    fail(8u);
+                    return false;
+                }
+                TC_T(12);
+                if (!b_first && !ptx::mbar_wait(bs_full + cur_bst, cur_bpar, lim)) {
+                    fail(8192u);
+                    return false;
+                }
                 ptx::tc_fence_after();
-                const uint32_t a_addr = ptx::smem_u32(smem + P.off_a + s * P.a_stride);
-                for (int uu = 0; uu < SWEEPS * U; ++uu, ++g) {
-                    const int u = uu >= U ? uu - U : uu;
-                    const int buf = (int)(g % NACC);
-                    TC_T0();
-                    if (BST > 0 && !ptx::mbar_wait(bs_full + bst, bpar, lim)) {
-                        fail(8192u);
-                        ok = false;
+                const uint32_t bu = BST > 0 ? b_addr + (uint32_t)cur_bst * b_stride
+                                            : b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
+                const uint32_t dt = tbase + (uint32_t)(buf * TN);
+#pragma unroll
+                for (int ks = 0; ks < k_steps(DT); ++ks) {
+                    int ka, kb;
+                    k_step_cols(DT, ks, ka, kb);
+                    const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
+                    const uint64_t bd = ptx::smem_desc(bu + (uint32_t)(kb / 8) * 128u, 128, sbo);
+                    ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
+                }
+                ptx::mma_commit(t_full + buf);
+                // the stage is free once these MMAs have completed
+                if (BST > 0) ptx::mma_commit(bs_empty + cur_bst);
+                return true;
+            };
+            // phase k: sweep 1 of row tile k (every column tile), then sweep 2 of row tile k - 1 (the column tiles
+            // with a candidate, published by the sweeps at the end of its sweep 1)
+            for (int64_t k = 0; ok && k <= n_my && !*abort_v; ++k) {
+                if (k < n_my) {
+                    const int sa = (int)(k % ASTAGES);
+                    if (!ptx::mbar_wait(a_full + sa, (uint32_t)((k / ASTAGES) & 1), lim)) { fail(4u); break; }
+                    ptx::tc_fence_after();
+                    const uint32_t a_addr = ptx::smem_u32(smem + P.off_a + sa * P.a_stride);
+                    for (int u = 0; ok && u < U; ++u) ok = tile(a_addr, u);
+                    if (!ok) break;
+                }
+                if (k >= 1) {
+                    const int64_t j = k - 1;
+                    const int sa = (int)(j % ASTAGES);
+                    if (!ptx::mbar_wait(u_full + (j & 1), (uint32_t)((j >> 1) & 1), lim)) {
+                        fail(32768u);
                         break;
                     }
-                    TC_T(13);
-                    const uint32_t bu = BST > 0 ? b_addr + (uint32_t)bst * b_stride
-                                                : b_addr + (uint32_t)u * (uint32_t)(TN / 8) * sbo;
-                    for (int pp = 0; pp < NSPLIT; ++pp) {
-                        const int part = buf * NSPLIT + pp;
-                        if (g >= NACC && !ptx::mbar_wait(t_empty + part, (uint32_t)((g / NACC - 1) & 1), lim)) {
-                            fail(8u);
-                            ok = false;
-                            break;
-                        }
-                        TC_T(12);
-                        ptx::tc_fence_after();
-                        const uint32_t dt = tbase + (uint32_t)(buf * TN + pp * (TN / NSPLIT));
-                        const uint32_t bp = bu + (uint32_t)pp * (uint32_t)(TN / NSPLIT / 8) * sbo;
-#pragma unroll
-                        for (int ks = 0; ks < k_steps(DT); ++ks) {
-                            int ka, kb;
-                            k_step_cols(DT, ks, ka, kb);
-                            const uint64_t ad = ptx::smem_desc(a_addr + (uint32_t)(ka / 8) * 128u, 128, sbo);
-                            const uint64_t bd = ptx::smem_desc(bp + (uint32_t)(kb / 8) * 128u, 128, sbo);
-                            ptx::mma_f16(dt, ad, bd, IDESC, ks > 0);
-                        }
-                        ptx::mma_commit(t_full + part);
-                    }
+                    const uint64_t un = union_of((int)(j & 1));
+                    if (ik == 0 && a.sweep2_tiles) atomicAdd(a.sweep2_tiles, (unsigned long long)__popcll(un));
+                    const uint32_t a_addr = ptx::smem_u32(smem + P.off_a + sa * P.a_stride);
+                    for (uint64_t rest = un; ok && rest != 0; rest &= rest - 1)
+                        ok = tile(a_addr, __ffsll((long long)rest) - 1);
                     if (!ok) break;
-                    if (BST > 0) {
-                        ptx::mma_commit(bs_empty + bst);   // the stage is free once these MMAs have completed
-                        if (++bst == BST) {
-                            bst = 0;
-                            bpar ^= 1u;
-                        }
-                    }
+                    ptx::mma_commit(a_empty + sa);   // A tile j is no longer read once these MMAs have completed
                 }
-                ptx::mma_commit(a_empty + s);
             }
-            // every MMA issued by this thread has completed once `drain` flips
-            ptx::mma_commit(drain);
-            if (!ptx::mbar_wait(drain, 0)) fail(256u);
+            // every MMA issued by this thread has completed once its drain barrier flips
+            ptx::mma_commit(drain + ik);
+            if (!ptx::mbar_wait(drain + ik, 0)) fail(256u);
         }
     } else if (warp < SWEEP_WARPS) {
         // ------------------------------ converter + sweep (warps 0..7) ----------------------------------------------
@@ -721,8 +788,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         // centred, scaled split-FP16 A row of `row`: this thread writes the 16-byte chunks kc = h, h + 2, ... of
         // kpad / 8; returns |x'|^2 (infinite when a coordinate is not finite or outside the FP16 split's range)
         auto convert = [&](int64_t it, float& xn_out) -> bool {
-            const int s2 = (int)(it & 1), s3 = (int)(it % XSTAGES);
-            if (it >= 2 && !wwait(a_empty + s2, (uint32_t)(((it >> 1) - 1) & 1))) { fail(16u); return false; }
+            const int s2 = (int)(it % ASTAGES), s3 = (int)(it % XSTAGES);
+            if (it >= ASTAGES && !wwait(a_empty + s2, (uint32_t)((it / ASTAGES - 1) & 1))) { fail(16u); return false; }
             if (!wwait(x_full + s3, (uint32_t)((it / XSTAGES) & 1))) { fail(32u); return false; }
             const float4* xs4 = (const float4*)(smem + P.off_x + s3 * P.x_stride) + row * (DT / 4);
             const float scale = sCenter[DT];
@@ -783,7 +850,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         auto release = [&](int buf) {
             ptx::tc_fence_before();
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(t_empty + buf * NSPLIT + (NSPLIT > 1 ? h : 0));
+            if (lane == 0) ptx::mbar_arrive(t_empty + buf);
         };
 
         // This warp's HW columns of TMEM tile `buf` in CPW 32-column chunks, software-pipelined: chunk c + 1 is loading
@@ -830,87 +897,127 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         int64_t gcons = 0;   // TMEM tiles consumed
         float xn_next = 0.0f;
         bool ok = n_my > 0 ? convert(0, xn_next) : true;
-        for (int64_t it = 0; ok && it < n_my && !waborted(); ++it) {
+        // Phase k: sweep 1 of row tile k, then sweep 2 of row tile k - 1 (the MMAs run in this order), so that the
+        // column tiles of a sweep 2 are known one sweep 1 ahead and the tensor pipe never waits for them. thr_p,
+        // thr_up_p, flagged_p: row tile k - 1's threshold state.
+        float thr_p = -INFINITY, thr_up_p = -INFINITY;
+        bool flagged_p = true;
+        for (int64_t k = 0; ok && k <= n_my && !waborted(); ++k) {
             const float xn = xn_next;
-            const int lb = (int)(it & 1);
             TC_T0();
-            if (it + 1 < n_my && !(ok = convert(it + 1, xn_next))) break;
+            if (k + 1 < n_my && !(ok = convert(k + 1, xn_next))) break;
             TC_T(4);
-            // the resolvers are done with buffer lb (row tile it - 2): its lists and the half exchange below may be
-            // rewritten
-            if (it >= 2 && !wwait(m_empty + lb, (uint32_t)(((it >> 1) - 1) & 1))) { fail(512u); break; }
-            TC_T(5);
-            // ---- sweep 1: the row's bounds over this half's columns ------------------------------------------------
-            float a1 = INFINITY, a2 = INFINITY;
-            for (int u = 0; u < U && ok; ++u, ++gcons) {
-                const int buf = (int)(gcons % NACC);
-                if (!wwait(t_full + buf * NSPLIT + (NSPLIT > 1 ? h : 0), (uint32_t)((gcons / NACC) & 1))) {
-                    fail(64u);
-                    ok = false;
-                    break;
+            float thr = -INFINITY, thr_up = -INFINITY;
+            bool flagged = true;
+            if (k < n_my) {
+                const int lb = (int)(k & 1);
+                // ---- sweep 1: the row's bounds over this half's columns --------------------------------------------
+                float a1 = INFINITY, a2 = INFINITY;
+                __half* tmin = sTmin + (size_t)h * U * TM + row;   // the row's minimum over its half of each tile
+                for (int u = 0; u < U && ok; ++u, ++gcons) {
+                    const int buf = (int)(gcons % NACC);
+                    if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) {
+                        fail(64u);
+                        ok = false;
+                        break;
+                    }
+                    TC_T(0);
+                    ptx::tc_fence_after();
+                    float tm = INFINITY;
+                    stream_tile(buf, [&](int, const uint32_t (&r)[32]) { tm = fminf(tm, chunk_min(r, a1, a2)); });
+                    // as |x' - w'|^2 = s~ + |x'|^2 (non-negative up to rounding, so FP16 holds it), rounded down
+                    tmin[(size_t)u * TM] = __float2half_rd(__fadd_rd(tm, xn));
+                    TC_T(1);
                 }
-                TC_T(0);
-                ptx::tc_fence_after();
-                stream_tile(buf, [&](int, const uint32_t (&r)[32]) { chunk_min(r, a1, a2); });
-                TC_T(1);
-            }
-            if (!ok) break;
-            // both halves' bounds: the row's threshold. ERR: M2 is the second smallest 8-unit group minimum, an upper
-            // bound of the second smallest s~ (two groups have a unit at or below it), so the threshold derived from it
-            // keeps every possible second BMU.
-            sPart[(lb * HALVES + h) * TM + row] = make_float2(a1, a2);
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
-            if (!wwait(p_full + lb * 4 + q, (uint32_t)((it >> 1) & 1))) { fail(2048u); break; }
-            const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
-            const float M1 = fminf(p0.x, p1.x);
-            const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
-            const float mref = ERR ? M2 : M1;
-            const bool flagged = !(xn < HUGE_S) || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
-            const float thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
-            // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
-            // floats never rounds to zero), so each value costs one subtraction and one shift of its sign bit
-            const float thr_up = nextafterf(thr, INFINITY);
-            // ---- sweep 2: the candidate lists -----------------------------------------------------------------------
-            const size_t lbase = (size_t)((lb * HALVES + h) * CAP) * TM + row;
-            uint32_t* lw = sLw + lbase;
-            uint8_t* lc = sLc + lbase;
-            int cnt = 0;
-            bool ovf = false;
-            for (int u = 0; u < U && ok; ++u, ++gcons) {
-                const int buf = (int)(gcons % NACC);
-                if (!wwait(t_full + buf * NSPLIT + (NSPLIT > 1 ? h : 0), (uint32_t)((gcons / NACC) & 1))) {
-                    fail(128u);
-                    ok = false;
-                    break;
-                }
-                TC_T(0);
-                ptx::tc_fence_after();
-                stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
-                    // the chunk's masks only when a row of the warp has a candidate in it
-                    if (__any_sync(0xffffffffu, fminf(min16<0>(r), min16<16>(r)) <= thr)) {
-                        const uint32_t mw = sign_mask32(r, thr_up);
-                        if (mw != 0u) {
-                            if (cnt < CAP) {
-                                lw[cnt * TM] = mw;
-                                lc[cnt * TM] = (uint8_t)(u * CPW + c);
-                                ++cnt;
-                            } else {
-                                ovf = true;
-                            }
+                if (!ok) break;
+                // both halves' bounds: the row's threshold. ERR: M2 is the second smallest 8-unit group minimum, an
+                // upper bound of the second smallest s~ (two groups have a unit at or below it), so the threshold
+                // derived from it keeps every possible second BMU.
+                sPart[(lb * HALVES + h) * TM + row] = make_float2(a1, a2);
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
+                if (!wwait(p_full + lb * 4 + q, (uint32_t)((k >> 1) & 1))) { fail(2048u); break; }
+                const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
+                const float M1 = fminf(p0.x, p1.x);
+                const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
+                const float mref = ERR ? M2 : M1;
+                flagged = !(xn < HUGE_S) || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
+                thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
+                // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
+                // floats never rounds to zero), so each value costs one subtraction and one shift of its sign bit
+                thr_up = nextafterf(thr, INFINITY);
+                // ---- the column tiles of sweep 2: those where a row of the tile has a candidate --------------------
+                // (a tile minimum at or under the threshold; both rounded outwards, so no candidate's tile is missed)
+                uint32_t ulo = 0, uhi = 0;
+                if (!flagged) {
+                    const float dlim = __fadd_ru(thr, xn);
+                    for (int u = 0; u < U; ++u) {
+                        if (__half2float(tmin[(size_t)u * TM]) <= dlim) {
+                            if (u < 32) ulo |= 1u << u;
+                            else uhi |= 1u << (u - 32);
                         }
                     }
-                });
-                TC_T(1);
+                }
+                ulo = __reduce_or_sync(0xffffffffu, ulo);
+                uhi = __reduce_or_sync(0xffffffffu, uhi);
+                if (lane == 0) {
+                    sUnion[lb * SWEEP_WARPS + warp] = ((uint64_t)uhi << 32) | ulo;
+                    ptx::mbar_arrive(u_full + lb);
+                }
             }
-            if (!ok) break;
-            sCnt[(lb * HALVES + h) * TM + row] = (uint8_t)(cnt | (ovf ? 0x80 : 0));
-            if (h == 0) {
-                sThr[lb * TM + row] = thr;
-                sFlag[lb * TM + row] = flagged ? 1 : 0;
+            if (k >= 1) {
+                const int64_t j = k - 1;
+                const int lb = (int)(j & 1);
+                // the resolvers are done with list buffer lb (row tile j - 2)
+                if (j >= 2 && !wwait(m_empty + lb, (uint32_t)(((j >> 1) - 1) & 1))) { fail(512u); break; }
+                TC_T(5);
+                if (!wwait(u_full + lb, (uint32_t)((j >> 1) & 1))) { fail(32768u); break; }
+                const uint64_t un = union_of(lb);
+                // ---- sweep 2: the candidate lists -------------------------------------------------------------------
+                const size_t lbase = (size_t)((lb * HALVES + h) * CAP) * TM + row;
+                uint32_t* lw = sLw + lbase;
+                uint8_t* lc = sLc + lbase;
+                int cnt = 0;
+                bool ovf = false;
+                for (uint64_t rest = un; rest != 0 && ok; rest &= rest - 1, ++gcons) {
+                    const int u = __ffsll((long long)rest) - 1;
+                    const int buf = (int)(gcons % NACC);
+                    if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) {
+                        fail(128u);
+                        ok = false;
+                        break;
+                    }
+                    TC_T(0);
+                    ptx::tc_fence_after();
+                    stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                        // the chunk's masks only when a row of the warp has a candidate in it
+                        if (__any_sync(0xffffffffu, fminf(min16<0>(r), min16<16>(r)) <= thr_p)) {
+                            const uint32_t mw = sign_mask32(r, thr_up_p);
+                            if (mw != 0u) {
+                                if (cnt < CAP) {
+                                    lw[cnt * TM] = mw;
+                                    lc[cnt * TM] = (uint8_t)(u * CPW + c);
+                                    ++cnt;
+                                } else {
+                                    ovf = true;
+                                }
+                            }
+                        }
+                    });
+                    TC_T(1);
+                }
+                if (!ok) break;
+                sCnt[(lb * HALVES + h) * TM + row] = (uint8_t)(cnt | (ovf ? 0x80 : 0));
+                if (h == 0) {
+                    sThr[lb * TM + row] = thr_p;
+                    sFlag[lb * TM + row] = flagged_p ? 1 : 0;
+                }
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(m_full + lb);
             }
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(m_full + lb);
+            thr_p = thr;
+            thr_up_p = thr_up;
+            flagged_p = flagged;
         }
     } else if (warp < SWEEP_WARPS + RES_WARPS) {
         // ------------------------------ resolvers: group g takes the row tiles it with it % RES_GROUPS == g ---------
@@ -1092,7 +1199,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
         }
     }
 #ifdef SOMGB_TC_PHASE_TIMING
-    if (lane == 0 && warp <= MMA_WARP)
+    if (lane == 0 && (warp <= MMA_WARP || warp == MMA_WARP2))
         for (int ph = 0; ph < TC_PHASES; ++ph) atomicAdd(&g_tc_phase_cycles[ph], _tc_acc[ph]);
 #endif
 
@@ -1253,6 +1360,8 @@ int launch_tc_pass(const PassArgs& a, void* ws, size_t ws_bytes, cudaStream_t st
     P.off_lc = s.off_lc;
     P.off_cnt = s.off_cnt;
     P.off_flag = s.off_flag;
+    P.off_tmin = s.off_tmin;
+    P.off_union = s.off_union;
     P.off_w = s.off_w;
     P.off_center = s.off_center;
     P.off_bar = s.off_bar;

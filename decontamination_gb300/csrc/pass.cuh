@@ -28,6 +28,7 @@ struct PassArgs {
     int32_t* train_bmu;    // OUT_TRAIN (n)
     unsigned long long* recheck_count;  // optional: samples that took the exact path
     unsigned int* status;  // optional: this call's status word (bounded waits that gave up), besides the global one
+    unsigned long long* sweep2_tiles;   // optional: column tiles the tensor-core pass's second sweeps computed
     int outs;
 };
 

@@ -90,7 +90,8 @@ class SOM_Batch(SOM_Abstract):
         are accumulated piece by piece), later epochs whole (pieces None, bounds complete). Generator datasets are
         uploaded every epoch, as the reference does."""
         if (dataset is None or is_array(dataset)) and (dataset_weights is None or is_array(dataset_weights)):
-            resident = []
+            resident = self._resident = []
+            self._regroup_bufs = {}
 
             def first():
                 for xr, rr in raw_chunks(dataset, dataset_weights):
@@ -99,7 +100,8 @@ class SOM_Batch(SOM_Abstract):
                     resident.append((xd, rd, bounds, None))
                     yield xd, rd, bounds, pieces
 
-            return lambda: first() if not resident else iter(resident)
+            return lambda: first() if not resident else iter(list(resident))
+        self._resident = None
         return lambda: ((*self._with_bounds(xc, rc, device), None)
                         for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device))
 
@@ -151,6 +153,36 @@ class SOM_Batch(SOM_Abstract):
             return
         _native.call('somgb_accumulate', xd.data_ptr(), _device.ptr(rd), self._bmu_buffer(n, xd.device).data_ptr(),
                      n, D, M, bounds.data_ptr(), S.data_ptr(), c.data_ptr(), _device.stream())
+
+    def _regroups(self, n):
+        """Whether the rows of a resident chunk of n rows are regrouped by BMU between epochs: when its passes take
+        the tensor-core path, whose second sweep then recomputes only the column tiles holding candidates, and the
+        map has more than one column tile (256 units)."""
+        M = self._m * self._n
+        if self._is_f64 or M <= 256 or n < 1024:
+            return False
+        algo = self._algo
+        if algo == _native.ALGO_FP32:
+            return False
+        return bool(_native.lib().somgb_algo_supported(algo, n, M, self._dim))
+
+    def _regroup(self, k, xd, rd, bounds, device):
+        """Replaces resident chunk k by its rows regrouped by the BMUs the epoch just found (somgb_sort_rows): each
+        row keeps its values and weight, so every result is unchanged. The rows go to one of two buffers allocated
+        here for the chunk, the one that is not the source; the caller's own tensors are never written."""
+        n, D, M = _device.rows(xd), self._dim, self._m * self._n
+        bufs = self._regroup_bufs.setdefault(k, [])
+        target = next((b for b in bufs if b[0] is not xd), None)
+        if target is None:
+            target = (torch.empty_like(xd), None if rd is None else torch.empty_like(rd))
+            bufs.append(target)
+        xs, rs = target
+        if getattr(self, '_sort_ws', None) is None:
+            self._sort_ws = _device.Workspace()
+        wsp, wsb = self._sort_ws.get(int(_native.lib().somgb_sort_rows_workspace_bytes(M)), device)
+        _native.call('somgb_sort_rows', xd.data_ptr(), _device.ptr(rd), self._bmu_buffer(n, device).data_ptr(), n, D,
+                     M, xs.data_ptr(), _device.ptr(rs), wsp, wsb, _device.stream())
+        self._resident[k] = (xs, rs, bounds, None)
 
     def _update(self, S, c, topo, sigma, w_out):
         """num = H S, den = H c, w = num / den, with the map's grid topography factorised by axis."""
@@ -214,7 +246,7 @@ class SOM_Batch(SOM_Abstract):
             c.zero_()
             err = errs[e] if with_errors else None
             last = e == n_epochs
-            for xd, rd, bounds, pieces in chunks():
+            for k, (xd, rd, bounds, pieces) in enumerate(chunks()):
                 if pieces is None:
                     pieces = [(0, _device.rows(xd))]
                 elif bounds is not None:
@@ -225,11 +257,15 @@ class SOM_Batch(SOM_Abstract):
                         self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
                     if not last:
                         self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
+                        if self._resident is not None and self._regroups(_device.rows(xd)):
+                            self._regroup(k, xd, rd, bounds, device)
                     continue
                 for a, b in pieces:
                     self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
                 if not last:
                     self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
+                    if self._resident is not None and self._regroups(_device.rows(xd)):
+                        self._regroup(k, xd, rd, bounds, device)
             if check_stop and e > 0 and with_errors:
                 qe, te = self._errors_of(errs[e].cpu().numpy())
                 if qe <= sq and te <= st:
@@ -251,6 +287,7 @@ class SOM_Batch(SOM_Abstract):
             for e in range(done):
                 self._quantization_errors[e], self._topographic_errors[e] = self._errors_of(eh[e + 1])
         self._weights[:] = history[done - 1].cpu().numpy() if done > 0 else self._weights
+        self._resident, self._regroup_bufs = None, {}   # the catalogue's device copies go with this call
         self._status.check()
 
     def _train_vectors(self, dataset, dataset_weights, n_vectors):

@@ -64,6 +64,11 @@ size_t somgb_workspace_bytes(int op, int64_t n, int64_t m, int d, int algo);
 /* Number of samples the last pass on this thread sent to the exact recheck (diagnostic; synchronises `stream`). */
 int somgb_last_recheck_count(int64_t* count, somgb_stream_t stream);
 
+/* Column tiles (256 units each) the second sweeps of the last tensor-core pass on this thread computed, summed over
+ * its 128-row tiles; their first sweeps compute every column tile (diagnostic; 0 after a CUDA-core pass;
+ * synchronises `stream`). */
+int somgb_last_sweep2_tiles(int64_t* tiles, somgb_stream_t stream);
+
 /*
  * Device status word of the current device (synchronises `stream`): 0 while healthy; non-zero once a bounded
  * device-side wait of a tensor-core pass gave up, in which case that pass returned early and its outputs are
@@ -178,6 +183,18 @@ int somgb_accumulate(const float* x, const double* rho, const int32_t* bmu, int6
                      const float* bounds, double* S, double* c, somgb_stream_t stream);
 int somgb_accumulate_f64(const double* x, const double* rho, const int32_t* bmu, int64_t n, int d, int64_t m,
                          double* S, double* c, somgb_stream_t stream);
+
+/*
+ * Row regrouping between epochs (no counterpart in the reference, which visits the catalogue in storage order,
+ * algo/som_batch.py:285-376): x_out/rho_out receive the rows of x/rho grouped by key (the rows of key k contiguous,
+ * in increasing k; keys outside [0, m) last; the order within a key unspecified). With the keys the BMUs an epoch just
+ * found, the 128-row tiles of the next tensor-core pass each meet few column tiles of candidates, and its second
+ * sweep recomputes only those; no row's result depends on the order. rho/rho_out may be NULL. Workspace:
+ * somgb_sort_rows_workspace_bytes(m).
+ */
+size_t somgb_sort_rows_workspace_bytes(int64_t m);
+int somgb_sort_rows(const float* x, const double* rho, const int32_t* key, int64_t n, int d, int64_t m,
+                    float* x_out, double* rho_out, void* ws, size_t ws_bytes, somgb_stream_t stream);
 
 /*
  * Neighbourhood contraction and weight update of one epoch:
