@@ -284,6 +284,10 @@ class EpochRunner:
         self.ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
         self.wsp = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
         self.wsb = nbytes
+        # the pass's sweep-2 column-tile counter (workspace header word 2), copied on the device after every pass
+        off = self.wsp - self.ws.data_ptr()
+        self.sweep2_word = self.ws[off + 16:off + 24].view(torch.int64)
+        self.sweep2_log = []
         self.penalty = 2.0 if w['topology'] == 'square' else 1.0
         nb = int(native.lib().somgb_neighbourhood_grid_workspace_bytes(w['m'], w['n'], self.D))
         self.upd_ws = torch.empty(nb, dtype=torch.uint8, device=device)
@@ -314,6 +318,7 @@ class EpochRunner:
                  self.wsp, self.wsb, s)
         if timer is not None:
             nat.call('somgb_set_kernel_timer', None, None)
+        self.sweep2_log.append(self.sweep2_word.clone())
         if phases is not None:
             phases[1].record()
         nat.call('somgb_accumulate', self.xd.data_ptr(), None, self.bmu.data_ptr(), self.N, self.D, self.M,
@@ -356,6 +361,7 @@ def time_epochs(torch, runner, warmup, steps, sustain_s=0.0):
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     launches0 = runner.nat.lib().somgb_kernel_launches()
+    runner.sweep2_log = []
     start.record()
     for i in range(steps):
         runner.step(errs[warmup + i], timer=kt[i])
@@ -363,6 +369,7 @@ def time_epochs(torch, runner, warmup, steps, sustain_s=0.0):
     torch.cuda.synchronize()
     launches = runner.nat.lib().somgb_kernel_launches() - launches0
     rechecks = runner.rechecks()
+    runner.timed_sweep2 = [int(t.item()) for t in runner.sweep2_log]   # per timed epoch
     total_ms = start.elapsed_time(stop)
     kernel_ms = [a.elapsed_time(b) for a, b in kt]
     extra = torch.zeros(3, dtype=torch.float64, device=runner.dev)
@@ -583,13 +590,17 @@ def gpu_arm(args, ws, rank, local):
                 'hbm_bytes_algorithmic': N * D * 4 + N * 4,
                 'hbm_frac': (N * D * 4 + N * 4) / (k_ms * 1e-3) / 1e9 / peaks.get('hbm_gbs', 6800.0)}
     if used_algo == 'tc':
-        # what the tensor pipe executes: two sweeps (the second recomputes the MMAs) of the split-FP16 contraction over
-        # the padded map, K = 16 x K-steps (lo.hi, hi.lo, hi.hi blocks and the |w|^2 step)
+        # What the tensor pipe executes: 128-row x 256-unit column tiles of the split-FP16 contraction, K = 16 x K-steps
+        # (lo.hi, hi.lo, hi.hi blocks and the |w|^2 step); sweep 1 computes every column tile of each row tile, sweep 2
+        # those with a candidate (counted by the pass).
         k_steps = 3 * (D // 16) + 1 if D % 16 == 0 else (3 * D + 2 + 15) // 16
-        m_pad = (M + 255) // 256 * 256
-        executed = 2 * 2.0 * N * m_pad * (16 * k_steps) / (k_ms * 1e-3) / 1e12
+        row_tiles, col_tiles = (N + 127) // 128, (M + 255) // 256
+        sweep2 = statistics.mean(runner.timed_sweep2)
+        tiles = row_tiles * col_tiles + sweep2
+        executed = tiles * 2.0 * 128 * 256 * (16 * k_steps) / (k_ms * 1e-3) / 1e12
         roofline['executed_tensor_tflops'] = executed
         roofline['executed_frac'] = executed / peak
+        roofline['column_tiles_per_row_tile'] = {'sweep1': col_tiles, 'sweep2': sweep2 / row_tiles}
     out = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,

@@ -86,6 +86,77 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_scatter_kernel(const float*
         unsigned long long first = 0;
         if (in && leader == lane) first = atomicAdd(cursor + b, (unsigned long long)__popc(same));
         first = __shfl_sync(0xffffffffu, first, leader);
+        // one bucket for the whole warp (b names a bucket, so every lane's row exists): 32 consecutive rows to 32
+        // consecutive slots
+        if (VEC == 4 && same == 0xffffffffu && b != ~0ull) {
+            const int64_t i0 = i - lane, p0 = (int64_t)first;
+            const float4* src = (const float4*)(x + i0 * d);
+            float4* dst = (float4*)(x_out + p0 * d);
+            for (int k = lane; k < 8 * d; k += 32) dst[k] = __ldg(src + k);
+            if (rho) rho_out[p0 + lane] = rho[i];
+            continue;
+        }
+        if (!in) continue;
+        const int64_t pos = (int64_t)(first + (unsigned long long)__popc(same & below));
+        if (VEC == 4) {
+            const float4* src = (const float4*)(x + i * d);
+            float4* dst = (float4*)(x_out + pos * d);
+            for (int k = 0; k < d / 4; ++k) dst[k] = __ldg(src + k);
+        } else {
+            for (int k = 0; k < d; ++k) x_out[pos * d + k] = __ldg(x + i * d + k);
+        }
+        if (rho) rho_out[pos] = rho[i];
+    }
+}
+
+// The same scatter for regrouped keys (long runs of one key along the rows) and m + 1 buckets in shared memory: block
+// b moves the contiguous rows [b * chunk, (b + 1) * chunk), first counting its rows per bucket, then taking each
+// bucket's slots with one global atomic, then placing its rows. Few blocks share a bucket, where the row-wise form
+// makes every warp of a long run contend for the same counter.
+constexpr int SORT_BLOCK_THREADS = 512;
+template <int VEC>
+__global__ void __launch_bounds__(SORT_BLOCK_THREADS) sort_scatter_block_kernel(
+    const float* __restrict__ x, const double* __restrict__ rho, const int32_t* __restrict__ key, int64_t n, int d,
+    int64_t m, int64_t chunk, unsigned long long* __restrict__ cursor, float* __restrict__ x_out,
+    double* __restrict__ rho_out) {
+    extern __shared__ unsigned long long slot[];   // [m + 1]: this block's rows per bucket, then its next slot
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = min64(n, r0 + chunk);
+    for (int64_t b = threadIdx.x; b <= m; b += SORT_BLOCK_THREADS) slot[b] = 0;
+    __syncthreads();
+    for (int64_t base = r0; base < r1; base += SORT_BLOCK_THREADS) {
+        const int64_t i = base + threadIdx.x;
+        const bool in = i < r1;
+        const unsigned long long b = in ? sort_bucket(key[i], m) : ~0ull;
+        const unsigned same = __match_any_sync(0xffffffffu, b);
+        if (in && __ffs(same) - 1 == lane) atomicAdd(slot + b, (unsigned long long)__popc(same));
+    }
+    __syncthreads();
+    for (int64_t b = threadIdx.x; b <= m; b += SORT_BLOCK_THREADS) {
+        const unsigned long long c = slot[b];
+        if (c) slot[b] = atomicAdd(cursor + b, c);
+    }
+    __syncthreads();
+    for (int64_t base = r0; base < r1; base += SORT_BLOCK_THREADS) {
+        const int64_t i = base + threadIdx.x;
+        const bool in = i < r1;
+        const unsigned long long b = in ? sort_bucket(key[i], m) : ~0ull;
+        const unsigned same = __match_any_sync(0xffffffffu, b);
+        const int leader = __ffs(same) - 1;
+        unsigned long long first = 0;
+        if (in && leader == lane) first = atomicAdd(slot + b, (unsigned long long)__popc(same));
+        first = __shfl_sync(0xffffffffu, first, leader);
+        // one bucket for the whole warp (b names a bucket, so every lane's row exists): 32 consecutive rows to 32
+        // consecutive slots
+        if (VEC == 4 && same == 0xffffffffu && b != ~0ull) {
+            const int64_t i0 = i - lane, p0 = (int64_t)first;
+            const float4* src = (const float4*)(x + i0 * d);
+            float4* dst = (float4*)(x_out + p0 * d);
+            for (int k = lane; k < 8 * d; k += 32) dst[k] = __ldg(src + k);
+            if (rho) rho_out[p0 + lane] = rho[i];
+            continue;
+        }
         if (!in) continue;
         const int64_t pos = (int64_t)(first + (unsigned long long)__popc(same & below));
         if (VEC == 4) {
@@ -116,6 +187,17 @@ int launch_sort_rows(const float* x, const double* rho, const int32_t* key, int6
     sort_scan_kernel<<<1, 1024, 0, stream>>>(counts, m + 1, cursor);
     SOMGB_LAUNCH_CHECK();
     const bool vec = d % 4 == 0 && ((uintptr_t)x) % 16 == 0 && ((uintptr_t)x_out) % 16 == 0;
+    const size_t smem = (size_t)(m + 1) * 8;
+    if (smem <= 96 * 1024) {   // the buckets fit shared memory: two blocks per SM, contiguous row ranges
+        const int64_t blocks = std::min<int64_t>(ceil_div(n, SORT_BLOCK_THREADS), 2 * (int64_t)num_sms());
+        const int64_t chunk = ceil_div(n, blocks);
+        auto kern = vec ? sort_scatter_block_kernel<4> : sort_scatter_block_kernel<1>;
+        SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<(unsigned)ceil_div(n, chunk), SORT_BLOCK_THREADS, smem, stream>>>(x, rho, key, n, d, m, chunk, cursor,
+                                                                                 x_out, rho_out);
+        SOMGB_LAUNCH_CHECK();
+        return SOMGB_OK;
+    }
     if (vec)
         sort_scatter_kernel<4><<<grid, SORT_THREADS, 0, stream>>>(x, rho, key, n, d, m, cursor, x_out, rho_out);
     else
