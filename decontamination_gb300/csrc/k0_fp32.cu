@@ -273,7 +273,9 @@ __global__ void __launch_bounds__(KR_THREADS) k0_rows_kernel(PassArgs a, const i
     const float g = (float)(d + 2) * 5.9604645e-8f;
     const float fac = 1.0f + 8.0f * g;
     double e0 = 0.0, e1 = 0.0, e2 = 0.0;
-    for (int64_t r = (int64_t)blockIdx.x * (KR_THREADS / 32) + (threadIdx.x >> 5); r < total; r += nwarps) {
+    // listed row r to warp r / gridDim.x of block r % gridDim.x: a short list spreads over every SM, one row per
+    // block, instead of filling the warps of a few blocks (each row scans the whole map)
+    for (int64_t r = (int64_t)blockIdx.x + (int64_t)(threadIdx.x >> 5) * gridDim.x; r < total; r += nwarps) {
         const int64_t i = rows[r];
         const float* xg = a.x + i * d;
         float xl[DMAX > 0 ? DMAX : 1];

@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_scatter_kernel(const float*
             const int64_t i0 = i - lane, p0 = (int64_t)first;
             const float4* src = (const float4*)(x + i0 * d);
             float4* dst = (float4*)(x_out + p0 * d);
+#pragma unroll 4   // several loads in flight per lane
             for (int k = lane; k < 8 * d; k += 32) dst[k] = __ldg(src + k);
             if (rho) rho_out[p0 + lane] = rho[i];
             continue;
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_scatter_kernel(const float*
         if (VEC == 4) {
             const float4* src = (const float4*)(x + i * d);
             float4* dst = (float4*)(x_out + pos * d);
+#pragma unroll 4
             for (int k = 0; k < d / 4; ++k) dst[k] = __ldg(src + k);
         } else {
             for (int k = 0; k < d; ++k) x_out[pos * d + k] = __ldg(x + i * d + k);
@@ -153,6 +155,7 @@ __global__ void __launch_bounds__(SORT_BLOCK_THREADS) sort_scatter_block_kernel(
             const int64_t i0 = i - lane, p0 = (int64_t)first;
             const float4* src = (const float4*)(x + i0 * d);
             float4* dst = (float4*)(x_out + p0 * d);
+#pragma unroll 4   // several loads in flight per lane
             for (int k = lane; k < 8 * d; k += 32) dst[k] = __ldg(src + k);
             if (rho) rho_out[p0 + lane] = rho[i];
             continue;
@@ -162,6 +165,7 @@ __global__ void __launch_bounds__(SORT_BLOCK_THREADS) sort_scatter_block_kernel(
         if (VEC == 4) {
             const float4* src = (const float4*)(x + i * d);
             float4* dst = (float4*)(x_out + pos * d);
+#pragma unroll 4
             for (int k = 0; k < d / 4; ++k) dst[k] = __ldg(src + k);
         } else {
             for (int k = 0; k < d; ++k) x_out[pos * d + k] = __ldg(x + i * d + k);

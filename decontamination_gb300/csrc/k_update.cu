@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
                                                                        const double* __restrict__ rho,
                                                                        const int32_t* __restrict__ bmu, int64_t n,
                                                                        int d, int64_t units_per_range, int64_t m,
-                                                                       int64_t chunk, const float* __restrict__ bounds,
+                                                                       int64_t chunk, int stripes, const float* __restrict__ bounds,
                                                                        double* __restrict__ S, double* __restrict__ c) {
     // [3][cnt * d] feature limbs, [cnt] counts or [3][cnt] weight limbs, then the warps' sample lists [32][128]
     extern __shared__ int32_t lane_bins[];
@@ -264,7 +264,13 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
     const uint32_t lt_mask = (1u << lane) - 1u;
     int32_t hot = -1;              // HOT: this slot's register-held unit (relative to lo), -1 before the first sample
     long long hacc = 0, hw = 0;    // its feature-k sum and its count (or weight sum) in fixed point
-    const int64_t s0 = (int64_t)blockIdx.x * chunk;
+    // CTA x takes slice x of each of the `stripes` stripes of gridDim.x * chunk samples: on rows grouped by BMU every
+    // unit range then meets samples in every CTA, instead of a few CTAs holding all of a range's samples
+    const int64_t span = (int64_t)gridDim.x * chunk, first = (int64_t)blockIdx.x * chunk;
+    const int t_last = first < n ? (int)min64(stripes - 1, (n - 1 - first) / span) : -1;   // its last non-empty slice
+    for (int t = 0; t <= t_last; ++t) {
+    const bool last_stripe = t == t_last;   // the bins are flushed at the end of it
+    const int64_t s0 = t * span + first;
     const int64_t s1 = min64(n, s0 + chunk);
     for (int64_t w0 = s0; w0 < s1; w0 += SCAN) {
         const int64_t w1 = min64(s1, w0 + SCAN);
@@ -338,7 +344,7 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
             __syncwarp();   // the list is rewritten by the next batch
         }
         __syncthreads();
-        const bool flush = w1 == s1 || added_s + SCAN > FX_WINDOW;
+        const bool flush = (w1 == s1 && last_stripe) || added_s + SCAN > FX_WINDOW;
         __syncthreads();   // every thread has read added_s
         if (!flush) continue;
         if (threadIdx.x == 0) added_s = 0;
@@ -380,6 +386,7 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
             else atomicAdd(c + lo + uu, val);
         }
         __syncthreads();
+    }
     }
 }
 
@@ -674,6 +681,13 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
     int64_t chunk = std::max<int64_t>(4096, ceil_div(n, chunks));
     chunk = ceil_div(chunk, ACC_BATCH) * ACC_BATCH;
     chunks = ceil_div(n, chunk);
+    // with several unit ranges, each CTA's samples come from `ranges` stripes of the dataset (slices of chunk / ranges
+    // samples, multiples of ACC_BATCH), so that rows grouped by BMU still give every range CTA a share
+    int stripes = 1;
+    if (ranges > 1 && chunk >= ranges * (int64_t)ACC_BATCH) {
+        stripes = (int)ranges;
+        chunk = ceil_div(ceil_div(n, chunks * stripes), ACC_BATCH) * ACC_BATCH;
+    }
     const dim3 grid((unsigned)chunks, (unsigned)ranges);
     if (lanes) {
         const bool hot = ranges > 1;
@@ -683,7 +697,8 @@ int launch_accumulate(const T* x, const double* rho, const int32_t* bmu, int64_t
         else if (d <= 16) kern = hot ? accumulate_lanes_kernel<16, true> : accumulate_lanes_kernel<16, false>;
         if (smem > 48 * 1024)
             SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<grid, ACC_THREADS, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, bounds, S, c);
+        kern<<<grid, ACC_THREADS, smem, stream>>>((const float*)x, rho, bmu, n, d, upr, m, chunk, stripes, bounds, S,
+                                                  c);
         SOMGB_LAUNCH_CHECK();
         return SOMGB_OK;
     }
