@@ -155,9 +155,10 @@ class SOM_Batch(SOM_Abstract):
                      n, D, M, bounds.data_ptr(), S.data_ptr(), c.data_ptr(), _device.stream())
 
     def _regroups(self, n):
-        """Whether the rows of a resident chunk of n rows are regrouped by BMU between epochs: when its passes take
-        the tensor-core path, whose second sweep then recomputes only the column tiles holding candidates, and the
-        map has more than one column tile (256 units)."""
+        """Whether the rows of a resident chunk of n rows are regrouped by BMU between training epochs (not after the
+        last one: the final error pass keeps the grouping of the epoch before): when its passes take the tensor-core
+        path, whose second sweep then recomputes only the column tiles holding candidates, and the map has more than
+        one column tile (256 units)."""
         M = self._m * self._n
         if self._is_f64 or M <= 256 or n < 1024:
             return False
@@ -257,14 +258,14 @@ class SOM_Batch(SOM_Abstract):
                         self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
                     if not last:
                         self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
-                        if self._resident is not None and self._regroups(_device.rows(xd)):
+                        if self._resident is not None and e + 1 < n_epochs and self._regroups(_device.rows(xd)):
                             self._regroup(k, xd, rd, bounds, device)
                     continue
                 for a, b in pieces:
                     self._piece_pass(xd, rd, a, b, last, with_errors, w, topo, err, e, device)
                 if not last:
                     self._accumulate(xd, rd, bounds, S, c, w, topo, err if e > 0 else None)
-                    if self._resident is not None and self._regroups(_device.rows(xd)):
+                    if self._resident is not None and e + 1 < n_epochs and self._regroups(_device.rows(xd)):
                         self._regroup(k, xd, rd, bounds, device)
             if check_stop and e > 0 and with_errors:
                 qe, te = self._errors_of(errs[e].cpu().numpy())

@@ -140,7 +140,7 @@ def test_training_regroups_rows_without_changing_results(cuda, native):
             inner = som._regroup
             som._regroup = lambda *a: (calls.append(1), inner(*a))
         som.train(x, n_epochs=E, use_best_epoch=False)
-        assert len(calls) == (E if regroup else 0)
+        assert len(calls) == (E - 1 if regroup else 0)   # between training epochs
         runs.append((som._history.copy(), som.quantization_errors.copy(), som.topographic_errors.copy()))
     assert np.array_equal(runs[0][0], runs[1][0])
     np.testing.assert_allclose(runs[0][1], runs[1][1], rtol=1e-12)
