@@ -877,6 +877,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             process(CPW - 1, rb);
         };
 
+        // The same with loads that also return each lane's chunk minimum: process(c, values, minimum).
+        auto stream_tile_red = [&](int buf, auto&& process) {
+            const uint32_t base = tbase + lane_base + (uint32_t)(buf * TN + h * HW);
+            uint32_t ra[32], rb[32];
+            float fa, fb;
+            ptx::tmem_ldred32_raw(base, ra, fa);
+            ptx::tmem_wait_ld_red(ra, fa);
+#pragma unroll
+            for (int c = 0; c + 2 < CPW; c += 2) {
+                ptx::tmem_ldred32_raw(base + 32 * (c + 1), rb, fb);
+                process(c, ra, fa);
+                ptx::tmem_wait_ld_red(rb, fb);
+                ptx::tmem_ldred32_raw(base + 32 * (c + 2), ra, fa);
+                process(c + 1, rb, fb);
+                ptx::tmem_wait_ld_red(ra, fa);
+            }
+            ptx::tmem_ldred32_raw(base + 32 * (CPW - 1), rb, fb);
+            process(CPW - 2, ra, fa);
+            ptx::tmem_wait_ld_red(rb, fb);
+            release(buf);
+            process(CPW - 1, rb, fb);
+        };
+
         // the chunk's minimum; for ERR it also folds the chunk's four 8-unit group minima into the running two
         // smallest (a1, a2), else the minimum into a1
         auto chunk_min = [&](const uint32_t (&r)[32], float& a1, float& a2) -> float {
@@ -989,9 +1012,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     }
                     TC_T(0);
                     ptx::tc_fence_after();
-                    stream_tile(buf, [&](int c, const uint32_t (&r)[32]) {
+                    stream_tile_red(buf, [&](int c, const uint32_t (&r)[32], float red) {
                         // the chunk's masks only when a row of the warp has a candidate in it
-                        if (__any_sync(0xffffffffu, fminf(min16<0>(r), min16<16>(r)) <= thr_p)) {
+                        if (__any_sync(0xffffffffu, red <= thr_p)) {
                             const uint32_t mw = sign_mask32(r, thr_up_p);
                             if (mw != 0u) {
                                 if (cnt < CAP) {
