@@ -86,16 +86,17 @@ def _smooth_map(m, n, d, rng):
     return np.tanh(g @ rng.standard_normal((2, d)) * 2.0 + rng.standard_normal(d)).astype(np.float32)
 
 
-@pytest.mark.parametrize('kind', ['random', 'smooth', 'clustered'])
+@pytest.mark.parametrize('kind,d', [('random', 16), ('smooth', 16), ('clustered', 16), ('smooth', 4), ('smooth', 8),
+                                    ('smooth', 32)])
 @pytest.mark.parametrize('with_err', [False, True])
-def test_tc_pass_on_rows_grouped_by_bmu(cuda, native, oracle, kind, with_err):
-    """A 64x64 map (16 column tiles of 256 units), rows grouped by their BMU. Random: units are catalogue rows, so a
+def test_tc_pass_on_rows_grouped_by_bmu(cuda, native, oracle, kind, d, with_err):
+    """A 64x64 map (16 column tiles of 256 units), D = 4 to 32, rows grouped by their BMU. Random: units are catalogue rows, so a
     row's candidates lie anywhere in the map and every column tile is recomputed. Smooth: the units lie on a sheet
     ordered along the grid, as in a trained map, and the rows near it, so a row tile's candidates lie in a few column
     tiles. Clustered: the rows lie near 40 units only. A few rows are not finite (they go to the exact recheck)."""
     rng = np.random.default_rng(41 + len(kind))
     m = n = 64
-    M, d, N = m * n, 16, 60_000
+    M, N = m * n, 60_000
     if kind == 'random':
         x = synthetic.correlated_lognormal(N, d, 12)
         w = (x[rng.integers(0, N, M)] * (1 + 0.02 * rng.standard_normal((M, d)))).astype(np.float32)
@@ -103,7 +104,7 @@ def test_tc_pass_on_rows_grouped_by_bmu(cuda, native, oracle, kind, with_err):
         w = _smooth_map(m, n, d, rng)
         pick = rng.integers(0, M, N) if kind == 'smooth' else rng.choice(M, 40, replace=False)[rng.integers(0, 40, N)]
         x = (w[pick] + 0.01 * rng.standard_normal((N, d))).astype(np.float32)
-    x[rng.choice(N, 7, replace=False), 3] = np.nan
+    x[rng.choice(N, 7, replace=False), d - 1] = np.nan
     topo = oracle.topography(m, n, 'square')
     order = np.argsort(oracle.find_bmus(w, x, 'numba'), kind='stable')
     xs = np.ascontiguousarray(x[order])
