@@ -932,11 +932,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
             TC_T(4);
             float thr = -INFINITY, thr_up = -INFINITY;
             bool flagged = true;
+            float a1 = INFINITY, a2 = INFINITY;   // row tile k's bounds over this half's columns
+            __half* const tmin = sTmin + (size_t)h * U * TM + row;   // the row's minimum over its half of each tile
             if (k < n_my) {
-                const int lb = (int)(k & 1);
                 // ---- sweep 1: the row's bounds over this half's columns --------------------------------------------
-                float a1 = INFINITY, a2 = INFINITY;
-                __half* tmin = sTmin + (size_t)h * U * TM + row;   // the row's minimum over its half of each tile
                 for (int u = 0; u < U && ok; ++u, ++gcons) {
                     const int buf = (int)(gcons % NACC);
                     if (!wwait(t_full + buf, (uint32_t)((gcons / NACC) & 1))) {
@@ -953,40 +952,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                     TC_T(1);
                 }
                 if (!ok) break;
-                // both halves' bounds: the row's threshold. ERR: M2 is the second smallest 8-unit group minimum, an
-                // upper bound of the second smallest s~ (two groups have a unit at or below it), so the threshold
-                // derived from it keeps every possible second BMU.
-                sPart[(lb * HALVES + h) * TM + row] = make_float2(a1, a2);
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
-                if (!wwait(p_full + lb * 4 + q, (uint32_t)((k >> 1) & 1))) { fail(2048u); break; }
-                const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
-                const float M1 = fminf(p0.x, p1.x);
-                const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
-                const float mref = ERR ? M2 : M1;
-                flagged = !(xn < HUGE_S) || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
-                thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
-                // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
-                // floats never rounds to zero), so each value costs one subtraction and one shift of its sign bit
-                thr_up = nextafterf(thr, INFINITY);
-                // ---- the column tiles of sweep 2: those where a row of the tile has a candidate --------------------
-                // (a tile minimum at or under the threshold; both rounded outwards, so no candidate's tile is missed)
-                uint32_t ulo = 0, uhi = 0;
-                if (!flagged) {
-                    const float dlim = __fadd_ru(thr, xn);
-                    for (int u = 0; u < U; ++u) {
-                        if (__half2float(tmin[(size_t)u * TM]) <= dlim) {
-                            if (u < 32) ulo |= 1u << u;
-                            else uhi |= 1u << (u - 32);
-                        }
-                    }
-                }
-                ulo = __reduce_or_sync(0xffffffffu, ulo);
-                uhi = __reduce_or_sync(0xffffffffu, uhi);
-                if (lane == 0) {
-                    sUnion[lb * SWEEP_WARPS + warp] = ((uint64_t)uhi << 32) | ulo;
-                    ptx::mbar_arrive(u_full + lb);
-                }
             }
             if (k >= 1) {
                 const int64_t j = k - 1;
@@ -1037,6 +1002,46 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) tc_pass_kernel(const __grid_co
                 }
                 __syncwarp();
                 if (lane == 0) ptx::mbar_arrive(m_full + lb);
+            }
+            // Row tile k's threshold and the column tiles of its sweep 2, after sweep 2 of row tile k - 1: its MMAs
+            // were issued behind those of sweep 1, so the tensor pipe computes the next sweep 1's first column tiles
+            // while this exchange runs, and the tile set is still published a whole sweep 1 before it is needed.
+            if (k < n_my) {
+                const int lb = (int)(k & 1);
+                // both halves' bounds: the row's threshold. ERR: M2 is the second smallest 8-unit group minimum, an
+                // upper bound of the second smallest s~ (two groups have a unit at or below it), so the threshold
+                // derived from it keeps every possible second BMU.
+                sPart[(lb * HALVES + h) * TM + row] = make_float2(a1, a2);
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(p_full + lb * 4 + q);
+                if (!wwait(p_full + lb * 4 + q, (uint32_t)((k >> 1) & 1))) { fail(2048u); break; }
+                const float2 p0 = sPart[(lb * HALVES + 0) * TM + row], p1 = sPart[(lb * HALVES + 1) * TM + row];
+                const float M1 = fminf(p0.x, p1.x);
+                const float M2 = fminf(fmaxf(p0.x, p1.x), fminf(p0.y, p1.y));
+                const float mref = ERR ? M2 : M1;
+                flagged = !(xn < HUGE_S) || !(M1 + xn < HUGE_S) || !(mref < HUGE_S);
+                thr = flagged ? -INFINITY : thr_of(mref, xn, fmaf(P.alpha, xn, GAMMA), P.beta, P.kthr);
+                // v <= thr  <=>  v - thr_up < 0 with thr_up the next float above thr (exact: a difference of distinct
+                // floats never rounds to zero), so each value costs one subtraction and one shift of its sign bit
+                thr_up = nextafterf(thr, INFINITY);
+                // ---- the column tiles of sweep 2: those where a row of the tile has a candidate --------------------
+                // (a tile minimum at or under the threshold; both rounded outwards, so no candidate's tile is missed)
+                uint32_t ulo = 0, uhi = 0;
+                if (!flagged) {
+                    const float dlim = __fadd_ru(thr, xn);
+                    for (int u = 0; u < U; ++u) {
+                        if (__half2float(tmin[(size_t)u * TM]) <= dlim) {
+                            if (u < 32) ulo |= 1u << u;
+                            else uhi |= 1u << (u - 32);
+                        }
+                    }
+                }
+                ulo = __reduce_or_sync(0xffffffffu, ulo);
+                uhi = __reduce_or_sync(0xffffffffu, uhi);
+                if (lane == 0) {
+                    sUnion[lb * SWEEP_WARPS + warp] = ((uint64_t)uhi << 32) | ulo;
+                    ptx::mbar_arrive(u_full + lb);
+                }
             }
             thr_p = thr;
             thr_up_p = thr_up;
