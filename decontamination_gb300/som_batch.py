@@ -163,9 +163,9 @@ class SOM_Batch(SOM_Abstract):
         if self._is_f64 or M <= 256 or n < 1024:
             return False
         algo = self._algo
-        if algo == _native.ALGO_FP32:
-            return False
-        return bool(_native.lib().somgb_algo_supported(algo, n, M, self._dim))
+        if algo == _native.ALGO_FP32 or (algo == _native.ALGO_AUTO and n * M < (1 << 22)):
+            return False   # the CUDA-core form (AUTO takes it below 2^22 sample-units) has no second sweep to spare
+        return bool(_native.lib().somgb_algo_supported(_native.ALGO_TC, n, M, self._dim))
 
     def _regroup(self, k, xd, rd, bounds, device):
         """Replaces resident chunk k by its rows regrouped by the BMUs the epoch just found (somgb_sort_rows): each

@@ -187,3 +187,18 @@ def test_piece_edges_cover_the_chunk(n):
     assert all(v % 16 == 0 for v in e[:-1])
     sizes = [b - a for a, b in zip(e, e[1:])]
     assert max(sizes) - min(sizes) <= 32
+
+
+def test_regrouping_is_decided_without_a_device():
+    """Rows are regrouped between epochs only for the tensor-core form on maps of more than one 256-unit column tile,
+    catalogues of 1024 rows or more, and (under auto) passes of at least 2^22 sample-units; these cases are decided
+    before any device query."""
+    import decontamination_gb300 as dg
+    small = dg.SOM_Batch(8, 8, 16)
+    assert not small._regroups(10_000_000)            # one column tile
+    som = dg.SOM_Batch(32, 32, 16)
+    assert not som._regroups(512)                     # too few rows
+    som.bmu_algo = 'fp32'
+    assert not som._regroups(10_000_000)              # the CUDA-core form
+    som.bmu_algo = 'auto'
+    assert not som._regroups(2_000)                   # auto takes the CUDA-core form below 2^22 sample-units
