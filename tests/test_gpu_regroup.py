@@ -147,3 +147,23 @@ def test_training_regroups_rows_without_changing_results(cuda, native):
     np.testing.assert_allclose(runs[0][1], runs[1][1], rtol=1e-12)
     np.testing.assert_allclose(runs[0][2], runs[1][2], rtol=1e-12)
     assert torch.equal(x, x0), "the caller's tensor is left as it was"
+
+
+def test_row_tiles_with_no_candidates_and_with_one_tile(cuda, native, oracle):
+    """Whole 128-row tiles whose rows are all non-finite (every row flagged: an empty tile set for sweep 2, every row
+    to the exact recheck), and whole tiles of one repeated row (a single column tile), between ordinary rows."""
+    rng = np.random.default_rng(77)
+    m = n = 64
+    M, d, N = m * n, 16, 20_000
+    w = _smooth_map(m, n, d, rng)
+    x = (w[rng.integers(0, M, N)] + 0.01 * rng.standard_normal((N, d))).astype(np.float32)
+    x[128:384] = np.nan                 # row tiles 1 and 2
+    x[640:1024] = x[5000]               # row tiles 5 to 7: one row
+    topo = oracle.topography(m, n, 'square')
+    for with_err in (False, True):
+        bmu, err, tiles = _pass(native, cuda, x, w, topo, 2.0, with_err)
+        want = oracle.find_bmus(w, x, 'numba')
+        if with_err:
+            want = np.where(np.isfinite(x).all(1), want, -1)
+            np.testing.assert_allclose(err, oracle.compute_errors_raw(w, topo, x, None, 2.0, 'numba'), rtol=ERR_RTOL)
+        np.testing.assert_array_equal(bmu, want)
