@@ -75,6 +75,7 @@ SIGNATURES = {
     'somgb_neighbourhood_update_f64': [P, P, P, I64, I32, D, P, P, P, P],
     'somgb_train_iter_pass': [P, P, I64, I32, P, P, I64, D, I64, I64, P, P, P, SZ, P],
     'somgb_train_iter_pass_f64': [P, P, I64, I32, P, P, I64, D, I64, I64, P, P, P, SZ, P],
+    'somgb_train_iter_pass_grid': [P, P, I64, I32, P, P, I64, I64, D, I64, I64, I32, P, P, P, SZ, P],
     'somgb_divide': [P, P, I64, I32, P, P],
     'somgb_divide_f64': [P, P, I64, I32, P, P],
 }

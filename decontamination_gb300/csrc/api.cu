@@ -19,6 +19,9 @@ int launch_neighbourhood_grid(const double* S, const double* c, const T* topo, i
                               cudaStream_t stream);
 size_t grid_neighbourhood_workspace(int64_t rows, int64_t cols, int d);
 size_t sort_rows_workspace(int64_t m);
+int launch_iter_grid(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, const float* topo,
+                     int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors, double* num,
+                     double* den, cudaStream_t stream);
 int launch_sort_rows(const float* x, const double* rho, const int32_t* key, int64_t n, int d, int64_t m,
                      float* x_out, double* rho_out, void* ws, size_t ws_bytes, cudaStream_t stream);
 int launch_bmu_histograms(const int32_t* bmu, const double* rho, int64_t n, int64_t m, double* hist_w, double* hist_c,
@@ -413,6 +416,27 @@ int somgb_train_iter_pass(const float* x, const double* rho, int64_t n, int d, c
     a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.train_bmu = W.train_bmu; a.outs = OUT_TRAIN;
     if (int s = run_pass(a, SOMGB_ALGO_FP32, W, false, st)) return s;
     return launch_iter<float>(x, rho, W.train_bmu, n, d, topo, m, sigma0, cur_vector, n_vectors, num, den, st);
+}
+
+int somgb_train_iter_pass_grid(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                               int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors,
+                               int algo, double* num, double* den, void* ws, size_t ws_bytes, somgb_stream_t stream) {
+    if (rows <= 0 || cols <= 0) return set_error(SOMGB_ERR_INVALID, "invalid grid %lld x %lld", (long long)rows,
+                                                 (long long)cols);
+    const int64_t m = rows * cols;
+    if (int s = check_common(x, n, d, w, m, algo)) return s;
+    if (!topo || !num || !den) return set_error(SOMGB_ERR_INVALID, "NULL argument");
+    if (n_vectors <= 0) return set_error(SOMGB_ERR_INVALID, "n_vectors must be > 0");
+    if (d > 64) return set_error(SOMGB_ERR_UNSUPPORTED, "the grid iteration pass supports D <= 64");
+    Workspace W;
+    bool tc = false;
+    if (int s = carve(ws, ws_bytes, SOMGB_OP_EPOCH, n, m, d, algo, &W, &tc)) return s;
+    if (n == 0) return SOMGB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    PassArgs a{};
+    a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.train_bmu = W.train_bmu; a.outs = OUT_TRAIN;
+    if (int s = run_pass(a, algo, W, tc, st)) return s;
+    return launch_iter_grid(x, rho, W.train_bmu, n, d, topo, rows, cols, sigma0, cur_vector, n_vectors, num, den, st);
 }
 
 int somgb_divide(const double* num, const double* den, int64_t m, int d, float* w_out, somgb_stream_t stream) {

@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(ACC_THREADS) accumulate_lanes_kernel(const flo
                                                                        const double* __restrict__ rho,
                                                                        const int32_t* __restrict__ bmu, int64_t n,
                                                                        int d, int64_t units_per_range, int64_t m,
-                                                                       int64_t chunk, int stripes, const float* __restrict__ bounds,
+                                                                       int64_t chunk, int stripes,
+                                                                       const float* __restrict__ bounds,
                                                                        double* __restrict__ S, double* __restrict__ c) {
     // [3][cnt * d] feature limbs, [cnt] counts or [3][cnt] weight limbs, then the warps' sample lists [32][128]
     extern __shared__ int32_t lane_bins[];
@@ -571,6 +572,147 @@ __global__ void __launch_bounds__(128) iter_kernel(const T* __restrict__ x, cons
     if (j < m && dacc != 0.0) atomicAdd(den + j, dacc);
 }
 
+// Iteration mode on the reference's square and hexagonal grids, in float32 with the grid factorisation. Unit
+// u = i * cols + j has x depending on (i, j mod 2) and y on j, so with b the sample's BMU
+//   h_u = rho exp(-|t_u - t_b|^2 / (2 sigma_i^2)) = rho Ex[i, j mod 2] Ey[j],
+// Ex = exp(-dx^2 / (2 sigma_i^2)) over the 2 * rows (row, parity) pairs and Ey over the cols columns, dx and dy the
+// float32 differences (the reference's typing of the topographic distance). Per staged batch of IG_SB samples a CTA
+// computes the tables (expf, within a few ulp of the float64 factor the reference casts to float32 for its atomics),
+// then each thread adds h * x for its units in float32 and folds the partial sums of every IG_FOLD batches into
+// compensated float32 accumulators in shared memory (no float64 arithmetic in the loop); at the end of its sample
+// chunk the CTA adds them to num, den (float64 atomics). Work: N * M * (D+1) float32 FMAs and N * (2 rows + cols)
+// exponentials per unit tile.
+constexpr int IG_SB = 32;
+constexpr int IG_FOLD = 2;   // batches summed in float32 before each compensated fold (64 samples)
+constexpr int IG_THREADS = 128;
+template <int DMAX, int UPT>
+__global__ void __launch_bounds__(IG_THREADS) iter_grid_kernel(const float* __restrict__ x,
+                                                               const double* __restrict__ rho,
+                                                               const int32_t* __restrict__ bmu, int64_t n, int d,
+                                                               const float* __restrict__ topo, int64_t rows,
+                                                               int64_t cols, double sigma0, int64_t cur_vector,
+                                                               int64_t n_vectors, int64_t chunk,
+                                                               double* __restrict__ num, double* __restrict__ den) {
+    extern __shared__ double ig_sm[];
+    const int64_t m = rows * cols;
+    const int ntab = (int)(2 * rows + cols);
+    constexpr int UPB = IG_THREADS * UPT;                 // units of this CTA's tile
+    float2* sacc = (float2*)ig_sm;                        // [UPB][d + 1] compensated float32 sums (sum, error)
+    float* xs = (float*)(sacc + (size_t)UPB * (d + 1));   // [IG_SB][d]
+    float* tab = xs + IG_SB * d;                          // [IG_SB][2 rows + cols]: Ex then rho * Ey
+    __shared__ float inv_s[IG_SB], rho_s[IG_SB], bx_s[IG_SB], by_s[IG_SB];   // per staged sample
+    __shared__ int valid_s[IG_SB];
+    const int64_t u0 = (int64_t)blockIdx.x * UPB;
+    for (int q = threadIdx.x; q < UPB * (d + 1); q += IG_THREADS) sacc[q] = make_float2(0.0f, 0.0f);
+    int tx_i[UPT], tx_j[UPT];
+    bool live[UPT];
+#pragma unroll
+    for (int t = 0; t < UPT; ++t) {
+        const int64_t u = u0 + t * IG_THREADS + threadIdx.x;
+        live[t] = u < m;
+        tx_i[t] = live[t] ? (int)(2 * (u / cols) + ((u % cols) & 1)) : 0;   // Ex column: (row, parity)
+        tx_j[t] = live[t] ? (int)(2 * rows + u % cols) : 0;                // Ey column
+    }
+    const int64_t s0 = (int64_t)blockIdx.y * chunk;
+    const int64_t s1 = min64(n, s0 + chunk);
+    float acc[UPT][DMAX];   // float32 sums of IG_FOLD batches, then folded into float64
+    float hacc[UPT];
+#pragma unroll
+    for (int t = 0; t < UPT; ++t) {
+        hacc[t] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < DMAX; ++k) acc[t][k] = 0.0f;
+    }
+    int batch = 0;
+    for (int64_t i0 = s0; i0 < s1; i0 += IG_SB, ++batch) {
+        const int nb = (int)min64(IG_SB, s1 - i0);
+        __syncthreads();   // the previous batch's tables and samples are no longer read
+        for (int q = threadIdx.x; q < nb * d; q += IG_THREADS) xs[q] = __ldg(x + i0 * d + q);
+        if (threadIdx.x < nb) {
+            const int64_t i = i0 + threadIdx.x;
+            const int32_t b = __ldg(bmu + i);
+            // sigma_i = sigma0 / (1 + 2 (cur + i) / n_vectors), clamped (som_batch.py:167-170); 1 / (2 sigma_i^2)
+            double sg = sigma0 * (1.0 / (1.0 + 2.0 * (double)(cur_vector + i) / (double)n_vectors));
+            if (sg < FLOAT_EPS) sg = FLOAT_EPS;
+            inv_s[threadIdx.x] = (float)(1.0 / (2.0 * sg * sg));
+            rho_s[threadIdx.x] = rho ? (float)__ldg(rho + i) : 1.0f;   // float32 training density
+            valid_s[threadIdx.x] = b >= 0;
+            bx_s[threadIdx.x] = b >= 0 ? topo[2 * (int64_t)b] : 0.0f;
+            by_s[threadIdx.x] = b >= 0 ? topo[2 * (int64_t)b + 1] : 0.0f;
+        }
+        __syncthreads();
+        for (int sidx = 0; sidx < nb; ++sidx) {
+            const bool ok = valid_s[sidx] != 0;
+            const float inv = inv_s[sidx], bx = bx_s[sidx], by = by_s[sidx], rr = rho_s[sidx];
+            float* t = tab + sidx * ntab;
+            for (int r = threadIdx.x; r < ntab; r += IG_THREADS) {
+                float v = 0.0f;
+                if (ok) {
+                    // exp(-dx^2 / (2 sigma^2)) in float32: within a few ulp of the float64 factor where it is above
+                    // 2^-24 of the BMU's own (|exponent| < 17), negligibly small beyond
+                    if (r < 2 * rows) {
+                        const int64_t ua = (r >> 1) * cols + ((r & 1) < cols ? (r & 1) : 0);
+                        const float dx = __fsub_rn(topo[2 * ua], bx);
+                        v = expf(-__fmul_rn(dx, dx) * inv);
+                    } else {
+                        const float dy = __fsub_rn(topo[2 * (r - 2 * rows) + 1], by);
+                        v = rr * expf(-__fmul_rn(dy, dy) * inv);
+                    }
+                }
+                t[r] = v;
+            }
+        }
+        __syncthreads();
+        for (int sidx = 0; sidx < nb; ++sidx) {
+            const float* tb = tab + sidx * ntab;
+            const float* xr = xs + sidx * d;
+            float xv[DMAX];
+#pragma unroll
+            for (int k = 0; k < DMAX; ++k) xv[k] = k < d ? xr[k] : 0.0f;
+#pragma unroll
+            for (int t = 0; t < UPT; ++t) {
+                const float h = tb[tx_i[t]] * tb[tx_j[t]];
+                hacc[t] += h;
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) acc[t][k] = fmaf(h, xv[k], acc[t][k]);
+            }
+        }
+        if ((batch + 1) % IG_FOLD == 0 || i0 + IG_SB >= s1) {
+            // compensated (Kahan) float32 accumulation: the running error stays at float32 rounding of the total
+            auto kahan = [](float2& a, float v) {
+                const float y = __fsub_rn(v, a.y);
+                const float t2 = __fadd_rn(a.x, y);
+                a.y = __fsub_rn(__fsub_rn(t2, a.x), y);
+                a.x = t2;
+            };
+#pragma unroll
+            for (int t = 0; t < UPT; ++t) {
+                float2* sa = sacc + (size_t)(t * IG_THREADS + threadIdx.x) * (d + 1);
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k)
+                    if (k < d) kahan(sa[k], acc[t][k]);
+                kahan(sa[d], hacc[t]);
+                hacc[t] = 0.0f;
+#pragma unroll
+                for (int k = 0; k < DMAX; ++k) acc[t][k] = 0.0f;
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < UPT; ++t) {
+        const int64_t u = u0 + t * IG_THREADS + threadIdx.x;
+        if (!live[t]) continue;
+        const float2* sa = sacc + (size_t)(t * IG_THREADS + threadIdx.x) * (d + 1);
+        for (int k = 0; k < d; ++k) {
+            const double v = (double)sa[k].x - (double)sa[k].y;
+            if (v != 0.0) atomicAdd(num + u * d + k, v);
+        }
+        const double v = (double)sa[d].x - (double)sa[d].y;
+        if (v != 0.0) atomicAdd(den + u, v);
+    }
+}
+
 template <typename T>
 __global__ void divide_kernel(const double* __restrict__ num, const double* __restrict__ den, int64_t m, int d,
                               T* __restrict__ w_out) {
@@ -849,6 +991,46 @@ int launch_iter(const T* x, const double* rho, const int32_t* bmu, int64_t n, in
                                                                         cur_vector, n_vectors, chunk, num, den);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
+}
+
+template <int DMAX, int UPT>
+int launch_iter_grid_d(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, const float* topo,
+                       int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors, double* num,
+                       double* den, cudaStream_t stream) {
+    constexpr int UPB = IG_THREADS * UPT;
+    const int64_t m = rows * cols;
+    const int64_t tiles = ceil_div(m, UPB);
+    int64_t chunks = std::max<int64_t>(1, (4 * num_sms()) / tiles);
+    int64_t chunk = std::max<int64_t>(4 * IG_SB, ceil_div(n, chunks));
+    chunk = ceil_div(chunk, IG_SB) * IG_SB;
+    chunks = ceil_div(n, chunk);
+    const size_t smem = (size_t)UPB * (d + 1) * 8 + (size_t)IG_SB * d * 4 + (size_t)IG_SB * (2 * rows + cols) * 4;
+    // (the float2 sums take the 8 bytes per unit and feature that float64 ones would)
+    if (smem > 200 * 1024) return set_error(SOMGB_ERR_UNSUPPORTED, "grid too large for the grid iteration pass");
+    auto kern = iter_grid_kernel<DMAX, UPT>;
+    SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<dim3((unsigned)tiles, (unsigned)chunks), IG_THREADS, smem, stream>>>(x, rho, bmu, n, d, topo, rows, cols,
+                                                                              sigma0, cur_vector, n_vectors, chunk,
+                                                                              num, den);
+    SOMGB_LAUNCH_CHECK();
+    return SOMGB_OK;
+}
+
+int launch_iter_grid(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, const float* topo,
+                     int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors, double* num,
+                     double* den, cudaStream_t stream) {
+    if (n == 0) return SOMGB_OK;
+    if (d <= 4) return launch_iter_grid_d<4, 4>(x, rho, bmu, n, d, topo, rows, cols, sigma0, cur_vector, n_vectors,
+                                                num, den, stream);
+    if (d <= 8) return launch_iter_grid_d<8, 4>(x, rho, bmu, n, d, topo, rows, cols, sigma0, cur_vector, n_vectors,
+                                                num, den, stream);
+    if (d <= 16) return launch_iter_grid_d<16, 4>(x, rho, bmu, n, d, topo, rows, cols, sigma0, cur_vector,
+                                                  n_vectors, num, den, stream);
+    if (d <= 32) return launch_iter_grid_d<32, 2>(x, rho, bmu, n, d, topo, rows, cols, sigma0, cur_vector,
+                                                  n_vectors, num, den, stream);
+    if (d <= 64) return launch_iter_grid_d<64, 1>(x, rho, bmu, n, d, topo, rows, cols, sigma0, cur_vector,
+                                                  n_vectors, num, den, stream);
+    return set_error(SOMGB_ERR_UNSUPPORTED, "the grid iteration pass supports D <= 64");
 }
 
 template <typename T>

@@ -301,14 +301,21 @@ class SOM_Batch(SOM_Abstract):
         den = torch.zeros(M, dtype=torch.float64, device=device)
         sigma0 = float(self._dtype(self._sigma))
         cur = 0
-        name = 'somgb_train_iter_pass_f64' if self._is_f64 else 'somgb_train_iter_pass'
+        grid = not self._is_f64 and D <= 64   # float32 maps: the grid-factorised float32 pass, BMUs by bmu_algo
         for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device):
             count = min(_device.rows(xc), n_vectors - cur)
             xk = xc[:count]
             rk = None if rc is None else rc[:count]
-            wsp, wsb = self._ws.for_op(_native.OP_EPOCH, count, M, D, _native.ALGO_FP32, device)
-            _native.call(name, xk.data_ptr(), _device.ptr(rk), count, D, w.data_ptr(), topo.data_ptr(), M, sigma0,
-                         cur, n_vectors, num.data_ptr(), den.data_ptr(), wsp, wsb, _device.stream())
+            if grid:
+                wsp, wsb = self._ws.for_op(_native.OP_EPOCH, count, M, D, self._algo, device)
+                _native.call('somgb_train_iter_pass_grid', xk.data_ptr(), _device.ptr(rk), count, D, w.data_ptr(),
+                             topo.data_ptr(), self._m, self._n, sigma0, cur, n_vectors, self._algo, num.data_ptr(),
+                             den.data_ptr(), wsp, wsb, _device.stream())
+            else:
+                name = 'somgb_train_iter_pass_f64' if self._is_f64 else 'somgb_train_iter_pass'
+                wsp, wsb = self._ws.for_op(_native.OP_EPOCH, count, M, D, _native.ALGO_FP32, device)
+                _native.call(name, xk.data_ptr(), _device.ptr(rk), count, D, w.data_ptr(), topo.data_ptr(), M,
+                             sigma0, cur, n_vectors, num.data_ptr(), den.data_ptr(), wsp, wsb, _device.stream())
             cur += count
             if cur >= n_vectors:
                 break

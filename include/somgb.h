@@ -233,6 +233,15 @@ int somgb_neighbourhood_update_grid_f64(const double* S, const double* c, const 
 int somgb_train_iter_pass(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
                           int64_t m, double sigma0, int64_t cur_vector, int64_t n_vectors, double* num, double* den,
                           void* ws, size_t ws_bytes, somgb_stream_t stream);
+/*
+ * The same on the reference's square and hexagonal grids (unit i * cols + j of a rows x cols map, topography as the
+ * reference builds it), with the neighbourhood factor split by grid axis and the sums in float32 per batch of 32
+ * samples folded into float64; BMUs by `algo` (workspace: somgb_workspace_bytes(SOMGB_OP_EPOCH, n, m, d, algo)).
+ * D <= 64.
+ */
+int somgb_train_iter_pass_grid(const float* x, const double* rho, int64_t n, int d, const float* w, const float* topo,
+                               int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors,
+                               int algo, double* num, double* den, void* ws, size_t ws_bytes, somgb_stream_t stream);
 int somgb_train_iter_pass_f64(const double* x, const double* rho, int64_t n, int d, const double* w,
                               const double* topo, int64_t m, double sigma0, int64_t cur_vector, int64_t n_vectors,
                               double* num, double* den, void* ws, size_t ws_bytes, somgb_stream_t stream);

@@ -125,3 +125,37 @@ def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
     assert np.array_equal(som.get_winners(x), want)
     st = ctypes.c_uint(0)
     native.call('somgb_device_status', ctypes.addressof(st), 1, torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.parametrize('m,n,d,topology,algo', [(32, 32, 16, 'hexagonal', 'tc'), (20, 17, 5, 'square', 'fp32'),
+                                                  (64, 64, 32, 'square', 'auto'), (1, 9, 3, 'hexagonal', 'fp32')])
+def test_grid_iteration_pass_matches_the_float64_pass(cuda, native, oracle, m, n, d, topology, algo):
+    """Iteration mode: the grid-factorised float32 pass (somgb_train_iter_pass_grid) against the float64 pass over an
+    arbitrary topography (somgb_train_iter_pass) on the same rows: the same numerators and denominators to 2e-6."""
+    rng = np.random.default_rng(m * n + d)
+    M, N = m * n, 60_000
+    x = synthetic.correlated_lognormal(N, d, 9) if d >= 4 else rng.standard_normal((N, d)).astype(np.float32)
+    w = x[rng.integers(0, N, M)].copy()
+    rho = rng.random(N)
+    rho[rng.random(N) < 0.05] = 0.0
+    topo = oracle.topography(m, n, topology)
+    xd, wd, td = (torch.from_numpy(np.ascontiguousarray(a)).to(cuda) for a in (x, w, topo))
+    rd = torch.from_numpy(rho).to(cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    out = []
+    for grid in (True, False):
+        num = torch.zeros((M, d), dtype=torch.float64, device=cuda)
+        den = torch.zeros(M, dtype=torch.float64, device=cuda)
+        A = native.ALGOS[algo] if grid else native.ALGO_FP32
+        buf, wsp, nbytes = _ws(native, native.OP_EPOCH, N, M, d, A, cuda)
+        if grid:
+            native.call('somgb_train_iter_pass_grid', xd.data_ptr(), rd.data_ptr(), N, d, wd.data_ptr(), td.data_ptr(),
+                        m, n, 6.0, 1000, 2 * N, A, num.data_ptr(), den.data_ptr(), wsp, nbytes, s)
+        else:
+            native.call('somgb_train_iter_pass', xd.data_ptr(), rd.data_ptr(), N, d, wd.data_ptr(), td.data_ptr(), M,
+                        6.0, 1000, 2 * N, num.data_ptr(), den.data_ptr(), wsp, nbytes, s)
+        torch.cuda.synchronize()
+        out.append((num.cpu().numpy(), den.cpu().numpy()))
+    (n_g, d_g), (n_r, d_r) = out
+    np.testing.assert_allclose(d_g, d_r, rtol=2e-6, atol=1e-9 * d_r.max())
+    np.testing.assert_allclose(n_g, n_r, rtol=2e-6, atol=2e-6 * np.abs(n_r).max())
