@@ -669,13 +669,14 @@ def gpu_arm(args, ws, rank, local):
 
     del runner, xd
     torch.cuda.empty_cache()
+    # --- BMU serving (rank 0, one GPU), before the large D = 32 catalogue comes and goes ----------------------------------
+    if not args.skip_serve and rank == 0 and ws == 1:
+        out['serve'] = serve_record(args)
+        torch.cuda.empty_cache()
+
     # --- the 64x64, D = 32 configuration (rank 0, one GPU) ---------------------------------------------------------------
     if not args.skip_sq64 and rank == 0 and ws == 1 and args.n is None:
         out['sq64'] = sq64_record(torch, _native, device, args)
-
-    # --- BMU serving (rank 0, one GPU) ----------------------------------------------------------------------------------
-    if not args.skip_serve and rank == 0 and ws == 1:
-        out['serve'] = serve_record(args)
 
     # --- CPU baseline (rank 0, N=1) -------------------------------------------------------------------------------------
     if not args.skip_cpu and rank == 0 and ws == 1:
