@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, 'csrc')
 LIB = os.path.join(HERE, 'libsomgb.so')
 OBJ_DIR = os.path.join(HERE, '_build')
 
-SOURCES = ['api.cu', 'k0_fp32.cu', 'k1_tc.cu', 'k_update.cu', 'k_moments.cu', 'k_sort.cu', 'noalloc.cu']
+SOURCES = ['api.cu', 'k0_fp32.cu', 'k1_tc.cu', 'k_update.cu', 'k_moments.cu', 'k_sort.cu', 'k4_iter_tc.cu', 'noalloc.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-Wall',
               '--expt-relaxed-constexpr']

@@ -436,6 +436,15 @@ int somgb_train_iter_pass_grid(const float* x, const double* rho, int64_t n, int
     PassArgs a{};
     a.x = x; a.rho = rho; a.n = n; a.d = d; a.w = w; a.m = m; a.train_bmu = W.train_bmu; a.outs = OUT_TRAIN;
     if (int s = run_pass(a, algo, W, tc, st)) return s;
+    // the tensor-core contraction (K4) for the tensor-core algorithms; AUTO keeps small passes on the CUDA cores
+    const bool k4 = algo != SOMGB_ALGO_FP32 && iter_tc_shape_ok(rows, cols, d) && device_has_tc() &&
+                    (algo == SOMGB_ALGO_TC || n * m >= ((int64_t)1 << 22));
+    if (k4) {
+        SOMGB_CUDA_TRY(cudaMemsetAsync(W.bounds, 0, (size_t)(d + 1) * 4, st));
+        if (int s = launch_feature_bounds(x, rho, n, d, W.bounds, st)) return s;
+        return launch_iter_tc(x, rho, W.train_bmu, n, d, topo, rows, cols, sigma0, cur_vector, n_vectors, W.bounds,
+                              num, den, (unsigned int*)(W.counter + 1), st);
+    }
     return launch_iter_grid(x, rho, W.train_bmu, n, d, topo, rows, cols, sigma0, cur_vector, n_vectors, num, den, st);
 }
 

@@ -1293,6 +1293,14 @@ thread_local uint32_t t_wait_limit = 0;
 
 }  // namespace
 
+unsigned int* device_status_word() {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_tc_status) != cudaSuccess) return nullptr;
+    return (unsigned int*)p;
+}
+
+bool device_has_tc() { return device_is_sm103(); }
+
 bool tc_shape_ok(int64_t m, int d) {
     if (d != 4 && d != 8 && d != 16 && d != 32) return false;
     if (m <= 0 || m > (int64_t)MAX_U * TN) return false;   // a list entry names its chunk in a byte

@@ -18,4 +18,19 @@ int read_device_status(unsigned int* status, bool clear, cudaStream_t stream);
 // protocol waits by `wait_limit` polls, so that a wait runs out and the pass returns with its status set.
 void tc_debug_withhold(int64_t row_tile, uint32_t wait_limit);
 
+// The sticky device status word above, as a device pointer (NULL if it cannot be resolved).
+unsigned int* device_status_word();
+// True on an sm_103 device (the tensor-core kernels' target).
+bool device_has_tc();
+
+// K4: the iteration-mode contraction on the tensor cores (k4_iter_tc.cu). Shape limits (host-only check): D <= 31 and
+// at most 640 exponential-table rows per 512-unit tile of the grid.
+bool iter_tc_shape_ok(int64_t rows, int64_t cols, int d);
+int64_t iter_tc_table_rows(int64_t rows, int64_t cols);
+// num[u, :] += sum_i h_iu rho_i x_i, den[u] += sum_i h_iu rho_i over the samples with bmu[i] >= 0 (iteration-mode
+// neighbourhood of sample cur_vector + i), `bounds` from launch_feature_bounds over the same samples.
+int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, const float* topo,
+                   int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors,
+                   const float* bounds, double* num, double* den, unsigned int* status, cudaStream_t stream);
+
 }  // namespace somgb

@@ -127,13 +127,23 @@ def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
     native.call('somgb_device_status', ctypes.addressof(st), 1, torch.cuda.current_stream().cuda_stream)
 
 
-@pytest.mark.parametrize('m,n,d,topology,algo', [(32, 32, 16, 'hexagonal', 'tc'), (20, 17, 5, 'square', 'fp32'),
-                                                  (64, 64, 32, 'square', 'auto'), (1, 9, 3, 'hexagonal', 'fp32')])
-def test_grid_iteration_pass_matches_the_float64_pass(cuda, native, oracle, m, n, d, topology, algo):
-    """Iteration mode: the grid-factorised float32 pass (somgb_train_iter_pass_grid) against the float64 pass over an
-    arbitrary topography (somgb_train_iter_pass) on the same rows: the same numerators and denominators to 2e-6."""
+@pytest.mark.parametrize('m,n,d,topology,algo,N', [
+    # the tensor-core contraction (K4): the 64x64 D = 16 map, one partial 512-unit tile, a single grid row, tiles that
+    # end inside a grid row, tiles inside and across rows longer than 512 units, the largest D, a batch or two
+    # (AUTO where D has no tensor-core BMU search: BMUs on the CUDA cores, the contraction on the tensor cores)
+    (64, 64, 16, 'square', 'tc', 15_000), (32, 32, 16, 'hexagonal', 'tc', 60_000),
+    (20, 17, 5, 'square', 'auto', 60_000), (1, 600, 3, 'hexagonal', 'auto', 20_000),
+    (80, 80, 8, 'hexagonal', 'tc', 8_000), (3, 700, 4, 'square', 'tc', 10_000), (64, 64, 31, 'square', 'auto', 10_000),
+    (32, 32, 16, 'square', 'tc', 37), (32, 32, 4, 'square', 'tc', 64),
+    # the float32 CUDA-core pass: the FP32 algorithm, and D = 32 (above the tensor-core contraction's limit)
+    (32, 32, 16, 'hexagonal', 'fp32', 60_000), (20, 17, 5, 'square', 'fp32', 60_000),
+    (64, 64, 32, 'square', 'auto', 15_000), (1, 9, 3, 'hexagonal', 'fp32', 60_000)])
+def test_grid_iteration_pass_matches_the_float64_pass(cuda, native, oracle, m, n, d, topology, algo, N):
+    """Iteration mode: the grid-factorised pass (somgb_train_iter_pass_grid; the tensor-core contraction for the TC
+    algorithm, the float32 CUDA-core pass otherwise) against the float64 pass over an arbitrary topography
+    (somgb_train_iter_pass) on the same rows: the same numerators and denominators to 2e-6."""
     rng = np.random.default_rng(m * n + d)
-    M, N = m * n, 60_000
+    M = m * n
     x = synthetic.correlated_lognormal(N, d, 9) if d >= 4 else rng.standard_normal((N, d)).astype(np.float32)
     w = x[rng.integers(0, N, M)].copy()
     rho = rng.random(N)
@@ -159,3 +169,6 @@ def test_grid_iteration_pass_matches_the_float64_pass(cuda, native, oracle, m, n
     (n_g, d_g), (n_r, d_r) = out
     np.testing.assert_allclose(d_g, d_r, rtol=2e-6, atol=1e-9 * d_r.max())
     np.testing.assert_allclose(n_g, n_r, rtol=2e-6, atol=2e-6 * np.abs(n_r).max())
+    st = ctypes.c_uint(0)
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    assert st.value == 0, 'no bounded wait ran out'
