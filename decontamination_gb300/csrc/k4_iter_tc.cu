@@ -24,8 +24,10 @@
 // TMEM (512 columns): NB = 16 (D <= 15) two accumulator sets of 4 x 32 columns, NB = 32 one set of 4 x 64, at
 // [0, 256); A operands at [256, 512): (buffer, split, M tile, K-step) at 256 + 8 (((buffer * 2 + split) * 4 + tile) *
 // 2 + K-step). An MMA of N <= 64 columns takes as long as one of 64, so the hi and lo parts of B share one MMA.
-// Error budget: 2^-21 relative per product from the FP16 parts, the FP32 accumulation of 4 * group MMAs, then float32
-// rounding of the compensated sums; it agrees with the float64 pass to a few 1e-7.
+// Error budget: 2^-21 relative per product from the FP16 parts, then the tensor core's FP32 accumulation, which loses
+// low bits with every MMA (measured: ~20 float32 ulps over 16 MMAs, ~8 over the 8 MMAs of a 2-batch group, ~3 over 4),
+// then float32 rounding of the compensated sums. With `group` = 2 the sums differ from the float32 CUDA-core pass by
+// at most 5.1e-7 relative (12.6 M samples on a 64 x 64 map), for 8% of the time a 1-batch group would take.
 // Every wait is bounded: one that gives up sets bit 65536 of the status words and the CTA returns.
 #include <cuda_fp16.h>
 
@@ -80,6 +82,23 @@ __device__ __forceinline__ uint32_t k4_off(int row, int k) {
 __device__ __forceinline__ uint32_t h2_bits(__half2 v) { return *reinterpret_cast<uint32_t*>(&v); }
 __device__ __forceinline__ float trunc11(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
 
+// c (Q + t)^2 in float32 arithmetic from Q = c[0] + c[1] (integers) and c = c[2] + c[3], for integer t < 2^24: q = Q + t
+// exactly as qh + ql (Knuth's two-sum; ql a small integer), qh^2 exactly as p + pe (FMA product error), then
+// (p + pe + 2 qh ql) (c[2] + c[3]) with the product p c[2] split the same way: about 2^-44 relative before the one
+// rounding, so the result is the correctly rounded float32 except in rare near-ties.
+__device__ __forceinline__ float inv_sigma_of(const float* c, float t) {
+    const float qh = __fadd_rn(c[0], t);
+    const float bv = __fsub_rn(qh, c[0]);
+    const float e = __fadd_rn(__fsub_rn(c[0], __fsub_rn(qh, bv)), __fsub_rn(t, bv));
+    const float ql = __fadd_rn(e, c[1]);
+    const float p = __fmul_rn(qh, qh);
+    const float pe = __fmaf_rn(qh, qh, -p);
+    const float r = __fadd_rn(pe, __fmul_rn(__fmul_rn(2.0f, qh), ql));
+    const float v = __fmul_rn(p, c[2]);
+    const float ve = __fmaf_rn(p, c[2], -v);
+    return __fadd_rn(v, __fadd_rn(ve, __fmaf_rn(p, c[3], __fmul_rn(r, c[2]))));
+}
+
 template <int DMAX, int NB>
 __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) {
     constexpr int N = 2 * NB;                       // MMA N: hi rows then lo rows of B
@@ -92,7 +111,7 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     float* tab = (float*)(k4_raw + 2 * K4_B_MAX);      // [table row][K4_TPAD]; row ntab is all zeros
     __shared__ float inv_s[K4_SB], rho_s[K4_SB], bx_s[K4_SB], by_s[K4_SB], scale_s[K4_NB_MAX];
     __shared__ int valid_s[K4_SB];
-    __shared__ float poly_s[4];
+    __shared__ float poly_s[5];
     __shared__ int perm_s[K4_UNITS];
     __shared__ __align__(8) uint64_t bars[5];
     __shared__ uint32_t tmem_s;
@@ -130,12 +149,14 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
         ptx::fence_mbar_init();
         abort_s = 0;
         // 1 / (2 sigma_i^2) = inv_coef (Q + t)^2 for sample i = s0 + t / 2 of this chunk, Q = n_vectors + 2 (cur + s0):
-        // the float64 coefficients once per CTA, the polynomial in float32 per sample (relative error ~1e-7)
+        // Q and inv_coef as float32 pairs (hi, lo) once per CTA, so that the per-sample value in float32 arithmetic
+        // is the correctly rounded one (inv_sigma_of)
         const double Q = (double)P.n_vectors + 2.0 * (double)(P.cur_vector + s0);
-        poly_s[0] = (float)(P.inv_coef * Q * Q);
-        poly_s[1] = (float)(2.0 * P.inv_coef * Q);
+        poly_s[0] = (float)Q;
+        poly_s[1] = (float)(Q - (double)poly_s[0]);
         poly_s[2] = (float)P.inv_coef;
-        poly_s[3] = (float)(P.clamp_q - Q);   // sigma_i < FLOAT_EPS beyond this t
+        poly_s[3] = (float)(P.inv_coef - (double)poly_s[2]);
+        poly_s[4] = (float)(P.clamp_q - Q);   // sigma_i < FLOAT_EPS beyond this t
     }
     if (tid < K4_NB_MAX) {   // B row scales 2^(14 - e), the feature's bound below 2^e: |B| < 2^14
         int e = 0;
@@ -265,8 +286,8 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
             rho_r = (lane < nb && P.rho) ? __ldg(P.rho + i) : 1.0;
             // sigma_i = sigma0 / (1 + 2 (cur + i) / n_vectors) clamped at FLOAT_EPS (som_batch.py:167-170), so
             // 1 / (2 sigma_i^2) = q^2 / (2 sigma0^2 n_vectors^2) with q = n_vectors + 2 (cur + i) = Q + t
-            const float t = (float)(2 * (i - s0));
-            inv_r = t > poly_s[3] ? P.inv_clamp_f : fmaf(fmaf(poly_s[2], t, poly_s[1]), t, poly_s[0]);
+            const float t = (float)(2 * (i - s0));   // exact below 2^24
+            inv_r = t > poly_s[4] ? P.inv_clamp_f : inv_sigma_of(poly_s, t);
         }
     };
     auto prefetch_bmu = [&]() {
@@ -446,7 +467,7 @@ int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_
     P.clamp_q = sigma0 * nv / FLOAT_EPS;
     P.cur_vector = cur_vector; P.n_vectors = n_vectors; P.chunk = chunk; P.bounds = bounds;
     P.num = num; P.den = den; P.status = status; P.gstatus = device_status_word();
-    P.group = 4;
+    P.group = 2;
     P.wait_limit = 1u << 22;
     if (!P.gstatus) return set_error(SOMGB_ERR_CUDA, "device status word unavailable");
     const int64_t ntab = iter_tc_table_rows(rows, cols);
