@@ -78,6 +78,7 @@ def parse():
     ap.add_argument('--skip-parity', action='store_true')
     ap.add_argument('--skip-sq64', action='store_true', help='no 64x64, D = 32, 50.3 M-row sub-record')
     ap.add_argument('--skip-serve', action='store_true', help='no serving sub-record')
+    ap.add_argument('--skip-iter', action='store_true', help='no iteration-mode sub-record')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--clock-seconds', type=float, default=2.0,
                     help='the epochs also run this long after the timed ones while the clocks are sampled')
@@ -497,6 +498,68 @@ def fp32_roofline(N, M, D, ms, clocks):
             'peak_source': f'nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 flops x {mhz:.0f} MHz'}
 
 
+def iteration_record(torch, native, xd, wmap, topo, w, device):
+    """Iteration mode (SOM_Batch.train(n_vectors=N)'s pass, algo/som_batch.py:154-210, 378-495) on the resident
+    catalogue and the trained map: one somgb_train_iter_pass_grid over every row on the tensor cores (BMU pass and the
+    contraction) and on the CUDA cores (float32 BMU search and contraction), CUDA-event timed, with the BMU pass alone
+    timed to give the contraction's share, and the largest relative difference of the two forms' sums."""
+    N, D = xd.shape
+    m, n = w['m'], w['n']
+    M = m * n
+    s = torch.cuda.current_stream(device).cuda_stream
+    out = {'call': f'somgb_train_iter_pass_grid(all {N} rows, cur_vector 0, n_vectors {N}, sigma0 {w["sigma0"]})',
+           'unit': UNIT}
+    sums = {}
+    for algo in ('tc', 'fp32'):
+        A = native.ALGOS[algo]
+        nbytes = native.workspace_bytes(native.OP_EPOCH, N, M, D, A)
+        buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+        wsp = buf.data_ptr() + (-buf.data_ptr()) % 256
+        num = torch.zeros((M, D), dtype=torch.float64, device=device)
+        den = torch.zeros(M, dtype=torch.float64, device=device)
+        bmu = torch.empty(N, dtype=torch.int32, device=device)
+
+        def whole():
+            num.zero_()
+            den.zero_()
+            native.call('somgb_train_iter_pass_grid', xd.data_ptr(), None, N, D, wmap.data_ptr(), topo.data_ptr(), m,
+                        n, float(w['sigma0']), 0, N, A, num.data_ptr(), den.data_ptr(), wsp, nbytes, s)
+
+        def bmus():
+            native.call('somgb_train_bmu_pass', xd.data_ptr(), None, N, D, wmap.data_ptr(), topo.data_ptr(), M, 1.0,
+                        A, bmu.data_ptr(), None, wsp, nbytes, s)
+
+        ms = {}
+        for label, fn in (('pass', whole), ('bmu', bmus)):
+            for _ in range(2):
+                fn()
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms[label] = statistics.mean(ts)
+        whole()
+        torch.cuda.synchronize()
+        sums[algo] = (num.clone(), den.clone())
+        key = 'tensor_cores' if algo == 'tc' else 'cuda_cores'
+        out[key] = {'ms_per_pass': ms['pass'], 'bmu_pass_ms': ms['bmu'], 'contraction_ms': ms['pass'] - ms['bmu'],
+                    'value': N * M / (ms['pass'] * 1e-3) / 1e9,
+                    'contraction': 'tcgen05 split-FP16 (k4_iter_kernel)' if algo == 'tc' else
+                                   'float32 CUDA cores (iter_grid_kernel)'}
+        del buf, num, den, bmu
+    (nt, dt), (nf, df) = sums['tc'], sums['fp32']
+    out['value'] = out['tensor_cores']['value']
+    out['contraction_speedup'] = out['cuda_cores']['contraction_ms'] / out['tensor_cores']['contraction_ms']
+    out['max_rel_diff_den'] = float(((dt - df).abs() / df.abs().clamp_min(1e-9 * float(df.abs().max()))).max())
+    out['max_rel_diff_num'] = float(((nt - nf).abs() / (nf.abs() + 1e-6 * float(nf.abs().max()))).max())
+    return out
+
+
 def sq64_record(torch, native, device, args):
     """The 64x64, D = 32 configuration over 50.3 M rows, catalogue generated on the device: tensor-core epochs, the
     plain FP32 form's epochs, the recheck rate and BMU mismatches between the two forms on the final map."""
@@ -666,6 +729,11 @@ def gpu_arm(args, ws, rank, local):
                       'call': 'SOM_Batch.train(pinned host tensor, n_epochs=1): upload, training pass, error pass, '
                               'weights/history/errors back to the host'}
         del som
+
+    # --- iteration mode on the resident catalogue and the trained map (rank 0, one GPU) --------------------------------------
+    if not args.skip_iter and rank == 0 and ws == 1 and w['topology'] in ('square', 'hexagonal'):
+        out['iteration'] = iteration_record(torch, _native, xd, runner.wcur, topo.float(), w, device)
+        torch.cuda.empty_cache()
 
     del runner, xd
     torch.cuda.empty_cache()
