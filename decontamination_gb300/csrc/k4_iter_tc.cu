@@ -10,7 +10,8 @@
 //   * thread t holds TMEM lane t mod 128 of M tile t / 128 and the unit of slot t in the CTA's order (even grid columns
 //     first, then odd, rows ascending within a column), so that a warp's 32 units share few table rows;
 //   * per batch the 12 warps that issue no MMAs compute the per-sample exponential tables over the grid rows (by
-//     column parity) and grid columns of the CTA's units (float32 expf, as the float32 CUDA-core pass computes them);
+//     column parity) and grid columns of the CTA's units (float32 arguments as the float32 CUDA-core pass forms them,
+//     the exponential from the hardware base-2 approximation with an extended-precision argument, k4_exp);
 //   * each thread writes its unit's factors A[u, s] = 2^15 h[s, u], split into FP16 hi (h truncated to 11 significant
 //     bits) + lo (the exact rest, rounded) parts, into its TMEM lane (tcgen05.st), and the CTA writes the B operand to
 //     shared memory: rows [0, NB) the FP16 hi parts and rows [NB, 2 NB) the lo parts of B[n, s] = rho_s x_s[n]
@@ -47,7 +48,7 @@ constexpr int K4_THREADS = K4_UNITS;           // one thread per unit
 constexpr int K4_SB = 32;                      // samples per batch: two K-steps of 16
 constexpr int K4_NB_MAX = 32;                  // B rows per FP16 part: the D features, the density, zero rows
 constexpr int K4_TPAD = 36;                    // floats per table row: 32 samples + 4 (conflict-free 16-byte reads)
-constexpr int K4_TAB_MAX = 640;                // table rows (2 per grid row + 1 per grid column) of a CTA
+constexpr int K4_TAB_MAX = 320;                // table rows (2 per grid row + 1 per grid column) of a CTA
 constexpr uint32_t K4_B_MAX = 2 * K4_NB_MAX * K4_SB * 2;   // bytes of one batch's B operand
 constexpr uint32_t K4_SBO = (K4_SB / 8) * 128;      // bytes between the 8-row groups of the canonical layout
 constexpr uint32_t K4_ACC_COLS = 256;               // accumulator columns; the A operands follow
@@ -82,6 +83,48 @@ __device__ __forceinline__ uint32_t k4_off(int row, int k) {
 __device__ __forceinline__ uint32_t h2_bits(__half2 v) { return *reinterpret_cast<uint32_t*>(&v); }
 __device__ __forceinline__ float trunc11(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
 
+// Two-lane float32 arithmetic (sm_100 and later): each lane rounds to nearest as __fmul_rn / __fadd_rn / __fsub_rn.
+__device__ __forceinline__ unsigned long long f2_bits(float2 v) {
+    unsigned long long u;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(u) : "f"(v.x), "f"(v.y));
+    return u;
+}
+__device__ __forceinline__ float2 f2_of(unsigned long long u) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(u));
+    return v;
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return f2_of(r);
+}
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return f2_of(r);
+}
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return f2_of(r);
+}
+__device__ __forceinline__ uint32_t h2_of(float2 v) { return h2_bits(__floats2half2_rn(v.x, v.y)); }
+
+// e^x from the hardware base-2 exponential (ex2.approx): y = x log2(e) is carried as y_hi + y_lo with log2(e) split
+// into float32 hi and lo parts and the FMA product error, and e^x = 2^y_hi (1 + y_lo ln 2), first order in
+// |y_lo| < 2^-23 |y|; the result is within the ex2 approximation's error of e^x (results below 2^-126 flush to zero).
+constexpr float K4_LOG2E_HI = 1.44269502162933349609375f;   // log2(e) rounded to float32
+constexpr float K4_LOG2E_LO = 1.925963033500011e-08f;       // log2(e) - K4_LOG2E_HI
+constexpr float K4_LN2 = 0.693147180559945309f;
+__device__ __forceinline__ float k4_exp(float x) {
+    const float yh = __fmul_rn(x, K4_LOG2E_HI);
+    const float yl = __fmaf_rn(x, K4_LOG2E_LO, __fmaf_rn(x, K4_LOG2E_HI, -yh));
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(yh));
+    return __fmaf_rn(e, __fmul_rn(yl, K4_LN2), e);
+}
+
 // c (Q + t)^2 in float32 arithmetic from Q = c[0] + c[1] (integers) and c = c[2] + c[3], for integer t < 2^24: q = Q + t
 // exactly as qh + ql (Knuth's two-sum; ql a small integer), qh^2 exactly as p + pe (FMA product error), then
 // (p + pe + 2 qh ql) (c[2] + c[3]) with the product p c[2] split the same way: about 2^-44 relative before the one
@@ -108,9 +151,10 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     static_assert(NSET * K4_MT * N <= (int)K4_ACC_COLS && DMAX < NB, "accumulators fit below the A operands");
     extern __shared__ __align__(128) uint8_t k4_raw[];
     uint8_t* sB = k4_raw;                              // [buffer] B operands
-    float* tab = (float*)(k4_raw + 2 * K4_B_MAX);      // [table row][K4_TPAD]; row ntab is all zeros
-    __shared__ float inv_s[K4_SB], rho_s[K4_SB], bx_s[K4_SB], by_s[K4_SB], scale_s[K4_NB_MAX];
-    __shared__ int valid_s[K4_SB];
+    float* tab0 = (float*)(k4_raw + 2 * K4_B_MAX);     // [batch parity][table row][K4_TPAD]; row ntab is all zeros
+    __shared__ float inv_s[K4_SB], bx_s[K4_SB], by_s[K4_SB], scale_s[K4_NB_MAX];
+    __shared__ float rho_s[2][K4_SB];                  // [batch parity]
+    __shared__ int valid_s[2][K4_SB];
     __shared__ float poly_s[5];
     __shared__ int perm_s[K4_UNITS];
     __shared__ __align__(8) uint64_t bars[5];
@@ -131,8 +175,9 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     const int64_t c0 = nrow > 1 ? 0 : u0 % cols;
     const int ncol = nrow > 1 ? (int)cols : (int)(ulast % cols - c0 + 1);
     const int ntab = 2 * nrow + ncol;
-    float* xs = tab + (ntab + 1) * K4_TPAD;           // [K4_SB][d]
-    float* gc = xs + K4_SB * d;                       // [ntab] the table rows' grid coordinates
+    const int tabn = (ntab + 1) * K4_TPAD;            // floats per table buffer
+    float* xs0 = tab0 + 2 * tabn;                     // [batch parity][K4_SB][d]
+    float* gc = xs0 + 2 * K4_SB * d;                  // [ntab] the table rows' grid coordinates
     const int64_t s0 = (int64_t)blockIdx.y * P.chunk;
     const int64_t s1 = min64(P.n, s0 + P.chunk);
     const int nbatch = s1 > s0 ? (int)((s1 - s0 + K4_SB - 1) / K4_SB) : 0;
@@ -165,7 +210,7 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
         e = max(e, -60);
         scale_s[tid] = tid <= d ? ldexpf(1.0f, 14 - e) : 0.0f;
     }
-    for (int q = tid; q < K4_TPAD; q += K4_THREADS) tab[ntab * K4_TPAD + q] = 0.0f;
+    for (int q = tid; q < 2 * K4_TPAD; q += K4_THREADS) tab0[(q / K4_TPAD) * tabn + ntab * K4_TPAD + q % K4_TPAD] = 0.0f;
     // table row e < 2 nrow: x of grid row r0 + e mod nrow at column parity e / nrow; else y of grid column c0 + e - 2 nrow
     for (int e = tid; e < ntab; e += K4_THREADS) {
         const int p = e / nrow;
@@ -215,11 +260,12 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     const int ix = live ? (ucol & 1) * nrow + (urow - (int)r0) : ntab;   // Ex row: (column parity, grid row)
     const int iy = live ? 2 * nrow + (ucol - (int)c0) : ntab;           // Ey row: grid column
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-    const float* tx = tab + ix * K4_TPAD;
-    const float* ty = tab + iy * K4_TPAD;
-    float2 acc[DMAX + 1];   // compensated float32 sums (sum, error) of the scaled accumulator columns
+    const int tx = ix * K4_TPAD, ty = iy * K4_TPAD;   // offsets in a table buffer
+    // compensated float32 sums of the scaled accumulator columns, features k and k + 1 in the lanes of one pair
+    constexpr int NP = DMAX / 2 + 1;
+    float2 asum[NP], aerr[NP];
 #pragma unroll
-    for (int k = 0; k <= DMAX; ++k) acc[k] = make_float2(0.0f, 0.0f);
+    for (int k = 0; k < NP; ++k) asum[k] = aerr[k] = make_float2(0.0f, 0.0f);
 
     // M tile mt's MMAs of K-step ks of batch b: A_lo.B, then A_hi.B
     auto issue = [&](int b, int ks) {
@@ -251,22 +297,24 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
             ptx::tmem_wait_ld8(rh);
             ptx::tmem_tie8(rl);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int k = 8 * c + j;
-                if (k > DMAX) break;
-                const float v = __fadd_rn(__uint_as_float(rh[j]), __uint_as_float(rl[j]));
-                const float y = __fsub_rn(v, acc[k].y);
-                const float t = __fadd_rn(acc[k].x, y);
-                acc[k].y = __fsub_rn(__fsub_rn(t, acc[k].x), y);
-                acc[k].x = t;
+            for (int j = 0; j < 8; j += 2) {
+                const int k2 = (8 * c + j) / 2;
+                if (k2 >= NP) break;
+                // the hi and lo halves, then Kahan's compensated addition, two features at a time
+                const float2 v = add2_rn(make_float2(__uint_as_float(rh[j]), __uint_as_float(rh[j + 1])),
+                                         make_float2(__uint_as_float(rl[j]), __uint_as_float(rl[j + 1])));
+                const float2 y = sub2_rn(v, aerr[k2]);
+                const float2 t = add2_rn(asum[k2], y);
+                aerr[k2] = sub2_rn(sub2_rn(t, asum[k2]), y);
+                asum[k2] = t;
             }
         }
         ptx::tc_fence_before();
         return true;
     };
 
-    // the next batch's samples, loaded a batch ahead: XPT features per thread; warp 1 lane s: sample s's BMU, weight
-    // and 1 / (2 sigma^2), then the BMU's grid coordinates
+    // the samples two batches ahead are loaded while this batch runs: XPT features per thread; warp 1 lane s:
+    // sample s's BMU, weight and 1 / (2 sigma^2), then the BMU's grid coordinates
     constexpr int XPT = (K4_SB * DMAX + K4_THREADS - 1) / K4_THREADS;
     float xr[XPT];
     int32_t bm_r = -1;
@@ -296,15 +344,113 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
             by_r = __ldg(P.topo + 2 * (int64_t)bm_r + 1);
         }
     };
+    // batch b's samples from the registers into shared memory (its parity's buffers)
+    auto stage = [&](int b) {
+        const int64_t i0 = s0 + (int64_t)b * K4_SB;
+        const int nb = (int)min64(K4_SB, s1 - i0);
+        float* xs = xs0 + (b & 1) * K4_SB * d;
+#pragma unroll
+        for (int j = 0; j < XPT; ++j) {
+            const int q = tid + j * K4_THREADS;
+            if (q < nb * d) xs[q] = xr[j];
+        }
+        if (warp == 1) {
+            const bool v = bm_r >= 0;
+            inv_s[lane] = inv_r;
+            rho_s[b & 1][lane] = v ? (float)rho_r : 0.0f;   // float32 training density
+            valid_s[b & 1][lane] = v;
+            bx_s[lane] = bx_r;
+            by_s[lane] = by_r;
+        }
+    };
+    // batch b's tables: lane s of the w-th warp that issues no MMAs computes sample s's entries of rows w, w + 12, ...;
+    // 2^15 is folded into the column factors; zero for absent samples
+    auto tables = [&](int b) {
+        if (warp % 5 == 0) return;
+        const int tw = warp - warp / 5 - 1;   // 0..11
+        float* tab = tab0 + (b & 1) * tabn;
+        const bool vs = valid_s[b & 1][lane] != 0;
+        const float ninv = -inv_s[lane], bx = bx_s[lane], by = by_s[lane];
+        // rows e and e + 12 in the two lanes of the float32 pairs
+        for (int e = tw; e < ntab; e += 24) {
+            const int e2 = e + 12;
+            const bool two = e2 < ntab, x1 = e < 2 * nrow, x2 = e2 < 2 * nrow;
+            const float2 dd = sub2_rn(make_float2(gc[e], two ? gc[e2] : 0.0f), make_float2(x1 ? bx : by, x2 ? bx : by));
+            const float2 xa = mul2_rn(mul2_rn(dd, dd), make_float2(ninv, ninv));   // -dd^2 / (2 sigma^2)
+            const float2 v = mul2_rn(make_float2(k4_exp(xa.x), k4_exp(xa.y)),
+                                     make_float2(x1 ? 1.0f : K4_ASCALE, x2 ? 1.0f : K4_ASCALE));
+            tab[e * K4_TPAD + lane] = vs ? v.x : 0.0f;
+            if (two) tab[e2 * K4_TPAD + lane] = vs ? v.y : 0.0f;
+        }
+    };
+    // batch b's B operand: thread t < 16 NB: feature row n = t mod NB, samples 2 (t / NB) + {0, 1}: rho x (scaled),
+    // rho, zeros; the hi parts to row n, the lo parts to row NB + n (a warp's lanes read consecutive features)
+    auto bgen = [&](int b) {
+        if (tid >= 16 * NB) return;
+        const float* xs = xs0 + (b & 1) * K4_SB * d;
+        const float* rs = rho_s[b & 1];
+        const int* vs = valid_s[b & 1];
+        const int nn = tid % NB, s = (tid / NB) * 2;
+        float v0 = 0.0f, v1 = 0.0f;
+        if (nn <= d) {
+            const float sc = scale_s[nn];
+            v0 = (nn < d ? rs[s] * xs[s * d + nn] : rs[s]) * sc;
+            v1 = (nn < d ? rs[s + 1] * xs[(s + 1) * d + nn] : rs[s + 1]) * sc;
+            if (!vs[s]) v0 = 0.0f;
+            if (!vs[s + 1]) v1 = 0.0f;
+        }
+        const __half2 hi = __floats2half2_rn(v0, v1);
+        const float2 hf = __half22float2(hi);
+        const __half2 lo = __floats2half2_rn(__fsub_rn(v0, hf.x), __fsub_rn(v1, hf.y));
+        *(uint32_t*)(sB + (b & 1) * B_BYTES + k4_off(nn, s)) = h2_bits(hi);
+        *(uint32_t*)(sB + (b & 1) * B_BYTES + k4_off(NB + nn, s)) = h2_bits(lo);
+    };
+    // batch b's A operand: this unit's factors, one K-step (16 samples, 8 TMEM columns) at a time
+    auto agen = [&](int b) {
+        const int sb = b & 1;
+        const float* tab = tab0 + sb * tabn;
+#pragma unroll
+        for (int ks = 0; ks < K4_SB / 16; ++ks) {
+            uint32_t hv[8], lv[8];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 ex = *(const float4*)(tab + tx + ks * 16 + q * 4);
+                const float4 ey = *(const float4*)(tab + ty + ks * 16 + q * 4);
+                const float2 h01 = mul2_rn(make_float2(ex.x, ex.y), make_float2(ey.x, ey.y));
+                const float2 h23 = mul2_rn(make_float2(ex.z, ex.w), make_float2(ey.z, ey.w));
+                // hi: h truncated to FP16's 11 significant bits (exact in FP16 for h >= 2^-29); lo = h - hi exactly
+                const float2 g01 = make_float2(trunc11(h01.x), trunc11(h01.y));
+                const float2 g23 = make_float2(trunc11(h23.x), trunc11(h23.y));
+                hv[2 * q] = h2_of(g01);
+                hv[2 * q + 1] = h2_of(g23);
+                lv[2 * q] = h2_of(sub2_rn(h01, g01));
+                lv[2 * q + 1] = h2_of(sub2_rn(h23, g23));
+            }
+            const uint32_t chi = K4_ACC_COLS + (uint32_t)((((sb * 2 + 0) * K4_MT + mt) * 2 + ks) * 8);
+            const uint32_t clo = K4_ACC_COLS + (uint32_t)((((sb * 2 + 1) * K4_MT + mt) * 2 + ks) * 8);
+            ptx::tmem_st8(tbase + lane_base + chi, hv);
+            ptx::tmem_st8(tbase + lane_base + clo, lv);
+        }
+    };
+
+    // Batch b: its tables were computed during batch b - 1, its samples staged then. Between the two barriers the CTA
+    // writes B and stages batch b + 1's samples; after the second the issuers take batch b - 1's MMAs, and the other
+    // warps write their units' A of batch b and compute batch b + 1's tables (half of the warps in each order, so that
+    // each scheduler has both kinds of work).
+    bool bad = false;
     if (nbatch > 0) {
         prefetch(0);
         prefetch_bmu();
+        stage(0);
+        __syncthreads();
+        tables(0);
+        if (nbatch > 1) {
+            prefetch(1);
+            prefetch_bmu();
+        }
     }
-
-    bool bad = false;
     for (int b = 0; b <= nbatch; ++b) {
-        // every thread has finished batch b - 1: its operands are written and fenced, the folds before it are done,
-        // its tables and samples are free; all stop together
+        // every thread has finished batch b - 1 (operands written and fenced, folds done) and batch b's tables
         if (__syncthreads_or(bad || *abort_v)) {
             bad = true;
             break;
@@ -317,93 +463,25 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
             }
             break;
         }
-        const int sb = b & 1;
-        const int64_t i0 = s0 + (int64_t)b * K4_SB;
-        const int nb = (int)min64(K4_SB, s1 - i0);
-#pragma unroll
-        for (int j = 0; j < XPT; ++j) {
-            const int q = tid + j * K4_THREADS;
-            if (q < nb * d) xs[q] = xr[j];
-        }
-        if (warp == 1) {
-            const bool v = bm_r >= 0;
-            inv_s[lane] = inv_r;
-            rho_s[lane] = v ? (float)rho_r : 0.0f;   // float32 training density
-            valid_s[lane] = v;
-            bx_s[lane] = bx_r;
-            by_s[lane] = by_r;
-        }
+        // operand buffer b mod 2 is free once the MMAs of batch b - 2 have completed
+        if (b >= 2) bad |= !ptx::mbar_wait(a_empty + (b & 1), (uint32_t)(((b >> 1) - 1) & 1), lim);
+        bgen(b);
+        ptx::fence_proxy_async();   // the B operand's generic writes, before the MMAs read them
+        if (b + 1 < nbatch) stage(b + 1);
         __syncthreads();
-        // the previous batch's MMAs: the issuers block while the tensor core takes them, so the tables below are
-        // computed by the other 12 warps
-        if (b >= 1 && issuer) {
-            ptx::tc_fence_after();
+        ptx::tc_fence_after();
+        if (b >= 1 && issuer) {   // the issuers wait while the tensor core takes each MMA
             issue(b - 1, 0);
             issue(b - 1, 1);
         }
-        if (b + 1 < nbatch) prefetch(b + 1);
-        // tables: lane s of the w-th warp that issues no MMAs computes sample s's entries of rows w, w + 12, ...;
-        // 2^15 is folded into the column factors; zero for absent samples
-        if (warp % 5 != 0) {
-            const int tw = warp - warp / 5 - 1;   // 0..11
-            const bool vs = valid_s[lane] != 0;
-            const float inv = inv_s[lane], bx = bx_s[lane], by = by_s[lane];
-#pragma unroll 2
-            for (int e = tw; e < ntab; e += 12) {
-                const bool isx = e < 2 * nrow;
-                const float dd = __fsub_rn(gc[e], isx ? bx : by);
-                const float v = (isx ? 1.0f : K4_ASCALE) * expf(-__fmul_rn(dd, dd) * inv);
-                tab[e * K4_TPAD + lane] = vs ? v : 0.0f;
-            }
-        }
-        // buffer sb is free once the MMAs of batch b - 2 have completed
-        if (b >= 2) bad |= !ptx::mbar_wait(a_empty + sb, (uint32_t)(((b >> 1) - 1) & 1), lim);
-        // B: thread t < 16 NB: feature row n = t mod NB, samples 2 (t / NB) + {0, 1}: rho x (scaled), rho, zeros;
-        // the hi parts to row n, the lo parts to row NB + n (a warp's lanes read consecutive features)
-        if (tid < 16 * NB) {
-            const int nn = tid % NB, s = (tid / NB) * 2;
-            float v0 = 0.0f, v1 = 0.0f;
-            if (nn <= d) {
-                const float sc = scale_s[nn];
-                v0 = (nn < d ? rho_s[s] * xs[s * d + nn] : rho_s[s]) * sc;
-                v1 = (nn < d ? rho_s[s + 1] * xs[(s + 1) * d + nn] : rho_s[s + 1]) * sc;
-                if (!valid_s[s]) v0 = 0.0f;
-                if (!valid_s[s + 1]) v1 = 0.0f;
-            }
-            const __half2 hi = __floats2half2_rn(v0, v1);
-            const float2 hf = __half22float2(hi);
-            const __half2 lo = __floats2half2_rn(__fsub_rn(v0, hf.x), __fsub_rn(v1, hf.y));
-            *(uint32_t*)(sB + sb * B_BYTES + k4_off(nn, s)) = h2_bits(hi);
-            *(uint32_t*)(sB + sb * B_BYTES + k4_off(NB + nn, s)) = h2_bits(lo);
-        }
-        ptx::fence_proxy_async();   // the B operand's generic writes, before the MMAs read them
-        __syncthreads();
-        ptx::tc_fence_after();
-        // A: this unit's factors for the batch's samples, one K-step (16 samples, 8 TMEM columns) at a time
-#pragma unroll
-        for (int ks = 0; ks < K4_SB / 16; ++ks) {
-            uint32_t hv[8], lv[8];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float4 ex = *(const float4*)(tx + ks * 16 + q * 4);
-                const float4 ey = *(const float4*)(ty + ks * 16 + q * 4);
-                const float h0 = __fmul_rn(ex.x, ey.x), h1 = __fmul_rn(ex.y, ey.y);
-                const float h2 = __fmul_rn(ex.z, ey.z), h3 = __fmul_rn(ex.w, ey.w);
-                // hi: h truncated to FP16's 11 significant bits (exact in FP16 for h >= 2^-29); lo = h - hi exactly
-                const float g0 = trunc11(h0), g1 = trunc11(h1), g2 = trunc11(h2), g3 = trunc11(h3);
-                hv[2 * q] = h2_bits(__floats2half2_rn(g0, g1));
-                hv[2 * q + 1] = h2_bits(__floats2half2_rn(g2, g3));
-                lv[2 * q] = h2_bits(__floats2half2_rn(__fsub_rn(h0, g0), __fsub_rn(h1, g1)));
-                lv[2 * q + 1] = h2_bits(__floats2half2_rn(__fsub_rn(h2, g2), __fsub_rn(h3, g3)));
-            }
-            const uint32_t chi = K4_ACC_COLS + (uint32_t)((((sb * 2 + 0) * K4_MT + mt) * 2 + ks) * 8);
-            const uint32_t clo = K4_ACC_COLS + (uint32_t)((((sb * 2 + 1) * K4_MT + mt) * 2 + ks) * 8);
-            ptx::tmem_st8(tbase + lane_base + chi, hv);
-            ptx::tmem_st8(tbase + lane_base + clo, lv);
-        }
+        if (b + 2 < nbatch) prefetch(b + 2);
+        const bool tables_first = ((warp >> 2) & 1) != 0;
+        if (tables_first && b + 1 < nbatch) tables(b + 1);
+        agen(b);
+        if (!tables_first && b + 1 < nbatch) tables(b + 1);
         ptx::tmem_wait_st();
         ptx::tc_fence_before();
-        prefetch_bmu();   // batch b + 1's BMU indices have arrived by now
+        prefetch_bmu();   // batch b + 2's BMU indices have arrived by now
         // the group that ended with batch b - 1 (its MMAs were issued during this batch): fold it now
         if (b >= 1 && (b - 1) % G == G - 1 && !bad) bad = !fold((b - 1) / G);
     }
@@ -413,7 +491,8 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
         for (int k = 0; k <= DMAX; ++k) {
             if (k > d) break;
             const double sc = (double)K4_ASCALE * (double)scale_s[k];
-            const double v = ((double)acc[k].x - (double)acc[k].y) / sc;
+            const float sk = (k & 1) ? asum[k / 2].y : asum[k / 2].x, ek = (k & 1) ? aerr[k / 2].y : aerr[k / 2].x;
+            const double v = ((double)sk - (double)ek) / sc;
             if (v != 0.0) atomicAdd(k < d ? P.num + (int64_t)u * d + k : P.den + u, v);
         }
     }
@@ -473,7 +552,7 @@ int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_
     const int64_t ntab = iter_tc_table_rows(rows, cols);
     // at least 120 KB, so that one CTA (which holds all 512 TMEM columns) is resident per SM
     const size_t smem = std::max<size_t>(
-        2 * K4_B_MAX + (size_t)(ntab + 1) * K4_TPAD * 4 + (size_t)K4_SB * d * 4 + (size_t)ntab * 4, 120 * 1024);
+        2 * K4_B_MAX + 2 * (size_t)(ntab + 1) * K4_TPAD * 4 + 2 * (size_t)K4_SB * d * 4 + (size_t)ntab * 4, 120 * 1024);
     auto kern = d <= 7    ? k4_iter_kernel<7, 16>
                 : d <= 15 ? k4_iter_kernel<15, 16>
                 : d <= 16 ? k4_iter_kernel<16, 32>
