@@ -710,8 +710,9 @@ def gpu_arm(args, ws, rank, local):
         som = dg.SOM_Batch(w['m'], w['n'], D, topology=w['topology'], sigma=w['sigma0'])
         som.bmu_algo = args.algo
         e2e_steps = max(1, min(args.steps, 5))
-        som._weights[...] = w0
-        som.train(xh, n_epochs=1, use_best_epoch=False)      # warm-up (allocations, library state)
+        for _ in range(2):                                      # warm-up (allocations, library state)
+            som._weights[...] = w0
+            som.train(xh, n_epochs=1, use_best_epoch=False)
         barrier()
         t0 = time.perf_counter()
         calls = []

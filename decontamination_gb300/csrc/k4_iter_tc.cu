@@ -9,26 +9,31 @@
 // (two MMA K-steps); its 512 threads (16 warps) each own one unit:
 //   * thread t holds TMEM lane t mod 128 of M tile t / 128 and the unit of slot t in the CTA's order (even grid columns
 //     first, then odd, rows ascending within a column), so that a warp's 32 units share few table rows;
-//   * per batch the 12 warps that issue no MMAs compute the per-sample exponential tables over the grid rows (by
-//     column parity) and grid columns of the CTA's units (float32 arguments as the float32 CUDA-core pass forms them,
-//     the exponential from the hardware base-2 approximation with an extended-precision argument, k4_exp);
-//   * each thread writes its unit's factors A[u, s] = 2^15 h[s, u], split into FP16 hi (h truncated to 11 significant
-//     bits) + lo (the exact rest, rounded) parts, into its TMEM lane (tcgen05.st), and the CTA writes the B operand to
-//     shared memory: rows [0, NB) the FP16 hi parts and rows [NB, 2 NB) the lo parts of B[n, s] = rho_s x_s[n]
-//     (n < D), rho_s (n = D), 0 (D < n < NB), each column scaled by a power of two from the catalogue's bounds;
-//   * lane 0 of warps 0, 5, 10, 15 (one per scheduler) issues its M tile's MMAs of the previous batch after the
-//     batch's second barrier, 128 x 2 NB x 16 with A from TMEM and B from shared memory: per K-step A_lo.B then A_hi.B
-//     (accumulator columns [0, NB) sum A.B_hi, [NB, 2 NB) A.B_lo); an issuing thread waits while the tensor core takes
-//     each MMA (about 46 cycles), which is why those warps compute no tables;
+//   * a batch has two CTA barriers. Between them the CTA writes the batch's B operand to shared memory (rows
+//     [0, NB) the FP16 hi parts and rows [NB, 2 NB) the lo parts of B[n, s] = rho_s x_s[n] (n < D), rho_s (n = D),
+//     0 (D < n < NB), each feature scaled by a power of two from the catalogue's bounds) and stages the next batch's
+//     samples (loaded into registers a batch earlier);
+//   * after the second, lane 0 of warps 0, 5, 10, 15 (one per scheduler) issues its M tile's MMAs of the previous
+//     batch, 128 x 2 NB x 16 with A from TMEM and B from shared memory: per K-step A_lo.B then A_hi.B (accumulator
+//     columns [0, NB) sum A.B_hi, [NB, 2 NB) A.B_lo); an issuing thread waits while the tensor core takes each MMA
+//     (about 46 cycles), which is why those warps compute no tables;
+//   * meanwhile each thread writes its unit's factors A[u, s] = 2^15 h[s, u] of this batch, split into FP16 hi (h
+//     truncated to 11 significant bits) + lo (the exact rest, rounded) parts, into its TMEM lane (tcgen05.st), and the
+//     other 12 warps compute the next batch's exponential tables over the grid rows (by column parity) and grid
+//     columns of the CTA's units (float32 arguments as the float32 CUDA-core pass forms them, the exponential from the
+//     hardware base-2 approximation with an extended-precision argument, k4_exp), half of them before their A and
+//     half after, so that every scheduler has both kinds of work;
 //   * every `group` batches each thread reads its unit's accumulator row (tcgen05.ld), adds the two halves and adds
 //     them to compensated float32 sums; at the end of the chunk it adds those to num, den in float64.
+// The tables, samples and operands are double-buffered by batch parity.
 // TMEM (512 columns): NB = 16 (D <= 15) two accumulator sets of 4 x 32 columns, NB = 32 one set of 4 x 64, at
 // [0, 256); A operands at [256, 512): (buffer, split, M tile, K-step) at 256 + 8 (((buffer * 2 + split) * 4 + tile) *
 // 2 + K-step). An MMA of N <= 64 columns takes as long as one of 64, so the hi and lo parts of B share one MMA.
 // Error budget: 2^-21 relative per product from the FP16 parts, then the tensor core's FP32 accumulation, which loses
 // low bits with every MMA (measured: ~20 float32 ulps over 16 MMAs, ~8 over the 8 MMAs of a 2-batch group, ~3 over 4),
-// then float32 rounding of the compensated sums. With `group` = 2 the sums differ from the float32 CUDA-core pass by
-// at most 5.1e-7 relative (12.6 M samples on a 64 x 64 map), for 8% of the time a 1-batch group would take.
+// then float32 rounding of the compensated sums, besides the float32 tables (k4_exp: within the ex2 approximation's
+// error of e^x). With `group` = 2 the sums differ from the float32 CUDA-core pass (expf) by at most 6e-7 relative
+// (12.6 M samples on a 64 x 64 map), for 8% of the time a 1-batch group would take.
 // Every wait is bounded: one that gives up sets bit 65536 of the status words and the CTA returns.
 #include <cuda_fp16.h>
 
