@@ -731,6 +731,11 @@ def gpu_arm(args, ws, rank, local):
                               'weights/history/errors back to the host'}
         del som
 
+    # --- BMU serving (rank 0, one GPU), before the other sub-records' large buffers come and go --------------------------
+    if not args.skip_serve and rank == 0 and ws == 1:
+        out['serve'] = serve_record(args)
+        torch.cuda.empty_cache()
+
     # --- iteration mode on the resident catalogue and the trained map (rank 0, one GPU) --------------------------------------
     if not args.skip_iter and rank == 0 and ws == 1 and w['topology'] in ('square', 'hexagonal'):
         out['iteration'] = iteration_record(torch, _native, xd, runner.wcur, topo.float(), w, device)
@@ -738,10 +743,6 @@ def gpu_arm(args, ws, rank, local):
 
     del runner, xd
     torch.cuda.empty_cache()
-    # --- BMU serving (rank 0, one GPU), before the large D = 32 catalogue comes and goes ----------------------------------
-    if not args.skip_serve and rank == 0 and ws == 1:
-        out['serve'] = serve_record(args)
-        torch.cuda.empty_cache()
 
     # --- the 64x64, D = 32 configuration (rank 0, one GPU) ---------------------------------------------------------------
     if not args.skip_sq64 and rank == 0 and ws == 1 and args.n is None:
