@@ -47,6 +47,7 @@ SIGNATURES = {
     'somgb_train_bmu_pass': [P, P, I64, I32, P, P, I64, D, I32, P, P, P, SZ, P],
     'somgb_workspace_status': [P, P, I32, P],
     'somgb_debug_tc_withhold': [I64, ctypes.c_uint],
+    'somgb_debug_iter_withhold': [ctypes.c_int, ctypes.c_uint],
     'somgb_accumulate': [P, P, P, I64, I32, I64, P, P, P, P],
     'somgb_feature_bounds': [P, P, I64, I32, P, P],
     'somgb_accumulate_f64': [P, P, P, I64, I32, I64, P, P, P],

@@ -334,6 +334,12 @@ int somgb_debug_tc_withhold(int64_t row_tile, unsigned int wait_limit) {
     return SOMGB_OK;
 }
 
+int somgb_debug_iter_withhold(int group, unsigned int wait_limit) {
+    if (group < 0 || wait_limit == 0) return set_error(SOMGB_ERR_INVALID, "group must be >= 0, wait_limit > 0");
+    iter_tc_debug_withhold(group, wait_limit);
+    return SOMGB_OK;
+}
+
 int somgb_feature_bounds(const float* x, const double* rho, int64_t n, int d, float* bounds, somgb_stream_t stream) {
     if (n < 0 || d <= 0) return set_error(SOMGB_ERR_INVALID, "invalid sizes");
     if ((n > 0 && !x) || !bounds) return set_error(SOMGB_ERR_INVALID, "x/bounds is NULL");

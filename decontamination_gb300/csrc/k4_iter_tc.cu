@@ -77,6 +77,7 @@ struct K4Args {
     unsigned int* status;
     unsigned int* gstatus;
     int group;             // batches per accumulator set before it is folded
+    int withhold_group;    // test hook: this group's completion is never signalled (-1: none)
     uint32_t wait_limit;
 };
 
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
         ptx::mma_f16_ta(dt, ahi, bd, IDESC, 1u);
         if (ks == 1) {
             ptx::mma_commit(a_empty + sb);
-            if (b % G == G - 1 || b == nbatch - 1) ptx::mma_commit(acc_full + ab);
+            if ((b % G == G - 1 || b == nbatch - 1) && g != P.withhold_group) ptx::mma_commit(acc_full + ab);
         }
     };
     // folds group g's accumulator set into acc; false when its wait gave up
@@ -512,7 +513,17 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     }
 }
 
+// Test hook (somgb_debug_iter_withhold): the next contraction on this thread withholds one group's completion and
+// bounds its waits by `limit` polls; one-shot.
+thread_local int t_withhold_group = -1;
+thread_local uint32_t t_wait_limit = 0;
+
 }  // namespace
+
+void iter_tc_debug_withhold(int group, uint32_t wait_limit) {
+    t_withhold_group = group;
+    t_wait_limit = wait_limit;
+}
 
 // Table rows of the CTA with the most: 2 per grid row that its units touch, plus its grid columns.
 int64_t iter_tc_table_rows(int64_t rows, int64_t cols) {
@@ -552,7 +563,10 @@ int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_
     P.cur_vector = cur_vector; P.n_vectors = n_vectors; P.chunk = chunk; P.bounds = bounds;
     P.num = num; P.den = den; P.status = status; P.gstatus = device_status_word();
     P.group = 2;
-    P.wait_limit = 1u << 22;
+    P.withhold_group = t_withhold_group;
+    P.wait_limit = t_wait_limit ? t_wait_limit : (1u << 22);
+    t_withhold_group = -1;   // one-shot
+    t_wait_limit = 0;
     if (!P.gstatus) return set_error(SOMGB_ERR_CUDA, "device status word unavailable");
     const int64_t ntab = iter_tc_table_rows(rows, cols);
     // at least 120 KB, so that one CTA (which holds all 512 TMEM columns) is resident per SM

@@ -666,9 +666,12 @@ __global__ void __launch_bounds__(IG_THREADS) iter_grid_kernel(const float* __re
         for (int sidx = 0; sidx < nb; ++sidx) {
             const float* tb = tab + sidx * ntab;
             const float* xr = xs + sidx * d;
+            // a sample without a training BMU (non-finite features or weight <= 0) adds nothing: its factors are 0 and
+            // its features are read as 0, so that 0 * NaN cannot reach the sums
+            const bool ok = valid_s[sidx] != 0;
             float xv[DMAX];
 #pragma unroll
-            for (int k = 0; k < DMAX; ++k) xv[k] = k < d ? xr[k] : 0.0f;
+            for (int k = 0; k < DMAX; ++k) xv[k] = (k < d && ok) ? xr[k] : 0.0f;
 #pragma unroll
             for (int t = 0; t < UPT; ++t) {
                 const float h = tb[tx_i[t]] * tb[tx_j[t]];

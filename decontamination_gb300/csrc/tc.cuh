@@ -29,6 +29,9 @@ bool iter_tc_shape_ok(int64_t rows, int64_t cols, int d);
 int64_t iter_tc_table_rows(int64_t rows, int64_t cols);
 // num[u, :] += sum_i h_iu rho_i x_i, den[u] += sum_i h_iu rho_i over the samples with bmu[i] >= 0 (iteration-mode
 // neighbourhood of sample cur_vector + i), `bounds` from launch_feature_bounds over the same samples.
+// Test hook: the next K4 launch on this thread never signals that accumulator group `group` is complete and bounds its
+// waits by `wait_limit` polls, so that the fold's wait runs out.
+void iter_tc_debug_withhold(int group, uint32_t wait_limit);
 int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, const float* topo,
                    int64_t rows, int64_t cols, double sigma0, int64_t cur_vector, int64_t n_vectors,
                    const float* bounds, double* num, double* den, unsigned int* status, cudaStream_t stream);

@@ -91,6 +91,15 @@ int somgb_workspace_status(const void* ws, unsigned int* status, int clear, somg
  */
 int somgb_debug_tc_withhold(int64_t row_tile, unsigned int wait_limit);
 
+/*
+ * Test hook for the bounded waits of the tensor-core iteration contraction (somgb_train_iter_pass_grid under
+ * SOMGB_ALGO_TC): the next contraction on the calling thread never signals that its accumulator group `group` (of two
+ * 32-sample batches per CTA) is complete and bounds its waits by `wait_limit` polls, so that the fold's wait runs out:
+ * each CTA stops, drains the MMAs it issued, frees its TMEM and returns with bit 65536 of the workspace's and the
+ * device's status words set; its partial sums are not added. One-shot; no product call sets it.
+ */
+int somgb_debug_iter_withhold(int group, unsigned int wait_limit);
+
 /* 1 if `algo` can run a pass of these sizes on the current device, else 0. */
 int somgb_algo_supported(int algo, int64_t n, int64_t m, int d);
 

@@ -97,6 +97,10 @@ def test_debug_hook_arguments_are_checked(native):
         native.call('somgb_debug_tc_withhold', -1, 100)
     with pytest.raises(native.SomgbError):
         native.call('somgb_debug_tc_withhold', 0, 0)
+    with pytest.raises(native.SomgbError):
+        native.call('somgb_debug_iter_withhold', -1, 100)
+    with pytest.raises(native.SomgbError):
+        native.call('somgb_debug_iter_withhold', 0, 0)
 
 
 def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
@@ -173,3 +177,77 @@ def test_grid_iteration_pass_matches_the_float64_pass(cuda, native, oracle, m, n
     st = ctypes.c_uint(0)
     native.call('somgb_device_status', ctypes.addressof(st), 1, s)
     assert st.value == 0, 'no bounded wait ran out'
+
+
+def _iter_pass(native, cuda, xd, rd, wd, td, m, n, sigma0, algo, ws=None):
+    N, d = xd.shape
+    M = m * n
+    num = torch.zeros((M, d), dtype=torch.float64, device=cuda)
+    den = torch.zeros(M, dtype=torch.float64, device=cuda)
+    buf, wsp, nbytes = ws if ws is not None else _ws(native, native.OP_EPOCH, N, M, d, algo, cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    if algo is None:
+        native.call('somgb_train_iter_pass', xd.data_ptr(), None if rd is None else rd.data_ptr(), N, d, wd.data_ptr(),
+                    td.data_ptr(), M, sigma0, 500, 2 * N, num.data_ptr(), den.data_ptr(), wsp, nbytes, s)
+    else:
+        native.call('somgb_train_iter_pass_grid', xd.data_ptr(), None if rd is None else rd.data_ptr(), N, d,
+                    wd.data_ptr(), td.data_ptr(), m, n, sigma0, 500, 2 * N, algo, num.data_ptr(), den.data_ptr(), wsp,
+                    nbytes, s)
+    torch.cuda.synchronize()
+    return num.cpu().numpy(), den.cpu().numpy()
+
+
+@pytest.mark.parametrize('sigma0', [6.0, 1e-13])
+@pytest.mark.parametrize('algo', ['tc', 'fp32'])
+def test_iteration_pass_edge_cases(cuda, native, oracle, sigma0, algo):
+    """Non-finite rows (no training BMU: they add nothing), zero weights (likewise), and sigma clamped at 1e-12 (every
+    factor 0 but the BMU's own, 1): both grid forms against the float64 pass."""
+    rng = np.random.default_rng(int(sigma0 > 1) + 2 * (algo == 'tc'))
+    m = n = 32
+    d, N, M = 16, 30_000, 1024
+    x = synthetic.correlated_lognormal(N, d, 4)
+    w = x[rng.integers(0, N, M)].copy()
+    x[rng.choice(N, N // 50, replace=False), rng.integers(0, d)] = np.nan
+    rho = rng.random(N)
+    rho[rng.random(N) < 0.05] = 0.0
+    topo = oracle.topography(m, n, 'hexagonal')
+    xd, wd, td = (torch.from_numpy(np.ascontiguousarray(a)).to(cuda) for a in (x, w, topo))
+    rd = torch.from_numpy(rho).to(cuda)
+    n_g, d_g = _iter_pass(native, cuda, xd, rd, wd, td, m, n, sigma0, native.ALGOS[algo])
+    n_r, d_r = _iter_pass(native, cuda, xd, rd, wd, td, m, n, sigma0, None, _ws(native, native.OP_EPOCH, N, M, d,
+                                                                                   native.ALGO_FP32, cuda))
+    assert np.isfinite(n_g).all() and np.isfinite(d_g).all()
+    np.testing.assert_allclose(d_g, d_r, rtol=2e-6, atol=1e-9 * d_r.max())
+    np.testing.assert_allclose(n_g, n_r, rtol=2e-6, atol=2e-6 * np.abs(n_r).max())
+
+
+def test_a_wait_of_the_iteration_contraction_that_runs_out(cuda, native, oracle):
+    """The test hook withholds the completion of the first accumulator group: every CTA's fold wait runs out, the call
+    reports bit 65536 in its workspace's and the device's status words instead of hanging, and the next call gives the
+    normal sums."""
+    rng = np.random.default_rng(23)
+    m = n = 32
+    d, N, M = 16, 50_000, 1024
+    x = synthetic.correlated_lognormal(N, d, 6)
+    w = x[rng.integers(0, N, M)].copy()
+    topo = oracle.topography(m, n, 'square')
+    xd, wd, td = (torch.from_numpy(np.ascontiguousarray(a)).to(cuda) for a in (x, w, topo))
+    s = torch.cuda.current_stream().cuda_stream
+    ws1 = _ws(native, native.OP_EPOCH, N, M, d, native.ALGO_TC, cuda)
+    ws2 = _ws(native, native.OP_EPOCH, N, M, d, native.ALGO_TC, cuda)
+    st = ctypes.c_uint(0)
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    before = _iter_pass(native, cuda, xd, None, wd, td, m, n, 8.0, native.ALGO_TC, ws1)
+    native.call('somgb_debug_iter_withhold', 0, 20_000)
+    _iter_pass(native, cuda, xd, None, wd, td, m, n, 8.0, native.ALGO_TC, ws1)
+    native.call('somgb_workspace_status', ws1[1], ctypes.addressof(st), 0, s)
+    assert st.value & 65536, 'the call whose wait ran out reports it in its own workspace'
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    assert st.value & 65536
+    after = _iter_pass(native, cuda, xd, None, wd, td, m, n, 8.0, native.ALGO_TC, ws2)   # the hook is one-shot
+    np.testing.assert_allclose(after[0], before[0], rtol=1e-12, atol=1e-12 * np.abs(before[0]).max())
+    np.testing.assert_allclose(after[1], before[1], rtol=1e-12)
+    native.call('somgb_workspace_status', ws2[1], ctypes.addressof(st), 0, s)
+    assert st.value == 0
+    native.call('somgb_device_status', ctypes.addressof(st), 1, s)
+    assert st.value == 0
