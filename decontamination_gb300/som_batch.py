@@ -301,7 +301,8 @@ class SOM_Batch(SOM_Abstract):
         den = torch.zeros(M, dtype=torch.float64, device=device)
         sigma0 = float(self._dtype(self._sigma))
         cur = 0
-        grid = not self._is_f64 and D <= 64   # float32 maps: the grid-factorised float32 pass, BMUs by bmu_algo
+        grid = not self._is_f64 and D <= 64   # float32 maps: the grid-factorised pass, BMUs by bmu_algo
+        status = _device.StatusCheck(device)
         for xc, rc in iterate_chunks(dataset, dataset_weights, self._dtype, device):
             count = min(_device.rows(xc), n_vectors - cur)
             xk = xc[:count]
@@ -311,6 +312,7 @@ class SOM_Batch(SOM_Abstract):
                 _native.call('somgb_train_iter_pass_grid', xk.data_ptr(), _device.ptr(rk), count, D, w.data_ptr(),
                              topo.data_ptr(), self._m, self._n, sigma0, cur, n_vectors, self._algo, num.data_ptr(),
                              den.data_ptr(), wsp, wsb, _device.stream())
+                status.note(self._ws)
             else:
                 name = 'somgb_train_iter_pass_f64' if self._is_f64 else 'somgb_train_iter_pass'
                 wsp, wsb = self._ws.for_op(_native.OP_EPOCH, count, M, D, _native.ALGO_FP32, device)
@@ -319,6 +321,7 @@ class SOM_Batch(SOM_Abstract):
             cur += count
             if cur >= n_vectors:
                 break
+        status.check()   # a bounded wait that gave up fails the call before its sums are used
         w_new = torch.empty((M, D), dtype=td, device=device)
         _native.call('somgb_divide_f64' if self._is_f64 else 'somgb_divide', num.data_ptr(), den.data_ptr(), M, D,
                      w_new.data_ptr(), _device.stream())

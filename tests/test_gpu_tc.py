@@ -138,7 +138,7 @@ def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
     (64, 64, 16, 'square', 'tc', 15_000), (32, 32, 16, 'hexagonal', 'tc', 60_000),
     (20, 17, 5, 'square', 'auto', 60_000), (1, 300, 3, 'hexagonal', 'auto', 20_000),
     (80, 80, 8, 'hexagonal', 'tc', 8_000), (2, 300, 4, 'square', 'tc', 10_000), (64, 64, 31, 'square', 'auto', 10_000),
-    (32, 32, 16, 'square', 'tc', 37), (32, 32, 4, 'square', 'tc', 64),
+    (32, 32, 16, 'square', 'tc', 37), (32, 32, 4, 'square', 'tc', 64), (40, 40, 20, 'square', 'auto', 10_000),
     # the float32 CUDA-core pass: the FP32 algorithm, D = 32 (above the tensor-core contraction's limit), and grid rows
     # too long for the tensor-core contraction's tables
     (32, 32, 16, 'hexagonal', 'fp32', 60_000), (20, 17, 5, 'square', 'fp32', 60_000),
@@ -251,3 +251,35 @@ def test_a_wait_of_the_iteration_contraction_that_runs_out(cuda, native, oracle)
     assert st.value == 0
     native.call('somgb_device_status', ctypes.addressof(st), 1, s)
     assert st.value == 0
+
+
+def test_iteration_training_through_the_api_on_the_tensor_cores(cuda, native):
+    """SOM_Batch.train(n_vectors=...) with the tensor-core algorithm (BMU pass and contraction on the tensor cores) and
+    with the FP32 algorithm (both on the CUDA cores) give the same map; a wait of the contraction that runs out fails
+    the call with SOMGB_ERR_TIMEOUT, and the next call trains normally."""
+    import decontamination_gb300 as dg
+    m = n = 32
+    d, N = 16, 300_000
+    x = torch.from_numpy(synthetic.correlated_lognormal(N, d, 8)).to(cuda)
+    w0 = synthetic.uniform_weights(m * n, d, 8)
+    maps = {}
+    for algo in ('tc', 'fp32'):
+        som = dg.SOM_Batch(m, n, d, topology='hexagonal', sigma=8.0)
+        som._weights[...] = w0.reshape(som._weights.shape)
+        som.bmu_algo = algo
+        som.train(x, n_vectors=N)
+        maps[algo] = (som.weights.copy(), som.quantization_errors.copy())
+    np.testing.assert_allclose(maps['tc'][0], maps['fp32'][0], rtol=2e-5, atol=2e-6)
+    np.testing.assert_allclose(maps['tc'][1], maps['fp32'][1], rtol=1e-5)
+    som = dg.SOM_Batch(m, n, d, topology='hexagonal', sigma=8.0)
+    som._weights[...] = w0.reshape(som._weights.shape)
+    som.bmu_algo = 'tc'
+    native.call('somgb_debug_iter_withhold', 0, 20_000)
+    with pytest.raises(native.SomgbError) as ei:
+        som.train(x, n_vectors=N)
+    assert ei.value.status == native.SOMGB_ERR_TIMEOUT
+    som._weights[...] = w0.reshape(som._weights.shape)
+    som.train(x, n_vectors=N)
+    np.testing.assert_allclose(som.weights, maps['tc'][0], rtol=1e-9, atol=1e-12)
+    st = ctypes.c_uint(0)
+    native.call('somgb_device_status', ctypes.addressof(st), 1, torch.cuda.current_stream().cuda_stream)
