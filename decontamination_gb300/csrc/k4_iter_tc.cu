@@ -5,30 +5,31 @@
 //   num[u, k] = sum_s h[s, u] rho_s x_s[k],   den[u] = sum_s h[s, u] rho_s,
 //   h[s, u] = exp(-|t_u - t_b(s)|^2 / (2 sigma_s^2)) = Ex_s[row(u), col(u) mod 2] * Ey_s[col(u)]
 // on the reference's square and hexagonal grids (a unit's x depends on its row and its column's parity, its y on its
-// column). Each CTA owns 512 units (four 128-unit M tiles) and a chunk of the samples, taken in batches of 32 samples
-// (two MMA K-steps); its 512 threads (16 warps) each own one unit:
+// column). Each CTA owns 512 units (four 128-unit M tiles; 384 units, three tiles, for D >= 32) and a chunk of the
+// samples, taken in batches of 32 samples (two MMA K-steps); each of its threads (16 warps, or 12) owns one unit:
 //   * thread t holds TMEM lane t mod 128 of M tile t / 128 and the unit of slot t in the CTA's order (even grid columns
 //     first, then odd, rows ascending within a column), so that a warp's 32 units share few table rows;
 //   * a batch has two CTA barriers. Between them the CTA writes the batch's B operand to shared memory (rows
 //     [0, NB) the FP16 hi parts and rows [NB, 2 NB) the lo parts of B[n, s] = rho_s x_s[n] (n < D), rho_s (n = D),
 //     0 (D < n < NB), each feature scaled by a power of two from the catalogue's bounds) and stages the next batch's
 //     samples (loaded into registers a batch earlier);
-//   * after the second, lane 0 of warps 0, 5, 10, 15 (one per scheduler) issues its M tile's MMAs of the previous
+//   * after the second, lane 0 of warps 0, 5, 10 (, 15) (one per scheduler) issues its M tile's MMAs of the previous
 //     batch, 128 x 2 NB x 16 with A from TMEM and B from shared memory: per K-step A_lo.B then A_hi.B (accumulator
 //     columns [0, NB) sum A.B_hi, [NB, 2 NB) A.B_lo); an issuing thread waits while the tensor core takes each MMA
 //     (about 46 cycles), which is why those warps compute no tables;
 //   * meanwhile each thread writes its unit's factors A[u, s] = 2^15 h[s, u] of this batch, split into FP16 hi (h
 //     truncated to 11 significant bits) + lo (the exact rest, rounded) parts, into its TMEM lane (tcgen05.st), and the
-//     other 12 warps compute the next batch's exponential tables over the grid rows (by column parity) and grid
+//     other warps compute the next batch's exponential tables over the grid rows (by column parity) and grid
 //     columns of the CTA's units (float32 arguments as the float32 CUDA-core pass forms them, the exponential from the
 //     hardware base-2 approximation with an extended-precision argument, k4_exp), half of them before their A and
 //     half after, so that every scheduler has both kinds of work;
 //   * every `group` batches each thread reads its unit's accumulator row (tcgen05.ld), adds the two halves and adds
 //     them to compensated float32 sums; at the end of the chunk it adds those to num, den in float64.
 // The tables, samples and operands are double-buffered by batch parity.
-// TMEM (512 columns): NB = 16 (D <= 15) two accumulator sets of 4 x 32 columns, NB = 32 one set of 4 x 64, at
-// [0, 256); A operands at [256, 512): (buffer, split, M tile, K-step) at 256 + 8 (((buffer * 2 + split) * 4 + tile) *
-// 2 + K-step). An MMA of N <= 64 columns takes as long as one of 64, so the hi and lo parts of B share one MMA.
+// TMEM (512 columns): NB = 16 (D <= 15) two accumulator sets of 4 x 32 columns, NB = 32 (D <= 31) one set of 4 x 64,
+// NB = 48 (D <= 47) one set of 3 x 96, from column 0; then the A operands, (buffer, split, M tile, K-step) at
+// ACC + 8 (((buffer * 2 + split) * tiles + tile) * 2 + K-step). An MMA of N <= 64 columns takes as long as one of
+// 64, so the hi and lo parts of B share one MMA.
 // Error budget: 2^-21 relative per product from the FP16 parts, then the tensor core's FP32 accumulation, which loses
 // low bits with every MMA (measured: ~20 float32 ulps over 16 MMAs, ~8 over the 8 MMAs of a 2-batch group, ~3 over 4),
 // then float32 rounding of the compensated sums, besides the float32 tables (k4_exp: within the ex2 approximation's
@@ -47,16 +48,13 @@ namespace somgb {
 
 namespace {
 
-constexpr int K4_MT = 4;                       // 128-unit M tiles per CTA
-constexpr int K4_UNITS = 128 * K4_MT;
-constexpr int K4_THREADS = K4_UNITS;           // one thread per unit
+constexpr int K4_UNITS_MAX = 512;              // units per CTA: 128 per M tile, 4 tiles (3 for D >= 32)
 constexpr int K4_SB = 32;                      // samples per batch: two K-steps of 16
-constexpr int K4_NB_MAX = 32;                  // B rows per FP16 part: the D features, the density, zero rows
+constexpr int K4_NB_MAX = 48;                  // B rows per FP16 part: the D features, the density, zero rows
 constexpr int K4_TPAD = 36;                    // floats per table row: 32 samples + 4 (conflict-free 16-byte reads)
 constexpr int K4_TAB_MAX = 320;                // table rows (2 per grid row + 1 per grid column) of a CTA
 constexpr uint32_t K4_B_MAX = 2 * K4_NB_MAX * K4_SB * 2;   // bytes of one batch's B operand
 constexpr uint32_t K4_SBO = (K4_SB / 8) * 128;      // bytes between the 8-row groups of the canonical layout
-constexpr uint32_t K4_ACC_COLS = 256;               // accumulator columns; the A operands follow
 constexpr unsigned K4_FAIL = 65536u;
 constexpr float K4_ASCALE = 32768.0f;          // A = 2^15 h: FP16 normals down to h = 2^-29
 
@@ -148,13 +146,17 @@ __device__ __forceinline__ float inv_sigma_of(const float* c, float t) {
     return __fadd_rn(v, __fadd_rn(ve, __fmaf_rn(p, c[3], __fmul_rn(r, c[2]))));
 }
 
-template <int DMAX, int NB>
-__global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) {
+template <int DMAX, int NB, int K4_MT>
+__global__ void __launch_bounds__(128 * K4_MT, 1) k4_iter_kernel(const K4Args P) {
+    constexpr int K4_UNITS = 128 * K4_MT;
+    constexpr int K4_THREADS = K4_UNITS;            // one thread per unit
+    constexpr int TW = K4_THREADS / 32 - K4_MT;     // the warps that issue no MMAs compute the tables
     constexpr int N = 2 * NB;                       // MMA N: hi rows then lo rows of B
     constexpr int NSET = NB == 16 ? 2 : 1;          // accumulator sets
     constexpr uint32_t IDESC = ptx::idesc_f16_f32(128, N);
     constexpr uint32_t B_BYTES = N * K4_SB * 2;
-    static_assert(NSET * K4_MT * N <= (int)K4_ACC_COLS && DMAX < NB, "accumulators fit below the A operands");
+    constexpr uint32_t K4_ACC_COLS = NSET * K4_MT * N;   // accumulator columns; the A operands follow
+    static_assert(K4_ACC_COLS + 64 * K4_MT <= 512 && DMAX < NB && N <= 256 && K4_MT <= 4, "the TMEM layout fits");
     extern __shared__ __align__(128) uint8_t k4_raw[];
     uint8_t* sB = k4_raw;                              // [buffer] B operands
     float* tab0 = (float*)(k4_raw + 2 * K4_B_MAX);     // [batch parity][table row][K4_TPAD]; row ntab is all zeros
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     __shared__ float rho_s[2][K4_SB];                  // [batch parity]
     __shared__ int valid_s[2][K4_SB];
     __shared__ float poly_s[5];
-    __shared__ int perm_s[K4_UNITS];
+    __shared__ int perm_s[K4_UNITS_MAX];
     __shared__ __align__(8) uint64_t bars[5];
     __shared__ uint32_t tmem_s;
     __shared__ int abort_s;
@@ -373,13 +375,13 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
     // 2^15 is folded into the column factors; zero for absent samples
     auto tables = [&](int b) {
         if (warp % 5 == 0) return;
-        const int tw = warp - warp / 5 - 1;   // 0..11
+        const int tw = warp - warp / 5 - 1;   // 0 .. TW - 1
         float* tab = tab0 + (b & 1) * tabn;
         const bool vs = valid_s[b & 1][lane] != 0;
         const float ninv = -inv_s[lane], bx = bx_s[lane], by = by_s[lane];
-        // rows e and e + 12 in the two lanes of the float32 pairs
-        for (int e = tw; e < ntab; e += 24) {
-            const int e2 = e + 12;
+        // rows e and e + TW in the two lanes of the float32 pairs
+        for (int e = tw; e < ntab; e += 2 * TW) {
+            const int e2 = e + TW;
             const bool two = e2 < ntab, x1 = e < 2 * nrow, x2 = e2 < 2 * nrow;
             const float2 dd = sub2_rn(make_float2(gc[e], two ? gc[e2] : 0.0f), make_float2(x1 ? bx : by, x2 ? bx : by));
             const float2 xa = mul2_rn(mul2_rn(dd, dd), make_float2(ninv, ninv));   // -dd^2 / (2 sigma^2)
@@ -389,27 +391,29 @@ __global__ void __launch_bounds__(K4_THREADS, 1) k4_iter_kernel(const K4Args P) 
             if (two) tab[e2 * K4_TPAD + lane] = vs ? v.y : 0.0f;
         }
     };
-    // batch b's B operand: thread t < 16 NB: feature row n = t mod NB, samples 2 (t / NB) + {0, 1}: rho x (scaled),
-    // rho, zeros; the hi parts to row n, the lo parts to row NB + n (a warp's lanes read consecutive features)
+    // batch b's B operand: item p < 16 NB (items strided over the threads): feature row n = p mod NB, samples
+    // 2 (p / NB) + {0, 1}: rho x (scaled), rho, zeros; the hi parts to row n, the lo parts to row NB + n (a warp's lanes
+    // read consecutive features)
     auto bgen = [&](int b) {
-        if (tid >= 16 * NB) return;
         const float* xs = xs0 + (b & 1) * K4_SB * d;
         const float* rs = rho_s[b & 1];
         const int* vs = valid_s[b & 1];
-        const int nn = tid % NB, s = (tid / NB) * 2;
-        float v0 = 0.0f, v1 = 0.0f;
-        if (nn <= d) {
-            const float sc = scale_s[nn];
-            v0 = (nn < d ? rs[s] * xs[s * d + nn] : rs[s]) * sc;
-            v1 = (nn < d ? rs[s + 1] * xs[(s + 1) * d + nn] : rs[s + 1]) * sc;
-            if (!vs[s]) v0 = 0.0f;
-            if (!vs[s + 1]) v1 = 0.0f;
+        for (int p = tid; p < 16 * NB; p += K4_THREADS) {
+            const int nn = p % NB, s = (p / NB) * 2;
+            float v0 = 0.0f, v1 = 0.0f;
+            if (nn <= d) {
+                const float sc = scale_s[nn];
+                v0 = (nn < d ? rs[s] * xs[s * d + nn] : rs[s]) * sc;
+                v1 = (nn < d ? rs[s + 1] * xs[(s + 1) * d + nn] : rs[s + 1]) * sc;
+                if (!vs[s]) v0 = 0.0f;
+                if (!vs[s + 1]) v1 = 0.0f;
+            }
+            const __half2 hi = __floats2half2_rn(v0, v1);
+            const float2 hf = __half22float2(hi);
+            const __half2 lo = __floats2half2_rn(__fsub_rn(v0, hf.x), __fsub_rn(v1, hf.y));
+            *(uint32_t*)(sB + (b & 1) * B_BYTES + k4_off(nn, s)) = h2_bits(hi);
+            *(uint32_t*)(sB + (b & 1) * B_BYTES + k4_off(NB + nn, s)) = h2_bits(lo);
         }
-        const __half2 hi = __floats2half2_rn(v0, v1);
-        const float2 hf = __half22float2(hi);
-        const __half2 lo = __floats2half2_rn(__fsub_rn(v0, hf.x), __fsub_rn(v1, hf.y));
-        *(uint32_t*)(sB + (b & 1) * B_BYTES + k4_off(nn, s)) = h2_bits(hi);
-        *(uint32_t*)(sB + (b & 1) * B_BYTES + k4_off(NB + nn, s)) = h2_bits(lo);
     };
     // batch b's A operand: this unit's factors, one K-step (16 samples, 8 TMEM columns) at a time
     auto agen = [&](int b) {
@@ -525,12 +529,15 @@ void iter_tc_debug_withhold(int group, uint32_t wait_limit) {
     t_wait_limit = wait_limit;
 }
 
+// Units per CTA: four 128-unit M tiles, three for D >= 32 (wider B operand, so wider accumulators).
+int iter_tc_units(int d) { return d + 1 <= 32 ? 512 : 384; }
+
 // Table rows of the CTA with the most: 2 per grid row that its units touch, plus its grid columns.
-int64_t iter_tc_table_rows(int64_t rows, int64_t cols) {
+int64_t iter_tc_table_rows(int64_t rows, int64_t cols, int units) {
     const int64_t m = rows * cols;
     int64_t best = 0;
-    for (int64_t u0 = 0; u0 < m; u0 += K4_UNITS) {
-        const int64_t ul = std::min<int64_t>(u0 + K4_UNITS, m) - 1;
+    for (int64_t u0 = 0; u0 < m; u0 += units) {
+        const int64_t ul = std::min<int64_t>(u0 + units, m) - 1;
         const int64_t nrow = ul / cols - u0 / cols + 1;
         const int64_t ncol = nrow > 1 ? cols : ul % cols - u0 % cols + 1;
         best = std::max<int64_t>(best, 2 * nrow + ncol);
@@ -540,7 +547,7 @@ int64_t iter_tc_table_rows(int64_t rows, int64_t cols) {
 
 bool iter_tc_shape_ok(int64_t rows, int64_t cols, int d) {
     return d >= 1 && d + 1 <= K4_NB_MAX && rows >= 1 && cols >= 1 && rows * cols <= ((int64_t)1 << 26) &&
-           iter_tc_table_rows(rows, cols) <= K4_TAB_MAX;
+           iter_tc_table_rows(rows, cols, iter_tc_units(d)) <= K4_TAB_MAX;
 }
 
 int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_t n, int d, const float* topo,
@@ -548,7 +555,8 @@ int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_
                    const float* bounds, double* num, double* den, unsigned int* status, cudaStream_t stream) {
     if (n == 0) return SOMGB_OK;
     const int64_t m = rows * cols;
-    const int64_t tiles = ceil_div(m, K4_UNITS);
+    const int units = iter_tc_units(d);
+    const int64_t tiles = ceil_div(m, units);
     int64_t chunks = std::max<int64_t>(1, num_sms() / tiles);
     const int64_t chunk = ceil_div(std::max<int64_t>(K4_SB, ceil_div(n, chunks)), K4_SB) * K4_SB;
     chunks = ceil_div(n, chunk);
@@ -568,17 +576,19 @@ int launch_iter_tc(const float* x, const double* rho, const int32_t* bmu, int64_
     t_withhold_group = -1;   // one-shot
     t_wait_limit = 0;
     if (!P.gstatus) return set_error(SOMGB_ERR_CUDA, "device status word unavailable");
-    const int64_t ntab = iter_tc_table_rows(rows, cols);
+    const int64_t ntab = iter_tc_table_rows(rows, cols, units);
     // at least 120 KB, so that one CTA (which holds all 512 TMEM columns) is resident per SM
     const size_t smem = std::max<size_t>(
         2 * K4_B_MAX + 2 * (size_t)(ntab + 1) * K4_TPAD * 4 + 2 * (size_t)K4_SB * d * 4 + (size_t)ntab * 4, 120 * 1024);
-    auto kern = d <= 7    ? k4_iter_kernel<7, 16>
-                : d <= 15 ? k4_iter_kernel<15, 16>
-                : d <= 16 ? k4_iter_kernel<16, 32>
-                : d <= 23 ? k4_iter_kernel<23, 32>
-                          : k4_iter_kernel<31, 32>;
+    auto kern = d <= 7    ? k4_iter_kernel<7, 16, 4>
+                : d <= 15 ? k4_iter_kernel<15, 16, 4>
+                : d <= 16 ? k4_iter_kernel<16, 32, 4>
+                : d <= 23 ? k4_iter_kernel<23, 32, 4>
+                : d <= 31 ? k4_iter_kernel<31, 32, 4>
+                : d <= 39 ? k4_iter_kernel<39, 48, 3>
+                          : k4_iter_kernel<47, 48, 3>;
     SOMGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<dim3((unsigned)tiles, (unsigned)chunks), K4_THREADS, smem, stream>>>(P);
+    kern<<<dim3((unsigned)tiles, (unsigned)chunks), units, smem, stream>>>(P);
     SOMGB_LAUNCH_CHECK();
     return SOMGB_OK;
 }

@@ -23,10 +23,11 @@ unsigned int* device_status_word();
 // True on an sm_103 device (the tensor-core kernels' target).
 bool device_has_tc();
 
-// K4: the iteration-mode contraction on the tensor cores (k4_iter_tc.cu). Shape limits (host-only check): D <= 31 and
-// at most 640 exponential-table rows per 512-unit tile of the grid.
+// K4: the iteration-mode contraction on the tensor cores (k4_iter_tc.cu). Shape limits (host-only check): D <= 47 and
+// at most 320 exponential-table rows per unit tile of the grid (512 units, 384 for D >= 32).
 bool iter_tc_shape_ok(int64_t rows, int64_t cols, int d);
-int64_t iter_tc_table_rows(int64_t rows, int64_t cols);
+int iter_tc_units(int d);
+int64_t iter_tc_table_rows(int64_t rows, int64_t cols, int units);
 // num[u, :] += sum_i h_iu rho_i x_i, den[u] += sum_i h_iu rho_i over the samples with bmu[i] >= 0 (iteration-mode
 // neighbourhood of sample cur_vector + i), `bounds` from launch_feature_bounds over the same samples.
 // Test hook: the next K4 launch on this thread never signals that accumulator group `group` is complete and bounds its

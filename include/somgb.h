@@ -246,7 +246,7 @@ int somgb_train_iter_pass(const float* x, const double* rho, int64_t n, int d, c
  * The same on the reference's square and hexagonal grids (unit i * cols + j of a rows x cols map, topography as the
  * reference builds it), with the neighbourhood factor split by grid axis; BMUs by `algo` (workspace:
  * somgb_workspace_bytes(SOMGB_OP_EPOCH, n, m, d, algo)). D <= 64. SOMGB_ALGO_TC, and SOMGB_ALGO_AUTO when n * m >=
- * 2^22, contract on the tensor cores for D <= 31 (split-FP16 products, float32 accumulation of 64 samples, folded
+ * 2^22, contract on the tensor cores for D <= 47 (split-FP16 products, float32 accumulation of 64 samples, folded
  * into compensated float32 sums, then float64); otherwise the sums are float32 per batch of 32 samples on the CUDA
  * cores, folded into float64. Both agree with somgb_train_iter_pass to ~1e-6 relative. A bounded wait of the
  * tensor-core contraction that gives up sets bit 65536 of the workspace's and the device's status words.

@@ -139,10 +139,13 @@ def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
     (20, 17, 5, 'square', 'auto', 60_000), (1, 300, 3, 'hexagonal', 'auto', 20_000),
     (80, 80, 8, 'hexagonal', 'tc', 8_000), (2, 300, 4, 'square', 'tc', 10_000), (64, 64, 31, 'square', 'auto', 10_000),
     (32, 32, 16, 'square', 'tc', 37), (32, 32, 4, 'square', 'tc', 64), (40, 40, 20, 'square', 'auto', 10_000),
-    # the float32 CUDA-core pass: the FP32 algorithm, D = 32 (above the tensor-core contraction's limit), and grid rows
+    # D = 32 to 47: three M tiles per CTA
+    (64, 64, 32, 'square', 'tc', 15_000), (30, 30, 40, 'hexagonal', 'auto', 8_000),
+    # the float32 CUDA-core pass: the FP32 algorithm, D above the tensor-core contraction's limit of 47, and grid rows
     # too long for the tensor-core contraction's tables
     (32, 32, 16, 'hexagonal', 'fp32', 60_000), (20, 17, 5, 'square', 'fp32', 60_000),
-    (64, 64, 32, 'square', 'auto', 15_000), (1, 9, 3, 'hexagonal', 'fp32', 60_000), (3, 700, 4, 'square', 'tc', 10_000)])
+    (32, 32, 32, 'square', 'fp32', 20_000), (20, 20, 50, 'square', 'auto', 8_000),
+    (1, 9, 3, 'hexagonal', 'fp32', 60_000), (3, 700, 4, 'square', 'tc', 10_000)])
 def test_grid_iteration_pass_matches_the_float64_pass(cuda, native, oracle, m, n, d, topology, algo, N):
     """Iteration mode: the grid-factorised pass (somgb_train_iter_pass_grid; the tensor-core contraction for the TC
     algorithm, the float32 CUDA-core pass otherwise) against the float64 pass over an arbitrary topography
