@@ -139,6 +139,8 @@ def test_a_wait_that_runs_out_fails_only_its_own_call(cuda, native):
     (20, 17, 5, 'square', 'auto', 60_000), (1, 300, 3, 'hexagonal', 'auto', 20_000),
     (80, 80, 8, 'hexagonal', 'tc', 8_000), (2, 300, 4, 'square', 'tc', 10_000), (64, 64, 31, 'square', 'auto', 10_000),
     (32, 32, 16, 'square', 'tc', 37), (32, 32, 4, 'square', 'tc', 64), (40, 40, 20, 'square', 'auto', 10_000),
+    # a single grid column
+    (100, 1, 4, 'square', 'tc', 20_000),
     # D = 32 to 47: three M tiles per CTA
     (64, 64, 32, 'square', 'tc', 15_000), (30, 30, 40, 'hexagonal', 'auto', 8_000),
     # the float32 CUDA-core pass: the FP32 algorithm, D above the tensor-core contraction's limit of 47, and grid rows
