@@ -51,8 +51,15 @@ class _Slot:
 
     def __init__(self, torch, device):
         self.stream = torch.cuda.Stream(device=device)
+        self.copy_stream = torch.cuda.Stream(device=device)   # uploads of large requests, piece by piece
         self.stage = None   # pinned host staging buffer for packed requests
         self.out = None     # pinned host buffer for packed results
+
+
+# A single request from pinned host memory of at least PIECE_MIN rows is uploaded in PIECES pieces on the worker's copy
+# stream, and the BMU pass of piece p runs while piece p + 1 is copied.
+PIECE_MIN = 1 << 21
+PIECES = 4
 
 
 class GpuExecutor:
@@ -117,9 +124,24 @@ class GpuExecutor:
         counts = [_rows(x) for x in xs]
         n = sum(counts)
         hist = hist or [False] * len(xs)
+        pieces = None
         with torch.cuda.stream(sl.stream):
             one = xs[0] if len(xs) == 1 and isinstance(xs[0], torch.Tensor) else None
-            if one is not None and (one.is_cuda or one.is_pinned()):
+            if one is not None and not one.is_cuda and one.is_pinned() and one.dtype == torch.float32 and \
+                    one.is_contiguous() and n >= PIECE_MIN:
+                # pinned host rows: copied in pieces on the copy stream, each piece's pass as soon as it has landed
+                xd = torch.empty((n, D), dtype=torch.float32, device=self.device)
+                bounds = [n * p // PIECES for p in range(PIECES + 1)]
+                pieces = []
+                for p in range(PIECES):
+                    r0, r1 = bounds[p], bounds[p + 1]
+                    done = torch.cuda.Event()
+                    with torch.cuda.stream(sl.copy_stream):
+                        sl.copy_stream.wait_stream(sl.stream)   # xd is allocated on the worker's stream
+                        xd[r0:r1].copy_(one[r0:r1], non_blocking=True)
+                        done.record(sl.copy_stream)
+                    pieces.append((r0, r1, done))
+            elif one is not None and (one.is_cuda or one.is_pinned()):
                 # device tensor, or pinned host memory: no staging copy
                 xd = one.to(device=self.device, dtype=torch.float32, non_blocking=True).contiguous()
             else:
@@ -134,10 +156,19 @@ class GpuExecutor:
             out = torch.empty(n, dtype=torch.int32, device=self.device)
             nh = sum(1 for h in hist if h)
             hd = torch.zeros((max(nh, 1), M), dtype=torch.float64, device=self.device) if nh else None
+            status = torch.zeros(1, dtype=torch.int32, device=self.device)
             if n:
-                wsp, wsb = entry['ws'][slot].for_op(nat.OP_FIND_BMUS, n, M, D, entry['algo'], self.device)
-                nat.call('somgb_find_bmus', xd.data_ptr(), n, D, entry['w'].data_ptr(), M, entry['algo'],
-                         out.data_ptr(), wsp, wsb, sl.stream.cuda_stream)
+                ws = entry['ws'][slot]
+                if pieces is None:
+                    pieces = [(0, n, None)]
+                wsp, wsb = ws.for_op(nat.OP_FIND_BMUS, max(r1 - r0 for r0, r1, _ in pieces), M, D, entry['algo'],
+                                     self.device)
+                for r0, r1, done in pieces:
+                    if done is not None:
+                        sl.stream.wait_event(done)
+                    nat.call('somgb_find_bmus', xd[r0:].data_ptr(), r1 - r0, D, entry['w'].data_ptr(), M,
+                             entry['algo'], out[r0:].data_ptr(), wsp, wsb, sl.stream.cuda_stream)
+                    ws.note_status(status)   # each pass clears the word when it starts
                 r, k = 0, 0
                 for c, h in zip(counts, hist):
                     if h:
@@ -152,7 +183,7 @@ class GpuExecutor:
                 hh = ob[n * 4 + (-(n * 4)) % 8:][:nh * M * 8].view(torch.float64).view(nh, M)
                 hh.copy_(hd[:nh], non_blocking=True)
         sl.stream.synchronize()
-        if n and int(entry['ws'][slot].status_word().item()):
+        if n and int(status.item()):
             # a bounded wait of this pass gave up: this batch fails, and no other (the word is this workspace's)
             raise nat.SomgbError(nat.SOMGB_ERR_TIMEOUT, 'a device-side wait gave up; the pass returned early')
         res = oh.numpy().copy()

@@ -369,3 +369,37 @@ def test_served_results_match_the_direct_calls(cuda):
         ft = srv.submit_train(a, x[:50_000], n_epochs=3)
         b.train(x[:50_000], n_epochs=3)
         assert np.array_equal(ft.result(120).weights, b.weights)
+
+
+@pytest.mark.gpu
+def test_a_large_pinned_request_is_served_in_pieces(cuda):
+    """A request of pinned host rows above serve.PIECE_MIN is uploaded in pieces, each piece's BMU pass running as soon
+    as it has landed: the BMUs and the histogram equal the direct calls, and a bounded wait that runs out in the first
+    piece's pass fails the request although the later passes clear their workspace's status word."""
+    import ctypes
+    import torch
+    import decontamination_gb300 as dg
+    from decontamination_gb300 import synthetic, serve, _native
+    from decontamination_gb300.serve import GpuExecutor
+    n = serve.PIECE_MIN + 300_001
+    x = synthetic.gaussian_mixture(n, 16, 7)
+    som = dg.SOM_Batch(32, 32, 16, topology='square')
+    som._weights[...] = x[np.random.default_rng(3).integers(0, n, 1024)].reshape(som._weights.shape)
+    som.bmu_algo = 'tc'
+    xp = torch.from_numpy(x).pin_memory()
+    want = som.get_winners(x)
+    ex = GpuExecutor(workers=2)
+    entry = ex.load(som)
+    b, h = ex.run_bmu(entry, [xp], slot=1, hist=[True])[0]
+    assert np.array_equal(b, want)
+    assert np.array_equal(h, np.bincount(want, minlength=1024).astype(np.float64))
+    _native.call('somgb_debug_tc_withhold', 3, 20_000)   # this thread's next pass: the first piece's
+    with pytest.raises(_native.SomgbError) as ei:
+        ex.run_bmu(entry, [xp], slot=0)
+    assert ei.value.status == _native.SOMGB_ERR_TIMEOUT
+    assert np.array_equal(ex.run_bmu(entry, [xp], slot=0)[0], want)
+    with SomServer() as srv:   # and through the request loop
+        mid = srv.add_map(som)
+        assert np.array_equal(srv.submit_bmu(mid, xp).result(120), want)
+    st = ctypes.c_uint(0)
+    _native.call('somgb_device_status', ctypes.addressof(st), 1, torch.cuda.current_stream().cuda_stream)
