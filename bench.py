@@ -28,6 +28,7 @@ time.
 """
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -713,6 +714,7 @@ def gpu_arm(args, ws, rank, local):
         for _ in range(2):                                      # warm-up (allocations, library state)
             som._weights[...] = w0
             som.train(xh, n_epochs=1, use_best_epoch=False)
+        gc.collect()   # no pending collection of the earlier records' objects lands in the timed calls
         barrier()
         t0 = time.perf_counter()
         calls = []
