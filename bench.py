@@ -711,7 +711,7 @@ def gpu_arm(args, ws, rank, local):
         som = dg.SOM_Batch(w['m'], w['n'], D, topology=w['topology'], sigma=w['sigma0'])
         som.bmu_algo = args.algo
         e2e_steps = max(1, min(args.steps, 5))
-        for _ in range(2):                                      # warm-up (allocations, library state)
+        for _ in range(3):                                      # warm-up (allocations, library state)
             som._weights[...] = w0
             som.train(xh, n_epochs=1, use_best_epoch=False)
         gc.collect()   # no pending collection of the earlier records' objects lands in the timed calls
